@@ -1,0 +1,1023 @@
+// capi.cu -- the C ABI (include/fans_gb300.h): context, setup and the solve
+// loops of SolverCG / SolverFP (solverCG.h:62-117, solverFP.h:33-52) driving
+// the fused sm_103a kernels.  Host code only orchestrates; every per-voxel
+// operation runs on the GPU.
+#include "../../include/fans_gb300.h"
+#include "fe_host.hpp"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace fansgpu;
+
+static std::string g_create_error;
+
+struct fansgpu_ctx {
+    fansgpu_desc desc{};
+    Grid3        g{};
+    int          C = 1, nstr = 3, ngp = 8;
+    long long    N = 0, n = 0;
+    double       le[3]{}, ve = 0;
+    std::vector<double> B, Bbar;
+
+    // materials
+    int                              nph = 0; // phases in the table: max(1 + max id in ms, assigned)
+    int                              ms_max = 0;
+    std::vector<int>                 law;
+    std::vector<std::vector<double>> prm;
+    std::vector<char>                assigned;
+    bool have_ms = false, have_ref = false, tables_dirty = true, force_dirty = true, green_dirty = true;
+    bool all_linear = true;
+    std::vector<double> kapparef, g0;
+    fansgpu_tol tol{FANSGPU_L2, FANSGPU_RELATIVE, 1e-10, 100, 5, 1e-2};
+    double      reliable_delta = 1e-2; // MIXED: true-residual refresh when the FP32 residual fell by this factor
+
+    cudaStream_t st = nullptr;
+    cudaEvent_t  ev0 = nullptr, ev1 = nullptr;
+    uint8_t     *d_ms = nullptr;
+    double *u = nullptr, *r = nullptr, *s = nullptr, *dd[2] = {nullptr, nullptr}, *Kd = nullptr, *uprev = nullptr;
+    float  *r32 = nullptr, *s32 = nullptr, *d32[2] = {nullptr, nullptr}, *Kd32 = nullptr;
+    double *K64 = nullptr, *f64 = nullptr, *Cph = nullptr, *Bbar_d = nullptr, *g0_d = nullptr, *K0c = nullptr;
+    float  *K32 = nullptr;
+    double *G64 = nullptr;
+    float  *G32 = nullptr;
+    cplx<double> *spec64 = nullptr, *tw64 = nullptr;
+    cplx<float>  *spec32 = nullptr, *tw32 = nullptr;
+    double       *trig = nullptr; // cos/sin tables for the Green's table
+    double       *staging = nullptr;
+    CgScalars    *scal = nullptr, *scal_h = nullptr;
+    GridRed       red{};
+    double       *red_out = nullptr;
+    ConvPlan<double> cp64{};
+    ConvPlan<float>  cp32{};
+    int              cur_d = 0;
+
+    std::vector<double> err_all;
+    int                 iter = 0;
+    std::string         err_msg;
+};
+
+namespace fansgpu {
+int fail(fansgpu_ctx *ctx, int code, const char *fmt, ...)
+{
+    char    buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx)
+        ctx->err_msg = buf;
+    else
+        g_create_error = buf;
+    return code;
+}
+} // namespace fansgpu
+
+namespace {
+
+constexpr int kMaxBlocks = 152 * 16;
+constexpr int kRedSites  = 16;
+enum { SITE_NORM = 0, SITE_CONV = 1, SITE_STENCIL = 2, SITE_UPDATE = 3, SITE_SS = 4 };
+
+template <typename P>
+int dalloc(fansgpu_ctx *ctx, P **p, size_t count)
+{
+    cudaError_t e = cudaMalloc((void **)p, sizeof(P) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(ctx, FANSGPU_ENOMEM, "cudaMalloc of %zu bytes failed: %s", sizeof(P) * count,
+                    cudaGetErrorString(e));
+    }
+    return 0;
+}
+
+int nstr_of(int C) { return C == 1 ? 3 : 6; }
+
+// Largest grid of any kernel that commits reduction partials.
+long long max_reduction_blocks(const Grid3 &g, int C)
+{
+    long long b = std::max<long long>(kMaxBlocks, stencil_blocks(g));
+    b           = std::max<long long>(b, (long long)C * g.nx * g.ny); // z passes: at least one row per CTA
+    return b;
+}
+
+// Twiddle tables of one precision: [x: nx][y: ny][z: M][r2c: M+1].
+template <typename T>
+void make_twiddles(const Grid3 &g, std::vector<cplx<T>> &out)
+{
+    const int    M   = g.nz / 2;
+    const double tpi = 2.0 * std::acos(-1.0);
+    out.clear();
+    auto push = [&](int n, int count) {
+        for (int q = 0; q < count; ++q)
+            out.push_back(cplx<T>{(T)std::cos(tpi * q / n), (T)(-std::sin(tpi * q / n))});
+    };
+    push(g.nx, g.nx);
+    push(g.ny, g.ny);
+    push(M, M);
+    push(g.nz, M + 1);
+}
+
+template <typename T>
+int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G)
+{
+    const Grid3 &g = ctx->g;
+    p.g            = g;
+    p.C            = ctx->C;
+    p.M            = g.nz / 2;
+    p.nzh          = g.nz / 2 + 1;
+    p.nzp          = ((p.nzh + 15) / 16) * 16;
+    p.dx.n         = g.nx;
+    p.dy.n         = g.ny;
+    p.dz.n         = p.M;
+    if (!fe::radix_plan(g.nx, p.dx.rad, &p.dx.nrad, kMaxRadices) ||
+        !fe::radix_plan(g.ny, p.dy.rad, &p.dy.nrad, kMaxRadices) ||
+        !fe::radix_plan(p.M, p.dz.rad, &p.dz.nrad, kMaxRadices))
+        return fail(ctx, FANSGPU_EUNSUPPORTED, "grid %dx%dx%d: FFT lengths need prime factors <= 13", g.nx, g.ny,
+                    g.nz);
+    p.tw_x   = tw;
+    p.tw_y   = tw + g.nx;
+    p.tw_z   = tw + g.nx + g.ny;
+    p.tw_r2c = tw + g.nx + g.ny + p.M;
+    p.spec   = spec;
+    p.G      = G;
+    const size_t cs = sizeof(cplx<T>), budget = 100 * 1024;
+    int          kc = 16;
+    while (kc > 1 && cs * (2 * (size_t)g.ny * kc + g.ny) > budget)
+        kc /= 2;
+    p.kc_y = kc;
+    kc     = 16;
+    while (kc > 1 && cs * (2 * (size_t)p.C * g.nx * kc + g.nx) > budget)
+        kc /= 2;
+    p.kc_x = kc;
+    if (cs * (2 * (size_t)p.C * g.nx * p.kc_x + g.nx) > 200 * 1024)
+        return fail(ctx, FANSGPU_EUNSUPPORTED, "n_x=%d too large for the shared-memory x pass", g.nx);
+    return 0;
+}
+
+int sync_scalars(fansgpu_ctx *ctx)
+{
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->scal_h, ctx->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+// Per-phase tables, reference stiffness and Green's operator (lazy).
+int setup(fansgpu_ctx *ctx)
+{
+    if (!ctx->have_ms)
+        return fail(ctx, FANSGPU_ESTATE, "set_microstructure must be called before solving");
+    const int C = ctx->C, nstr = ctx->nstr, NC = 8 * C;
+    if (ctx->tables_dirty) {
+        const int nph = std::max(ctx->ms_max + 1, (int)ctx->law.size());
+        if (nph > 16)
+            return fail(ctx, FANSGPU_EUNSUPPORTED, "%d phases: at most 16 phases per context in this build", nph);
+        ctx->law.resize(nph, -1);
+        ctx->prm.resize(nph);
+        ctx->assigned.resize(nph, 0);
+        for (int ph = 0; ph < nph; ++ph)
+            if (!ctx->assigned[ph])
+                return fail(ctx, FANSGPU_EINVAL, "MaterialManager: Phase %d not assigned", ph);
+        if (nph != ctx->nph) {
+            void *old[] = {ctx->K64, ctx->K32, ctx->f64, ctx->Cph};
+            for (void *p : old)
+                if (p)
+                    cudaFree(p);
+            ctx->K64 = ctx->f64 = ctx->Cph = nullptr;
+            ctx->K32                       = nullptr;
+            ctx->nph                       = 0;
+            int rc;
+            if ((rc = dalloc(ctx, &ctx->K64, (size_t)nph * NC * NC)) ||
+                (rc = dalloc(ctx, &ctx->K32, (size_t)nph * NC * NC)) || (rc = dalloc(ctx, &ctx->f64, (size_t)nph * NC)) ||
+                (rc = dalloc(ctx, &ctx->Cph, (size_t)nph * nstr * nstr)))
+                return rc;
+            ctx->nph = nph;
+        }
+        ctx->all_linear = true;
+        std::vector<double> K64(ctx->nph * NC * NC), Cph(ctx->nph * nstr * nstr), Ke;
+        std::vector<float>  K32(ctx->nph * NC * NC);
+        for (int ph = 0; ph < ctx->nph; ++ph) {
+            if (ctx->law[ph] == FANSGPU_LAW_J2_LINEAR)
+                ctx->all_linear = false;
+            if (!fe::law_C(ctx->law[ph], ctx->prm[ph], nstr, &Cph[ph * nstr * nstr]))
+                return fail(ctx, FANSGPU_EINVAL, "phase %d: law %d does not fit problem with n_str=%d", ph,
+                            ctx->law[ph], nstr);
+            fe::element_stiffness(C, ctx->ngp, ctx->B, &Cph[ph * nstr * nstr], ctx->ve, Ke);
+            for (int i = 0; i < NC * NC; ++i) {
+                K64[ph * NC * NC + i] = Ke[i];
+                K32[ph * NC * NC + i] = (float)Ke[i];
+            }
+        }
+        if (!ctx->all_linear)
+            return fail(ctx, FANSGPU_EUNSUPPORTED,
+                        "J2PlasticityNew (nonlinear CG with secant line search) is not in this build yet");
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->K64, K64.data(), sizeof(double) * K64.size(), cudaMemcpyHostToDevice, ctx->st));
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->K32, K32.data(), sizeof(float) * K32.size(), cudaMemcpyHostToDevice, ctx->st));
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Cph, Cph.data(), sizeof(double) * Cph.size(), cudaMemcpyHostToDevice, ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        ctx->tables_dirty = false;
+        ctx->force_dirty  = true;
+    }
+    if (ctx->green_dirty) {
+        if (!ctx->have_ref)
+            return fail(ctx, FANSGPU_ESTATE, "set_reference (kapparef_mat) must be called before solving");
+        std::vector<double> K0n, K0c;
+        fe::element_stiffness(C, ctx->ngp, ctx->B, ctx->kapparef.data(), ctx->ve, K0n);
+        fe::to_component_major(C, K0n, K0c);
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->K0c, K0c.data(), sizeof(double) * K0c.size(), cudaMemcpyHostToDevice, ctx->st));
+        const Grid3 &g = ctx->g;
+        const int    nzh = g.nz / 2 + 1;
+        GreenArgs    ga{};
+        ga.g   = g;
+        ga.C   = C;
+        ga.K0c = ctx->K0c;
+        ga.cx  = ctx->trig;
+        ga.sx  = ga.cx + g.nx;
+        ga.cy  = ga.sx + g.nx;
+        ga.sy  = ga.cy + g.ny;
+        ga.cz  = ga.sy + g.ny;
+        ga.sz  = ga.cz + nzh;
+        ga.G64 = ctx->G64;
+        ga.G32 = ctx->G32;
+        FANS_CUDA_CHECK(launch_green(ga, ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        ctx->green_dirty = false;
+    }
+    if (ctx->force_dirty) {
+        std::vector<double> f(ctx->nph * NC);
+        std::vector<double> Cm(nstr * nstr);
+        for (int ph = 0; ph < ctx->nph; ++ph) {
+            fe::law_C(ctx->law[ph], ctx->prm[ph], nstr, Cm.data());
+            fe::element_force(C, ctx->ngp, ctx->B, Cm.data(), ctx->g0.data(), ctx->ve, &f[ph * NC]);
+        }
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->f64, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice, ctx->st));
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->g0_d, ctx->g0.data(), sizeof(double) * nstr, cudaMemcpyHostToDevice, ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        ctx->force_dirty = false;
+    }
+    return 0;
+}
+
+// y = K x (+F) in FP64 (optionally FP32), no fusion.
+template <typename T>
+int run_stencil(fansgpu_ctx *ctx, const T *x, T *y, bool with_f)
+{
+    StencilArgs a{};
+    a.g      = ctx->g;
+    a.C      = ctx->C;
+    a.x      = x;
+    a.y      = y;
+    a.ms     = ctx->d_ms;
+    a.Kph    = std::is_same<T, double>::value ? (const void *)ctx->K64 : (const void *)ctx->K32;
+    a.fph    = with_f ? ctx->f64 : nullptr;
+    a.nph    = ctx->nph;
+    a.scal   = ctx->scal;
+    a.red    = ctx->red;
+    a.red_site = SITE_STENCIL;
+    FANS_CUDA_CHECK(launch_stencil<T>(a, ctx->st));
+    return 0;
+}
+
+int init_scalars(fansgpu_ctx *ctx)
+{
+    CgScalars s{};
+    s.delta    = 1.0; // solverCG.h:82
+    s.deltamid = 0.0;
+    s.beta     = 0.0;
+    *ctx->scal_h = s;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->scal, ctx->scal_h, sizeof(CgScalars), cudaMemcpyHostToDevice, ctx->st));
+    return 0;
+}
+
+double err_value(fansgpu_ctx *ctx, double err)
+{
+    // Solver::compute_error return value (solver.h:432-451)
+    if (ctx->tol.type == FANSGPU_ABSOLUTE)
+        return err;
+    return ctx->iter == 0 ? 100.0 : err / ctx->err_all[0];
+}
+
+// FP64 flexible CG (SolverCG::internalSolve, linear branch).
+int solve_cg64(fansgpu_ctx *ctx)
+{
+    const long long n = ctx->n;
+    int             rc;
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s, 0, sizeof(double) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->dd[0], 0, sizeof(double) * n, ctx->st));
+    ctx->cur_d = 0;
+    if ((rc = init_scalars(ctx)))
+        return rc;
+    // r = R(u) (compute_residual<2>, solverCG.h:76)
+    if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+        return rc;
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
+                                               SITE_NORM, ctx->st));
+    if ((rc = sync_scalars(ctx)))
+        return rc;
+    ctx->iter = 0;
+    ctx->err_all.assign(1, ctx->scal_h->err);
+    double err_rel = err_value(ctx, ctx->scal_h->err);
+    while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
+        ConvArgs ca{ctx->r, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+        FANS_CUDA_CHECK(launch_convolution<double>(ctx->cp64, ca, ctx->st));
+        StencilArgs sa{};
+        sa.g        = ctx->g;
+        sa.C        = ctx->C;
+        sa.x        = ctx->s;
+        sa.d_old    = ctx->dd[ctx->cur_d];
+        sa.d_new    = ctx->dd[ctx->cur_d ^ 1];
+        sa.y        = ctx->Kd;
+        sa.ms       = ctx->d_ms;
+        sa.Kph      = ctx->K64;
+        sa.nph      = ctx->nph;
+        sa.fuse_d   = 1;
+        sa.reduce   = 1;
+        sa.scal     = ctx->scal;
+        sa.red      = ctx->red;
+        sa.red_site = SITE_STENCIL;
+        FANS_CUDA_CHECK(launch_stencil<double>(sa, ctx->st));
+        ctx->cur_d ^= 1;
+        UpdateArgs ua{n, ctx->r, ctx->Kd, ctx->u, ctx->dd[ctx->cur_d], ctx->s, ctx->tol.measure, 1, ctx->scal,
+                      ctx->red, SITE_UPDATE};
+        FANS_CUDA_CHECK((launch_cg_update<double, double>(ua, ctx->st)));
+        if ((rc = sync_scalars(ctx)))
+            return rc;
+        ctx->iter++;
+        ctx->err_all.push_back(ctx->scal_h->err);
+        if (ctx->scal_h->converged < 0)
+            return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at iteration %d", ctx->iter);
+        err_rel = err_value(ctx, ctx->scal_h->err);
+    }
+    return 0;
+}
+
+// Mixed precision: FANS's flexible CG run on FP32 fields (stencil, FFT
+// preconditioner, recursive residual) with FP64 dot products, an FP64
+// solution and reliable updates -- the true residual R(u) recomputed in FP64
+// whenever the FP32 residual has dropped by `reliable_delta` since the last
+// refresh, and always before convergence is accepted.
+int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
+{
+    const long long n = ctx->n;
+    int             rc;
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s32, 0, sizeof(float) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->d32[0], 0, sizeof(float) * n, ctx->st));
+    ctx->cur_d = 0;
+    if ((rc = init_scalars(ctx)))
+        return rc;
+    if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+        return rc;
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, ctx->r32, ctx->red,
+                                               SITE_NORM, ctx->st));
+    if ((rc = sync_scalars(ctx)))
+        return rc;
+    ctx->iter = 0;
+    ctx->err_all.assign(1, ctx->scal_h->err);
+    *refinements      = 0;
+    double err_rel    = err_value(ctx, ctx->scal_h->err);
+    double last_true  = ctx->scal_h->err;
+    while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
+        ConvArgs ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+        FANS_CUDA_CHECK(launch_convolution<float>(ctx->cp32, ca, ctx->st));
+        StencilArgs sa{};
+        sa.g        = ctx->g;
+        sa.C        = ctx->C;
+        sa.x        = ctx->s32;
+        sa.d_old    = ctx->d32[ctx->cur_d];
+        sa.d_new    = ctx->d32[ctx->cur_d ^ 1];
+        sa.y        = ctx->Kd32;
+        sa.ms       = ctx->d_ms;
+        sa.Kph      = ctx->K32;
+        sa.nph      = ctx->nph;
+        sa.fuse_d   = 1;
+        sa.reduce   = 1;
+        sa.scal     = ctx->scal;
+        sa.red      = ctx->red;
+        sa.red_site = SITE_STENCIL;
+        FANS_CUDA_CHECK(launch_stencil<float>(sa, ctx->st));
+        ctx->cur_d ^= 1;
+        UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->u, ctx->d32[ctx->cur_d], ctx->s32, ctx->tol.measure, 1, ctx->scal,
+                      ctx->red, SITE_UPDATE};
+        FANS_CUDA_CHECK((launch_cg_update<float, double>(ua, ctx->st)));
+        if ((rc = sync_scalars(ctx)))
+            return rc;
+        ctx->iter++;
+        if (ctx->scal_h->converged < 0)
+            return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at iteration %d", ctx->iter);
+        double est     = ctx->scal_h->err;
+        double est_rel = err_value(ctx, est);
+        if (est_rel <= ctx->tol.tolerance || est <= ctx->reliable_delta * last_true) {
+            // reliable update: true residual in FP64, re-seed the FP32 residual
+            if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+                return rc;
+            FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
+                                                       ctx->red, SITE_NORM, ctx->st));
+            if ((rc = sync_scalars(ctx)))
+                return rc;
+            (*refinements)++;
+            last_true = ctx->scal_h->err;
+            ctx->err_all.push_back(last_true);
+            err_rel = err_value(ctx, last_true);
+        } else {
+            ctx->err_all.push_back(est);
+            err_rel = std::max(est_rel, ctx->tol.tolerance * (1.0 + 1e-12)); // never accept an estimate
+        }
+    }
+    return 0;
+}
+
+// SolverFP::internalSolve: u -= G*r; r = R(u).
+int solve_fp64(fansgpu_ctx *ctx)
+{
+    const long long n = ctx->n;
+    int             rc;
+    if ((rc = init_scalars(ctx)))
+        return rc;
+    if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+        return rc;
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
+                                               SITE_NORM, ctx->st));
+    if ((rc = sync_scalars(ctx)))
+        return rc;
+    ctx->iter = 0;
+    ctx->err_all.assign(1, ctx->scal_h->err);
+    double err_rel = err_value(ctx, ctx->scal_h->err);
+    while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
+        ConvArgs ca{ctx->r, ctx->s, 1.0, 0, ctx->scal, ctx->red, SITE_CONV};
+        FANS_CUDA_CHECK(launch_convolution<double>(ctx->cp64, ca, ctx->st));
+        FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, ctx->s, -1.0, n, ctx->st));
+        if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+            return rc;
+        FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, nullptr, ctx->red,
+                                                   SITE_NORM, ctx->st));
+        if ((rc = sync_scalars(ctx)))
+            return rc;
+        ctx->iter++;
+        ctx->err_all.push_back(ctx->scal_h->err);
+        if (ctx->scal_h->converged < 0)
+            return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at iteration %d", ctx->iter);
+        err_rel = err_value(ctx, ctx->scal_h->err);
+    }
+    return 0;
+}
+
+int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *stress_f, double *out)
+{
+    StrainStressArgs a{};
+    a.g            = ctx->g;
+    a.C            = ctx->C;
+    a.nstr         = ctx->nstr;
+    a.u            = ctx->u;
+    a.ms           = ctx->d_ms;
+    a.Bbar         = ctx->Bbar_d;
+    a.Cph          = ctx->Cph;
+    a.g0           = ctx->g0_d;
+    a.nph          = ctx->nph;
+    a.phase_filter = phase_filter;
+    a.strain       = strain_f;
+    a.stress       = stress_f;
+    a.out_red      = ctx->red_out;
+    a.red          = ctx->red;
+    a.red_site     = SITE_SS;
+    FANS_CUDA_CHECK(launch_strain_stress(a, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(out, ctx->red_out, sizeof(double) * (2 * ctx->nstr + 1), cudaMemcpyDeviceToHost,
+                                    ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *fansgpu_version(void) { return "fans_gb300 0.1 (sm_103a)"; }
+
+const char *fansgpu_last_error(const fansgpu_ctx *ctx)
+{
+    return ctx ? ctx->err_msg.c_str() : g_create_error.c_str();
+}
+
+int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
+{
+    if (!desc || !out)
+        return fail(nullptr, FANSGPU_EINVAL, "fansgpu_create: null argument");
+    *out = nullptr;
+    const int *n = desc->n;
+    for (int i = 0; i < 3; ++i)
+        if (n[i] < 4 || n[i] > 1024 || (n[i] % 2) != 0)
+            return fail(nullptr, FANSGPU_EUNSUPPORTED, "grid dimension %d = %d: need an even size in [4, 1024]", i,
+                        n[i]);
+    if (desc->howmany != 1 && desc->howmany != 3)
+        return fail(nullptr, FANSGPU_EINVAL, "howmany must be 1 (thermal) or 3 (small-strain mechanics)");
+    if (desc->fe_type < 0 || desc->fe_type > 2)
+        return fail(nullptr, FANSGPU_EINVAL, "FE_type must be one of: 'HEX8', 'HEX8R', or 'BBAR'");
+    if (desc->precision != FANSGPU_FP64 && desc->precision != FANSGPU_MIXED)
+        return fail(nullptr, FANSGPU_EINVAL, "precision must be FANSGPU_FP64 or FANSGPU_MIXED");
+    if (desc->method != FANSGPU_CG && desc->method != FANSGPU_FP)
+        return fail(nullptr, FANSGPU_EINVAL, "method must be cg or fp");
+    if (desc->precision == FANSGPU_MIXED && desc->method != FANSGPU_CG)
+        return fail(nullptr, FANSGPU_EUNSUPPORTED, "mixed precision is implemented for the CG method");
+    for (int i = 0; i < 3; ++i)
+        if (!(desc->L[i] > 0))
+            return fail(nullptr, FANSGPU_EINVAL, "L must be positive");
+
+    fansgpu_ctx *ctx = new fansgpu_ctx();
+    ctx->desc        = *desc;
+    ctx->g           = Grid3{n[0], n[1], n[2]};
+    ctx->C           = desc->howmany;
+    ctx->nstr        = nstr_of(ctx->C);
+    ctx->N           = ctx->g.N();
+    ctx->n           = ctx->N * ctx->C;
+    for (int i = 0; i < 3; ++i)
+        ctx->le[i] = desc->L[i] / (double)n[i]; // reader.cpp:293-296
+    ctx->ve  = ctx->le[0] * ctx->le[1] * ctx->le[2];
+    ctx->ngp = fe::gauss_B(desc->fe_type, ctx->C, ctx->le, ctx->B);
+    const int NC = 8 * ctx->C, ns = ctx->nstr;
+    ctx->Bbar.assign(ns * NC, 0.0);
+    for (int gp = 0; gp < ctx->ngp; ++gp)
+        for (int i = 0; i < ns * NC; ++i)
+            ctx->Bbar[i] += ctx->B[gp * ns * NC + i] / ctx->ngp;
+    ctx->g0.assign(ns, 0.0);
+    ctx->kapparef.assign(ns * ns, 0.0);
+
+    int rc = 0;
+    auto bail = [&](int code) {
+        g_create_error = ctx->err_msg;
+        fansgpu_destroy(ctx);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        fail(ctx, FANSGPU_ECUDA, "no CUDA device/stream: %s", cudaGetErrorString(cudaGetLastError()));
+        return bail(FANSGPU_ECUDA);
+    }
+    const long long nn = ctx->n, N = ctx->N;
+    const int       nzh = ctx->g.nz / 2 + 1, nzp = ((nzh + 15) / 16) * 16, NT = ctx->C * (ctx->C + 1) / 2;
+    const long long F = (long long)ctx->g.nx * ctx->g.ny * nzh;
+    const long long nspec = (long long)ctx->C * ctx->g.nx * ctx->g.ny * nzp;
+    const bool      mixed = desc->precision == FANSGPU_MIXED;
+    if ((rc = dalloc(ctx, &ctx->d_ms, N)) || (rc = dalloc(ctx, &ctx->u, nn)) || (rc = dalloc(ctx, &ctx->r, nn)) ||
+        (rc = dalloc(ctx, &ctx->s, nn)) || (rc = dalloc(ctx, &ctx->dd[0], nn)) ||
+        (rc = dalloc(ctx, &ctx->dd[1], nn)) || (rc = dalloc(ctx, &ctx->Kd, nn)) ||
+        (rc = dalloc(ctx, &ctx->uprev, nn)) || (rc = dalloc(ctx, &ctx->spec64, nspec)) ||
+        (rc = dalloc(ctx, &ctx->G64, F * NT)) || (rc = dalloc(ctx, &ctx->staging, N * std::max(ctx->C, ns))) ||
+        (rc = dalloc(ctx, &ctx->scal, 1)) || (rc = dalloc(ctx, &ctx->red.partials, (size_t)max_reduction_blocks(ctx->g, ctx->C) * kMaxRed)) ||
+        (rc = dalloc(ctx, &ctx->red.counter, kRedSites)) || (rc = dalloc(ctx, &ctx->red_out, 64)) ||
+        (rc = dalloc(ctx, &ctx->K0c, NC * NC)) || (rc = dalloc(ctx, &ctx->Bbar_d, ns * NC)) ||
+        (rc = dalloc(ctx, &ctx->g0_d, ns)) ||
+        (rc = dalloc(ctx, &ctx->trig, 2 * (ctx->g.nx + ctx->g.ny + nzh))))
+        return bail(rc);
+    if (mixed) {
+        if ((rc = dalloc(ctx, &ctx->r32, nn)) || (rc = dalloc(ctx, &ctx->s32, nn)) ||
+            (rc = dalloc(ctx, &ctx->d32[0], nn)) || (rc = dalloc(ctx, &ctx->d32[1], nn)) ||
+            (rc = dalloc(ctx, &ctx->Kd32, nn)) || (rc = dalloc(ctx, &ctx->spec32, nspec)) ||
+            (rc = dalloc(ctx, &ctx->G32, F * NT)))
+            return bail(rc);
+    }
+    if (cudaMallocHost((void **)&ctx->scal_h, sizeof(CgScalars)) != cudaSuccess) {
+        fail(ctx, FANSGPU_ENOMEM, "pinned host allocation failed");
+        return bail(FANSGPU_ENOMEM);
+    }
+    cudaMemsetAsync(ctx->red.counter, 0, sizeof(unsigned) * kRedSites, ctx->st);
+    cudaMemsetAsync(ctx->u, 0, sizeof(double) * nn, ctx->st);
+    cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * nn, ctx->st);
+    cudaMemsetAsync(ctx->r, 0, sizeof(double) * nn, ctx->st);
+    cudaMemcpyAsync(ctx->Bbar_d, ctx->Bbar.data(), sizeof(double) * ns * NC, cudaMemcpyHostToDevice, ctx->st);
+    // trig tables for the Green's operator (solver.h:156-158)
+    {
+        std::vector<double> t;
+        const double        tpi = 2.0 * std::acos(-1.0);
+        auto                add = [&](int nn_, int count, bool sn) {
+            for (int k = 0; k < count; ++k)
+                t.push_back(sn ? std::sin(tpi * k / nn_) : std::cos(tpi * k / nn_));
+        };
+        add(ctx->g.nx, ctx->g.nx, false);
+        add(ctx->g.nx, ctx->g.nx, true);
+        add(ctx->g.ny, ctx->g.ny, false);
+        add(ctx->g.ny, ctx->g.ny, true);
+        add(ctx->g.nz, nzh, false);
+        add(ctx->g.nz, nzh, true);
+        cudaMemcpyAsync(ctx->trig, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, ctx->st);
+        std::vector<cplx<double>> tw;
+        make_twiddles<double>(ctx->g, tw);
+        if ((rc = dalloc(ctx, &ctx->tw64, tw.size())))
+            return bail(rc);
+        cudaMemcpyAsync(ctx->tw64, tw.data(), sizeof(cplx<double>) * tw.size(), cudaMemcpyHostToDevice, ctx->st);
+        if (mixed) {
+            std::vector<cplx<float>> tw32;
+            make_twiddles<float>(ctx->g, tw32);
+            if ((rc = dalloc(ctx, &ctx->tw32, tw32.size())))
+                return bail(rc);
+            cudaMemcpyAsync(ctx->tw32, tw32.data(), sizeof(cplx<float>) * tw32.size(), cudaMemcpyHostToDevice, ctx->st);
+        }
+        if (cudaStreamSynchronize(ctx->st) != cudaSuccess) {
+            fail(ctx, FANSGPU_ECUDA, "initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
+            return bail(FANSGPU_ECUDA);
+        }
+    }
+    if ((rc = make_plan<double>(ctx, ctx->cp64, ctx->spec64, ctx->tw64, ctx->G64)))
+        return bail(rc);
+    if (mixed && (rc = make_plan<float>(ctx, ctx->cp32, ctx->spec32, ctx->tw32, ctx->G32)))
+        return bail(rc);
+    *out = ctx;
+    return 0;
+}
+
+int fansgpu_destroy(fansgpu_ctx *ctx)
+{
+    if (!ctx)
+        return 0;
+    if (ctx->st)
+        cudaStreamSynchronize(ctx->st);
+    void *ptrs[] = {ctx->d_ms, ctx->u,    ctx->r,      ctx->s,      ctx->dd[0],  ctx->dd[1],      ctx->Kd,
+                    ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32,       ctx->K64,
+                    ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
+                    ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
+                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    if (ctx->scal_h)
+        cudaFreeHost(ctx->scal_h);
+    if (ctx->ev0)
+        cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1)
+        cudaEventDestroy(ctx->ev1);
+    if (ctx->st)
+        cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return 0;
+}
+
+int fansgpu_set_microstructure(fansgpu_ctx *ctx, const uint16_t *ms)
+{
+    if (!ctx || !ms)
+        return ctx ? fail(ctx, FANSGPU_EINVAL, "null microstructure") : FANSGPU_EINVAL;
+    std::vector<uint8_t> m8(ctx->N);
+    int                  mx = 0;
+    for (long long i = 0; i < ctx->N; ++i) {
+        if (ms[i] > 255)
+            return fail(ctx, FANSGPU_EUNSUPPORTED, "phase id %u > 255 at voxel %lld", (unsigned)ms[i], i);
+        m8[i] = (uint8_t)ms[i];
+        mx    = std::max(mx, (int)ms[i]);
+    }
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->d_ms, m8.data(), ctx->N, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    ctx->ms_max       = mx;
+    ctx->have_ms      = true;
+    ctx->tables_dirty = true;
+    return 0;
+}
+
+int fansgpu_set_phase_material(fansgpu_ctx *ctx, int32_t phase, int32_t law, const double *params, int32_t n_params)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (phase < 0 || phase > 255)
+        return fail(ctx, FANSGPU_EINVAL, "MaterialManager: Invalid or duplicate phase %d", phase);
+    if (law < 0 || law > 4 || !params || n_params < 1)
+        return fail(ctx, FANSGPU_EINVAL, "invalid material law %d / parameters", law);
+    const bool thermal = (law == FANSGPU_LAW_THERMAL_ISO || law == FANSGPU_LAW_THERMAL_TRI);
+    if (thermal != (ctx->C == 1))
+        return fail(ctx, FANSGPU_EINVAL, "law %d is not valid for a %s problem", law, ctx->C == 1 ? "thermal" : "mechanical");
+    const int need[5] = {1, 2, 4, 9, 36};
+    if (n_params < need[law])
+        return fail(ctx, FANSGPU_EINVAL, "law %d needs %d parameters, got %d", law, need[law], n_params);
+    for (int i = 0; i < need[law]; ++i)
+        if (!std::isfinite(params[i]))
+            return fail(ctx, FANSGPU_EINVAL, "non-finite material parameter %d of phase %d", i, phase);
+    if (phase >= (int)ctx->law.size()) {
+        ctx->law.resize(phase + 1, -1);
+        ctx->prm.resize(phase + 1);
+        ctx->assigned.resize(phase + 1, 0);
+    }
+    ctx->law[phase]      = law;
+    ctx->prm[phase]      = std::vector<double>(params, params + need[law]);
+    ctx->assigned[phase] = 1;
+    ctx->tables_dirty    = true;
+    return 0;
+}
+
+int fansgpu_set_reference(fansgpu_ctx *ctx, const double *kref)
+{
+    if (!ctx || !kref)
+        return ctx ? fail(ctx, FANSGPU_EINVAL, "null reference material") : FANSGPU_EINVAL;
+    const int ns = ctx->nstr;
+    for (int i = 0; i < ns * ns; ++i)
+        if (!std::isfinite(kref[i]))
+            return fail(ctx, FANSGPU_EINVAL, "reference_material has non-finite entries");
+    // LLT check as MaterialManager.h:189-192 (symmetric positive definite)
+    std::vector<double> L(ns * ns, 0.0);
+    for (int j = 0; j < ns; ++j) {
+        double d = kref[j * ns + j];
+        for (int k = 0; k < j; ++k)
+            d -= L[j * ns + k] * L[j * ns + k];
+        if (!(d > 0))
+            return fail(ctx, FANSGPU_EINVAL, "reference_material must be symmetric positive definite");
+        L[j * ns + j] = std::sqrt(d);
+        for (int i = j + 1; i < ns; ++i) {
+            double s = kref[i * ns + j];
+            for (int k = 0; k < j; ++k)
+                s -= L[i * ns + k] * L[j * ns + k];
+            L[i * ns + j] = s / L[j * ns + j];
+        }
+    }
+    ctx->kapparef.assign(kref, kref + ns * ns);
+    ctx->have_ref    = true;
+    ctx->green_dirty = true;
+    return 0;
+}
+
+int fansgpu_set_gradient(fansgpu_ctx *ctx, const double *g0)
+{
+    if (!ctx || !g0)
+        return ctx ? fail(ctx, FANSGPU_EINVAL, "null gradient") : FANSGPU_EINVAL;
+    for (int i = 0; i < ctx->nstr; ++i)
+        if (!std::isfinite(g0[i]))
+            return fail(ctx, FANSGPU_EINVAL, "non-finite macroscale loading component %d", i);
+    ctx->g0.assign(g0, g0 + ctx->nstr);
+    ctx->force_dirty = true;
+    return 0;
+}
+
+int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *t)
+{
+    if (!ctx || !t)
+        return FANSGPU_EINVAL;
+    if (t->measure < 0 || t->measure > 2)
+        return fail(ctx, FANSGPU_EINVAL, "Unknown measure type");
+    if (t->type < 0 || t->type > 1)
+        return fail(ctx, FANSGPU_EINVAL, "Unknown error type");
+    if (t->n_it < 0 || !(t->tolerance >= 0))
+        return fail(ctx, FANSGPU_EINVAL, "n_it >= 0 and tolerance >= 0 required");
+    if (t->ls_max_iter < 1 || !(t->ls_tol > 0))
+        return fail(ctx, FANSGPU_EINVAL, "linesearch_parameters: max_iter >= 1 and tol > 0 required");
+    ctx->tol = *t;
+    return 0;
+}
+
+int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    FANS_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->st));
+    int refinements = 0;
+    if (ctx->desc.method == FANSGPU_FP)
+        rc = solve_fp64(ctx);
+    else if (ctx->desc.precision == FANSGPU_MIXED)
+        rc = solve_cg_mixed(ctx, &refinements);
+    else
+        rc = solve_cg64(ctx);
+    if (rc)
+        return rc;
+    FANS_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->st));
+    FANS_CUDA_CHECK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    const double err     = ctx->err_all.back();
+    const double err_rel = err_value(ctx, err);
+    const bool   conv    = err_rel <= ctx->tol.tolerance;
+    if (stats) {
+        stats->iterations  = ctx->iter;
+        stats->converged   = conv ? 1 : 0;
+        stats->err0        = ctx->err_all[0];
+        stats->err         = err;
+        stats->refinements = refinements;
+        stats->solve_ms    = ms;
+    }
+    // internal variables are committed here (solver.h:299); linear laws have none
+    return conv ? 0 : FANSGPU_ENOTCONV;
+}
+
+int fansgpu_homogenized_stress(fansgpu_ctx *ctx, double *out)
+{
+    if (!ctx || !out)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    double red[16];
+    if ((rc = strain_stress(ctx, -1, nullptr, nullptr, red)))
+        return rc;
+    for (int i = 0; i < ctx->nstr; ++i)
+        out[i] = red[ctx->nstr + i] / (double)ctx->N;
+    return 0;
+}
+
+int fansgpu_postprocess_averages(fansgpu_ctx *ctx, double *strain_avg, double *stress_avg, double *phase_strain,
+                                 double *phase_stress, int64_t *phase_count, int32_t n_phase)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const int ns = ctx->nstr;
+    double    red[16];
+    if ((rc = strain_stress(ctx, -1, nullptr, nullptr, red)))
+        return rc;
+    for (int i = 0; i < ns; ++i) {
+        if (strain_avg)
+            strain_avg[i] = red[i] / (double)ctx->N;
+        if (stress_avg)
+            stress_avg[i] = red[ns + i] / (double)ctx->N;
+    }
+    for (int ph = 0; ph < n_phase; ++ph) {
+        if (ph >= ctx->nph) {
+            for (int i = 0; i < ns; ++i) {
+                if (phase_strain) phase_strain[ph * ns + i] = 0.0;
+                if (phase_stress) phase_stress[ph * ns + i] = 0.0;
+            }
+            if (phase_count) phase_count[ph] = 0;
+            continue;
+        }
+        if ((rc = strain_stress(ctx, ph, nullptr, nullptr, red)))
+            return rc;
+        const double cnt = red[2 * ns];
+        for (int i = 0; i < ns; ++i) {
+            if (phase_strain) phase_strain[ph * ns + i] = cnt > 0 ? red[i] / cnt : 0.0;
+            if (phase_stress) phase_stress[ph * ns + i] = cnt > 0 ? red[ns + i] / cnt : 0.0;
+        }
+        if (phase_count)
+            phase_count[ph] = (int64_t)cnt;
+    }
+    return 0;
+}
+
+int fansgpu_homogenized_tangent(fansgpu_ctx *ctx, double pert, double *out)
+{
+    if (!ctx || !out)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const int ns = ctx->nstr;
+    // solver.h:749-750: relative error type and TOL >= 1e-6 for the rest of the run
+    ctx->tol.type      = FANSGPU_RELATIVE;
+    ctx->tol.tolerance = std::max(1e-6, ctx->tol.tolerance);
+    std::vector<double> g_save = ctx->g0, T(ns * ns), sig(ns);
+    for (int i = 0; i < ns; ++i) {
+        std::vector<double> g(ns, 0.0);
+        g[i] = 1.0; // linear laws: unit gradients (solver.h:760-762)
+        (void)pert;
+        if ((rc = fansgpu_set_gradient(ctx, g.data())))
+            return rc;
+        rc = fansgpu_solve(ctx, nullptr);
+        if (rc && rc != FANSGPU_ENOTCONV)
+            return rc;
+        if ((rc = fansgpu_homogenized_stress(ctx, sig.data())))
+            return rc;
+        for (int k = 0; k < ns; ++k)
+            T[k * ns + i] = sig[k];
+    }
+    for (int i = 0; i < ns; ++i)
+        for (int j = 0; j < ns; ++j)
+            out[i * ns + j] = 0.5 * (T[i * ns + j] + T[j * ns + i]);
+    return 0;
+}
+
+int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host)
+{
+    if (!ctx || !host)
+        return FANSGPU_EINVAL;
+    const long long N = ctx->N;
+    if (which == FANSGPU_FIELD_U || which == FANSGPU_FIELD_R || which == FANSGPU_FIELD_U_PREV) {
+        const double *src = which == FANSGPU_FIELD_U ? ctx->u : which == FANSGPU_FIELD_R ? ctx->r : ctx->uprev;
+        FANS_CUDA_CHECK((launch_soa_to_aos<double, double>(src, ctx->staging, N, ctx->C, ctx->st)));
+        FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N * ctx->C, cudaMemcpyDeviceToHost, ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        return 0;
+    }
+    if (which == FANSGPU_FIELD_STRAIN || which == FANSGPU_FIELD_STRESS) {
+        int rc = setup(ctx);
+        if (rc)
+            return rc;
+        double red[16];
+        if ((rc = strain_stress(ctx, -1, which == FANSGPU_FIELD_STRAIN ? ctx->staging : nullptr,
+                                which == FANSGPU_FIELD_STRESS ? ctx->staging : nullptr, red)))
+            return rc;
+        FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N * ctx->nstr, cudaMemcpyDeviceToHost, ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        return 0;
+    }
+    return fail(ctx, FANSGPU_EINVAL, "unknown field %d", which);
+}
+
+int fansgpu_set_field(fansgpu_ctx *ctx, int32_t which, const double *host)
+{
+    if (!ctx || !host)
+        return FANSGPU_EINVAL;
+    double *dst = which == FANSGPU_FIELD_U ? ctx->u : which == FANSGPU_FIELD_R ? ctx->r : which == FANSGPU_FIELD_U_PREV ? ctx->uprev : nullptr;
+    if (!dst)
+        return fail(ctx, FANSGPU_EINVAL, "field %d cannot be set", which);
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, host, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, dst, ctx->N, ctx->C, ctx->st)));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_get_error_history(fansgpu_ctx *ctx, double *out, int32_t max_n, int32_t *n_out)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    int n = (int)ctx->err_all.size();
+    if (n_out)
+        *n_out = n;
+    if (out)
+        for (int i = 0; i < std::min(n, (int)max_n); ++i)
+            out[i] = ctx->err_all[i];
+    return 0;
+}
+
+int fansgpu_extrapolate_displacement(fansgpu_ctx *ctx)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    FANS_CUDA_CHECK(launch_extrapolate(ctx->u, ctx->uprev, ctx->n, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_commit_state(fansgpu_ctx *ctx)
+{
+    return ctx ? 0 : FANSGPU_EINVAL;
+}
+
+int fansgpu_residual(fansgpu_ctx *ctx, const double *u, double *r)
+{
+    if (!ctx || !u || !r)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const long long N = ctx->N;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, u, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, ctx->Kd, N, ctx->C, ctx->st)));
+    if ((rc = run_stencil<double>(ctx, ctx->Kd, ctx->s, true)))
+        return rc;
+    FANS_CUDA_CHECK((launch_soa_to_aos<double, double>(ctx->s, ctx->staging, N, ctx->C, ctx->st)));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(r, ctx->staging, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_apply_operator(fansgpu_ctx *ctx, const double *x, double *y)
+{
+    if (!ctx || !x || !y)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const long long N = ctx->N;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, x, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, ctx->Kd, N, ctx->C, ctx->st)));
+    if ((rc = run_stencil<double>(ctx, ctx->Kd, ctx->s, false)))
+        return rc;
+    FANS_CUDA_CHECK((launch_soa_to_aos<double, double>(ctx->s, ctx->staging, N, ctx->C, ctx->st)));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(y, ctx->staging, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_convolve(fansgpu_ctx *ctx, const double *rin, double *sout)
+{
+    if (!ctx || !rin || !sout)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const long long N = ctx->N;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, rin, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, ctx->Kd, N, ctx->C, ctx->st)));
+    ConvArgs ca{ctx->Kd, ctx->s, 1.0, 0, ctx->scal, ctx->red, SITE_CONV};
+    FANS_CUDA_CHECK(launch_convolution<double>(ctx->cp64, ca, ctx->st));
+    FANS_CUDA_CHECK((launch_soa_to_aos<double, double>(ctx->s, ctx->staging, N, ctx->C, ctx->st)));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(sout, ctx->staging, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_green_table(fansgpu_ctx *ctx, double *host)
+{
+    if (!ctx || !host)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const long long F = (long long)ctx->g.nx * ctx->g.ny * (ctx->g.nz / 2 + 1);
+    const int       NT = ctx->C * (ctx->C + 1) / 2;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->G64, sizeof(double) * F * NT, cudaMemcpyDeviceToHost, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+} // extern "C"

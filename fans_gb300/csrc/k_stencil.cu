@@ -1,0 +1,350 @@
+// k_stencil.cu -- voxel-element kernels of the FANS solve path on sm_103a.
+//
+// The CG operator and the linear residual are node-centric gathers: node n sums
+// the rows of its 8 surrounding elements' stiffness (solver.h:315-385 visits
+// elements and scatters; gathering per node gives the same sum with no write
+// conflicts, no atomics and a fixed summation order).  A CTA stages a
+// (TX+2)x(TY+2)x(TZ+2) halo tile of the input field and the (TX+1)(TY+1)(TZ+1)
+// element phases in shared memory with periodic wrap, then each thread computes
+// TX nodes of one (y,z) column.
+#include "kernels.cuh"
+
+namespace fansgpu {
+
+namespace {
+constexpr int TX = 4, TY = 8, TZ = 32;
+constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;
+constexpr int EX = TX + 1, EY = TY + 1, EZ = TZ + 1;
+constexpr int kStencilThreads = TY * TZ; // 256
+
+__device__ __forceinline__ int pmod(int i, int n)
+{
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+template <typename T, int C>
+__global__ void __launch_bounds__(kStencilThreads) k_stencil(StencilArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const long long N = (long long)nx * ny * nz;
+    constexpr int NC  = 8 * C;
+    T       *xs  = reinterpret_cast<T *>(smem_raw);                 // C * HX*HY*HZ
+    T       *Ks  = xs + C * HX * HY * HZ;                           // nph * NC*NC
+    T       *fs  = Ks + (size_t)a.nph * NC * NC;                    // nph * NC (if fph)
+    uint8_t *mss = reinterpret_cast<uint8_t *>(fs + (a.fph ? a.nph * NC : 0)); // EX*EY*EZ
+    __shared__ double red_smem[32 * 2];
+
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    const int tid = threadIdx.x;
+
+    // stage per-phase tables
+    const T *Kg = reinterpret_cast<const T *>(a.Kph);
+    for (int i = tid; i < a.nph * NC * NC; i += blockDim.x)
+        Ks[i] = Kg[i];
+    if (a.fph) {
+        const T *fg = reinterpret_cast<const T *>(a.fph);
+        for (int i = tid; i < a.nph * NC; i += blockDim.x)
+            fs[i] = fg[i];
+    }
+    // stage element phases of elements (x0-1 .. x0+TX-1, ...)
+    for (int i = tid; i < EX * EY * EZ; i += blockDim.x) {
+        int ez = i % EZ, ey = (i / EZ) % EY, ex = i / (EZ * EY);
+        int gx = pmod(x0 - 1 + ex, nx), gy = pmod(y0 - 1 + ey, ny), gz = pmod(z0 - 1 + ez, nz);
+        mss[i] = a.ms[((long long)gx * ny + gy) * nz + gz];
+    }
+    // stage the input field on nodes (x0-1 .. x0+TX, ...), computing d = s + beta d_old when fused
+    const T     *xin  = reinterpret_cast<const T *>(a.x);
+    const T     *dold = reinterpret_cast<const T *>(a.d_old);
+    const double beta = a.fuse_d ? a.scal->beta : 0.0;
+    for (int i = tid; i < HX * HY * HZ; i += blockDim.x) {
+        int hz = i % HZ, hy = (i / HZ) % HY, hx = i / (HZ * HY);
+        int gx = pmod(x0 - 1 + hx, nx), gy = pmod(y0 - 1 + hy, ny), gz = pmod(z0 - 1 + hz, nz);
+        long long gi = ((long long)gx * ny + gy) * nz + gz;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            T v = xin[c * N + gi];
+            if (a.fuse_d)
+                v = (T)((double)v + beta * (double)dold[c * N + gi]);
+            xs[c * HX * HY * HZ + i] = v;
+        }
+    }
+    __syncthreads();
+
+    const int tz = tid % TZ, ty = tid / TZ;
+    const int gy = y0 + ty, gz = z0 + tz;
+    double    dot = 0.0;
+    const bool col_ok = (gy < ny) && (gz < nz);
+    for (int tx = 0; tx < TX; ++tx) {
+        const int gx = x0 + tx;
+        if (!col_ok || gx >= nx)
+            break;
+        // halo-tile coordinates of this node: (tx+1, ty+1, tz+1)
+        const int hc = ((tx + 1) * HY + (ty + 1)) * HZ + (tz + 1);
+        T         ctr[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            ctr[c] = xs[c * HX * HY * HZ + hc];
+        T acc[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            acc[c] = (T)0;
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            const int a0 = p & 1, b0 = (p >> 1) & 1, c0 = (p >> 2) & 1;
+            // element whose local node p is this node: origin (tx-a0, ty-b0, tz-c0)
+            const int ex = tx - a0 + 1, ey = ty - b0 + 1, ez = tz - c0 + 1; // element-tile coords
+            const int ph = mss[(ex * EY + ey) * EZ + ez];
+            const T  *Kr = Ks + (size_t)ph * NC * NC + (size_t)(p * C) * NC;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int qa = q & 1, qb = (q >> 1) & 1, qc = (q >> 2) & 1;
+                // node e + q in halo coordinates: (tx - a0 + qa + 1, ...)
+                const int hq = ((tx - a0 + qa + 1) * HY + (ty - b0 + qb + 1)) * HZ + (tz - c0 + qc + 1);
+#pragma unroll
+                for (int cb = 0; cb < C; ++cb) {
+                    const T v = xs[cb * HX * HY * HZ + hq] - ctr[cb];
+#pragma unroll
+                    for (int cr = 0; cr < C; ++cr)
+                        acc[cr] += Kr[cr * NC + q * C + cb] * v;
+                }
+            }
+            if (a.fph) {
+                const T *fr = fs + (size_t)ph * NC + p * C;
+#pragma unroll
+                for (int cr = 0; cr < C; ++cr)
+                    acc[cr] += fr[cr];
+            }
+        }
+        const long long gi = ((long long)gx * ny + gy) * nz + gz;
+        T *yout = reinterpret_cast<T *>(a.y);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            yout[c * N + gi] = acc[c];
+            if (a.reduce)
+                dot += (double)ctr[c] * (double)acc[c];
+        }
+        if (a.fuse_d) {
+            T *dn = reinterpret_cast<T *>(a.d_new);
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                dn[c * N + gi] = ctr[c];
+        }
+    }
+    if (a.reduce) {
+        double    v[1]   = {dot};
+        const int ops[1] = {RED_SUM};
+        block_reduce<1>(v, ops, red_smem);
+        const int nb = gridDim.x * gridDim.y * gridDim.z;
+        double   *partials = a.red.partials;
+        if (grid_partial_commit<1>(v, partials, a.red.counter + a.red_site, nb)) {
+            grid_final<1>(v, ops, partials, nb, red_smem);
+            if (threadIdx.x == 0) {
+                a.scal->dAd   = v[0];
+                a.scal->alpha = a.scal->delta / v[0];
+            }
+        }
+    }
+}
+
+template <typename T, int C>
+size_t stencil_smem(const StencilArgs &a)
+{
+    constexpr int NC = 8 * C;
+    size_t        b  = sizeof(T) * ((size_t)C * HX * HY * HZ + (size_t)a.nph * NC * NC + (a.fph ? a.nph * NC : 0));
+    return b + EX * EY * EZ;
+}
+
+template <typename T, int C>
+cudaError_t launch_stencil_c(const StencilArgs &a, cudaStream_t st)
+{
+    dim3   grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + TZ - 1) / TZ);
+    size_t sm = stencil_smem<T, C>(a);
+    cudaError_t e = cudaFuncSetAttribute(k_stencil<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess)
+        return e;
+    k_stencil<T, C><<<grid, kStencilThreads, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ strain/stress --
+template <int C, int NSTR>
+__global__ void __launch_bounds__(256) k_strain_stress(StrainStressArgs a)
+{
+    __shared__ double Bs[NSTR * 8 * C];
+    __shared__ double Cs[16 * NSTR * NSTR];
+    __shared__ double red_smem[32 * (2 * NSTR + 1)];
+    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const long long N = (long long)nx * ny * nz;
+    for (int i = threadIdx.x; i < NSTR * 8 * C; i += blockDim.x)
+        Bs[i] = a.Bbar[i];
+    for (int i = threadIdx.x; i < a.nph * NSTR * NSTR; i += blockDim.x)
+        Cs[i] = a.Cph[i];
+    __syncthreads();
+    double se[NSTR], ss[NSTR], cnt = 0.0;
+#pragma unroll
+    for (int i = 0; i < NSTR; ++i)
+        se[i] = ss[i] = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N; e += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(e % nz), y = (int)((e / nz) % ny), x = (int)(e / ((long long)nz * ny));
+        const int ph = a.ms[e];
+        const bool take = (a.phase_filter < 0) || (a.phase_filter == ph);
+        if (!take && !a.strain && !a.stress)
+            continue;
+        const int x1 = x + 1 == nx ? 0 : x + 1, y1 = y + 1 == ny ? 0 : y + 1, z1 = z + 1 == nz ? 0 : z + 1;
+        long long idx[8];
+        idx[0] = ((long long)x * ny + y) * nz + z;
+        idx[1] = ((long long)x1 * ny + y) * nz + z;
+        idx[2] = ((long long)x * ny + y1) * nz + z;
+        idx[3] = ((long long)x1 * ny + y1) * nz + z;
+        idx[4] = ((long long)x * ny + y) * nz + z1;
+        idx[5] = ((long long)x1 * ny + y) * nz + z1;
+        idx[6] = ((long long)x * ny + y1) * nz + z1;
+        idx[7] = ((long long)x1 * ny + y1) * nz + z1;
+        double eps[NSTR];
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i)
+            eps[i] = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const double uq = a.u[c * N + idx[q]];
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i)
+                    eps[i] += Bs[i * 8 * C + q * C + c] * uq;
+            }
+        double sig[NSTR];
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i)
+            eps[i] += a.g0[i];
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < NSTR; ++k)
+                acc += Cs[(ph * NSTR + i) * NSTR + k] * eps[k];
+            sig[i] = acc;
+        }
+        if (a.strain)
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i)
+                a.strain[e * NSTR + i] = eps[i];
+        if (a.stress)
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i)
+                a.stress[e * NSTR + i] = sig[i];
+        if (take) {
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i) {
+                se[i] += eps[i];
+                ss[i] += sig[i];
+            }
+            cnt += 1.0;
+        }
+    }
+    double v[2 * NSTR + 1];
+    int    ops[2 * NSTR + 1];
+#pragma unroll
+    for (int i = 0; i < NSTR; ++i) {
+        v[i]        = se[i];
+        v[NSTR + i] = ss[i];
+    }
+    v[2 * NSTR] = cnt;
+#pragma unroll
+    for (int i = 0; i < 2 * NSTR + 1; ++i)
+        ops[i] = RED_SUM;
+    block_reduce<2 * NSTR + 1>(v, ops, red_smem);
+    if (grid_partial_commit<2 * NSTR + 1>(v, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+        grid_final<2 * NSTR + 1>(v, ops, a.red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0)
+            for (int i = 0; i < 2 * NSTR + 1; ++i)
+                a.out_red[i] = v[i];
+    }
+}
+
+// ----------------------------------------------------------------- layout ---
+template <typename TI, typename TO>
+__global__ void k_aos_to_soa(const TI *__restrict__ aos, TO *__restrict__ soa, long long N, int C)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N * C; i += (long long)gridDim.x * blockDim.x) {
+        long long node = i / C;
+        int       c    = (int)(i % C);
+        soa[c * N + node] = (TO)aos[i];
+    }
+}
+template <typename TI, typename TO>
+__global__ void k_soa_to_aos(const TI *__restrict__ soa, TO *__restrict__ aos, long long N, int C)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N * C; i += (long long)gridDim.x * blockDim.x) {
+        long long node = i / C;
+        int       c    = (int)(i % C);
+        aos[i] = (TO)soa[c * N + node];
+    }
+}
+template <typename TI, typename TO>
+__global__ void k_convert(const TI *__restrict__ in, TO *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (TO)in[i];
+}
+
+} // namespace
+
+int grid_blocks_for(long long n)
+{
+    long long b = (n + 255) / 256;
+    const long long cap = 152LL * 16;
+    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
+
+long long stencil_blocks(const Grid3 &g)
+{
+    return (long long)((g.nx + TX - 1) / TX) * ((g.ny + TY - 1) / TY) * ((g.nz + TZ - 1) / TZ);
+}
+
+template <typename T>
+cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st)
+{
+    if (a.C == 1)
+        return launch_stencil_c<T, 1>(a, st);
+    return launch_stencil_c<T, 3>(a, st);
+}
+template cudaError_t launch_stencil<double>(const StencilArgs &, cudaStream_t);
+template cudaError_t launch_stencil<float>(const StencilArgs &, cudaStream_t);
+
+cudaError_t launch_strain_stress(const StrainStressArgs &a, cudaStream_t st)
+{
+    const int nb = grid_blocks_for(a.g.N());
+    if (a.C == 1)
+        k_strain_stress<1, 3><<<nb, 256, 0, st>>>(a);
+    else
+        k_strain_stress<3, 6><<<nb, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename TI, typename TO>
+cudaError_t launch_aos_to_soa(const TI *aos, TO *soa, long long N, int C, cudaStream_t st)
+{
+    k_aos_to_soa<TI, TO><<<grid_blocks_for(N * C), 256, 0, st>>>(aos, soa, N, C);
+    return cudaGetLastError();
+}
+template <typename TI, typename TO>
+cudaError_t launch_soa_to_aos(const TI *soa, TO *aos, long long N, int C, cudaStream_t st)
+{
+    k_soa_to_aos<TI, TO><<<grid_blocks_for(N * C), 256, 0, st>>>(soa, aos, N, C);
+    return cudaGetLastError();
+}
+template <typename TI, typename TO>
+cudaError_t launch_convert(const TI *in, TO *out, long long n, cudaStream_t st)
+{
+    k_convert<TI, TO><<<grid_blocks_for(n), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_aos_to_soa<double, double>(const double *, double *, long long, int, cudaStream_t);
+template cudaError_t launch_soa_to_aos<double, double>(const double *, double *, long long, int, cudaStream_t);
+template cudaError_t launch_convert<double, float>(const double *, float *, long long, cudaStream_t);
+template cudaError_t launch_convert<float, double>(const float *, double *, long long, cudaStream_t);
+
+} // namespace fansgpu

@@ -1,0 +1,149 @@
+// k_vec.cu -- streaming CG vector kernels with fused FP64 reductions.
+#include "kernels.cuh"
+
+namespace fansgpu {
+
+namespace {
+constexpr int kVecThreads = 256;
+
+__device__ __forceinline__ double norm_term(double v, int measure)
+{
+    double a = fabs(v);
+    return measure == 1 ? a * a : a; // L2: squares; L1 / Linf: |v|
+}
+
+// r -= alpha*Kd; u -= alpha*d; partial ||r|| and <r, s>  (solverCG.h:105-113, solver.h:415-430)
+template <typename T, typename TU>
+__global__ void __launch_bounds__(kVecThreads) k_cg_update(UpdateArgs a)
+{
+    __shared__ double red_smem[32 * 2];
+    const double alpha = a.scal->alpha;
+    T           *r  = reinterpret_cast<T *>(a.r);
+    const T     *Kd = reinterpret_cast<const T *>(a.Kd);
+    TU          *u  = reinterpret_cast<TU *>(a.u);
+    const T     *d  = reinterpret_cast<const T *>(a.d);
+    const T     *s  = reinterpret_cast<const T *>(a.s);
+    double       nrm = 0.0, rs = 0.0;
+    const bool   mx  = a.measure == 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.n; i += (long long)gridDim.x * blockDim.x) {
+        T rv = (T)((double)r[i] - alpha * (double)Kd[i]);
+        r[i] = rv;
+        if (a.do_u)
+            u[i] = (TU)((double)u[i] - alpha * (double)d[i]);
+        double t = norm_term((double)rv, a.measure);
+        nrm      = mx ? fmax(nrm, t) : nrm + t;
+        rs += (double)rv * (double)s[i];
+    }
+    double v[2]   = {nrm, rs};
+    int    ops[2] = {mx ? RED_MAX : RED_SUM, RED_SUM};
+    block_reduce<2>(v, ops, red_smem);
+    if (grid_partial_commit<2>(v, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+        grid_final<2>(v, ops, a.red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0) {
+            a.scal->err      = a.measure == 1 ? sqrt(v[0]) : v[0];
+            a.scal->deltamid = v[1];
+            if (!isfinite(a.scal->err))
+                a.scal->converged = -1;
+        }
+    }
+}
+
+template <typename T, typename TO>
+__global__ void __launch_bounds__(kVecThreads) k_norm(const T *__restrict__ r, long long n, int measure,
+                                                      CgScalars *scal, int set_err0, TO *r_out, GridRed red,
+                                                      int site)
+{
+    __shared__ double red_smem[32];
+    double     nrm = 0.0;
+    const bool mx  = measure == 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        T      v = r[i];
+        double t = norm_term((double)v, measure);
+        nrm      = mx ? fmax(nrm, t) : nrm + t;
+        if (r_out)
+            r_out[i] = (TO)v;
+    }
+    double v[1]   = {nrm};
+    int    ops[1] = {mx ? RED_MAX : RED_SUM};
+    block_reduce<1>(v, ops, red_smem);
+    if (grid_partial_commit<1>(v, red.partials, red.counter + site, gridDim.x)) {
+        grid_final<1>(v, ops, red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0) {
+            double e  = measure == 1 ? sqrt(v[0]) : v[0];
+            scal->err = e;
+            if (set_err0)
+                scal->err0 = e;
+            if (!isfinite(e))
+                scal->converged = -1;
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_axpy(T *__restrict__ y, const T *__restrict__ x, double a, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = (T)((double)y[i] + a * (double)x[i]);
+}
+
+__global__ void k_extrapolate(double *__restrict__ u, double *__restrict__ up, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double delta = u[i] - up[i];
+        up[i]              = u[i];
+        u[i] += delta;
+    }
+}
+
+__global__ void k_fold(double *__restrict__ u, float *__restrict__ e, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        u[i] += (double)e[i];
+        e[i] = 0.0f;
+    }
+}
+} // namespace
+
+template <typename T, typename TU>
+cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st)
+{
+    k_cg_update<T, TU><<<grid_blocks_for(a.n), kVecThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_cg_update<double, double>(const UpdateArgs &, cudaStream_t);
+template cudaError_t launch_cg_update<float, double>(const UpdateArgs &, cudaStream_t);
+template cudaError_t launch_cg_update<float, float>(const UpdateArgs &, cudaStream_t);
+
+template <typename T, typename TO>
+cudaError_t launch_norm(const T *r, long long n, int measure, CgScalars *scal, int set_err0, TO *r_out, GridRed red,
+                        int site, cudaStream_t st)
+{
+    k_norm<T, TO><<<grid_blocks_for(n), kVecThreads, 0, st>>>(r, n, measure, scal, set_err0, r_out, red, site);
+    return cudaGetLastError();
+}
+template cudaError_t launch_norm<double, float>(const double *, long long, int, CgScalars *, int, float *, GridRed, int,
+                                                cudaStream_t);
+template cudaError_t launch_norm<float, float>(const float *, long long, int, CgScalars *, int, float *, GridRed, int,
+                                               cudaStream_t);
+
+template <typename T>
+cudaError_t launch_axpy(T *y, const T *x, double a, long long n, cudaStream_t st)
+{
+    k_axpy<T><<<grid_blocks_for(n), kVecThreads, 0, st>>>(y, x, a, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_axpy<double>(double *, const double *, double, long long, cudaStream_t);
+
+cudaError_t launch_extrapolate(double *u, double *u_prev, long long n, cudaStream_t st)
+{
+    k_extrapolate<<<grid_blocks_for(n), kVecThreads, 0, st>>>(u, u_prev, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fold(double *u, float *e, long long n, cudaStream_t st)
+{
+    k_fold<<<grid_blocks_for(n), kVecThreads, 0, st>>>(u, e, n);
+    return cudaGetLastError();
+}
+
+} // namespace fansgpu

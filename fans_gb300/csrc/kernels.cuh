@@ -1,0 +1,153 @@
+// kernels.cuh -- host-side launchers of the GB300 FANS kernels (one declaration
+// per fused pass).  Fields on the device are SoA: component planes of N values,
+// node (x,y,z) at (x*ny + y)*nz + z.  Reductions accumulate in FP64 and are
+// deterministic: per-block partials summed in block order by the last block.
+#pragma once
+#include "fans_common.cuh"
+#include "fft.cuh"
+
+namespace fansgpu {
+
+struct Grid3 {
+    int nx, ny, nz;
+    long long N() const { return (long long)nx * ny * nz; }
+};
+
+// ---------------------------------------------------------------- stencil ---
+// y = K x (+ F), the CG linear operator (solverCG.h:97-103) and, with F, the
+// linear residual R(u) = K u + F(g0) (solver.h:272-280, matmodel.h:191-201).
+// Node-centric gather over the 8 elements around each node, with per-phase
+// element stiffness K_ph (8C x 8C, node-major rows/cols) and per-phase force
+// f_ph (8C).  Optional fusion:
+//   fuse_d: x = s + beta*d_old (beta from scal) and x written to d_new;
+//   reduction of <x, y> into scal->dAd and alpha = delta/dAd.
+struct StencilArgs {
+    Grid3          g;
+    int            C;
+    const void    *x;      // x, or s when fuse_d
+    const void    *d_old;  // fuse_d only
+    void          *d_new;  // fuse_d only
+    void          *y;
+    const uint8_t *ms;
+    const void    *Kph;    // nph * 64*C*C
+    const void    *fph;    // nph * 8C, or null
+    int            nph;
+    int            fuse_d;
+    int            reduce; // 1: <x,y> -> scal (dAd, alpha)
+    CgScalars     *scal;
+    GridRed        red;
+    int            red_site;
+};
+template <typename T>
+cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st);
+
+// Element-averaged strain/stress of linear laws (matmodel.h:203-225,
+// solver.h:708-737): eps_e = Bbar u_e + g0, sig_e = C_ph eps_e.  Sums over the
+// elements whose phase matches `phase_filter` (-1: all) land in out_red:
+// [0,nstr) sum eps, [nstr,2nstr) sum sig, [2nstr] count.  Optional AoS fields.
+struct StrainStressArgs {
+    Grid3          g;
+    int            C, nstr;
+    const double  *u;      // SoA FP64
+    const uint8_t *ms;
+    const double  *Bbar;   // nstr x 8C (GP-averaged B)
+    const double  *Cph;    // nph x nstr x nstr
+    const double  *g0;     // nstr
+    int            nph;
+    int            phase_filter;
+    double        *strain; // [N][nstr] or null
+    double        *stress; // [N][nstr] or null
+    double        *out_red;
+    GridRed        red;
+    int            red_site;
+};
+cudaError_t launch_strain_stress(const StrainStressArgs &a, cudaStream_t st);
+
+// ----------------------------------------------------------------- layout ---
+template <typename TI, typename TO>
+cudaError_t launch_aos_to_soa(const TI *aos, TO *soa, long long N, int C, cudaStream_t st);
+template <typename TI, typename TO>
+cudaError_t launch_soa_to_aos(const TI *soa, TO *aos, long long N, int C, cudaStream_t st);
+template <typename TI, typename TO>
+cudaError_t launch_convert(const TI *in, TO *out, long long n, cudaStream_t st);
+
+// -------------------------------------------------------------------- fft ---
+template <typename T>
+struct ConvPlan {
+    Grid3          g;
+    int            C, M, nzh, nzp; // M = nz/2 complex z-length, nzp = spectrum row stride
+    FftDim         dx, dy, dz;     // dz has length M
+    const cplx<T> *tw_x, *tw_y, *tw_z, *tw_r2c; // tw_r2c: exp(-2 pi i k/nz), k <= M
+    cplx<T>       *spec;           // C * nx * ny * nzp
+    const T       *G;              // nx*ny*nzh*C(C+1)/2
+    int            kc_y, kc_x;     // kz columns per CTA in the y / x passes
+};
+
+// s = sign * IFFT(G . FFT(r)); with reduce, <r, s> -> scal (delta0, delta,
+// beta) as in solverCG.h:86-94.
+struct ConvArgs {
+    const void *r;
+    void       *s;
+    double      sign;
+    int         reduce;
+    CgScalars  *scal;
+    GridRed     red;
+    int         red_site;
+};
+template <typename T>
+cudaError_t launch_convolution(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st);
+template <typename T>
+size_t conv_smem_bytes(const ConvPlan<T> &p, int pass);
+
+// Green's table (solver.h:145-204) in FP64, optionally also rounded to FP32.
+struct GreenArgs {
+    Grid3         g;
+    int           C;
+    const double *K0c;   // 8C x 8C, component-major ("C groups of 8")
+    const double *cx, *sx, *cy, *sy, *cz, *sz; // cos/sin(2 pi k / n)
+    double       *G64;
+    float        *G32;   // optional
+};
+cudaError_t launch_green(const GreenArgs &a, cudaStream_t st);
+
+// ------------------------------------------------------------------ CG vec ---
+// r -= alpha*Kd; u -= alpha*d (alpha from scal); err = ||r|| (measure) and
+// deltamid = <r, s> -> scal.  T: type of r, Kd, d, s; TU: type of u.
+struct UpdateArgs {
+    long long  n;
+    void      *r;
+    const void *Kd;
+    void      *u;
+    const void *d;
+    const void *s;
+    int        measure;
+    int        do_u;
+    CgScalars *scal;
+    GridRed    red;
+    int        red_site;
+};
+template <typename T, typename TU>
+cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st);
+
+// err = ||r|| (measure) -> scal->err (and err0 if set_err0); optionally also
+// writes a copy of r converted to `r_out` (mixed precision re-seed).
+template <typename T, typename TO>
+cudaError_t launch_norm(const T *r, long long n, int measure, CgScalars *scal, int set_err0, TO *r_out, GridRed red,
+                        int red_site, cudaStream_t st);
+
+// u -= s (fixed-point update, solverFP.h:38).
+template <typename T>
+cudaError_t launch_axpy(T *y, const T *x, double a, long long n, cudaStream_t st);
+
+// u = u + (u - u_prev); u_prev = u_old (solver.h:303-311).
+cudaError_t launch_extrapolate(double *u, double *u_prev, long long n, cudaStream_t st);
+
+// u64 += e32 (mixed precision: fold the FP32 correction into the FP64 solution).
+cudaError_t launch_fold(double *u, float *e, long long n, cudaStream_t st);
+
+int grid_blocks_for(long long n);
+
+// number of CTAs of the stencil kernel for grid g
+long long stencil_blocks(const Grid3 &g);
+
+} // namespace fansgpu

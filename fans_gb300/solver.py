@@ -1,0 +1,243 @@
+"""Host mirror of FANS's Solver / SolverCG / SolverFP API over the C ABI.
+
+`Context` is a thin owner of one `fansgpu_ctx` (one GPU solver state).
+`Solver`, `SolverCG` and `SolverFP` keep the reference's public surface
+(solver.h:11-103): solve(), get_homogenized_stress(), get_homogenized_tangent(),
+extrapolateDisplacement(), fields v_u / v_r, iter and err_all.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as C
+from .materials import MaterialManager
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """One GPU solver context (fansgpu_create .. fansgpu_destroy)."""
+
+    def __init__(self, n, L=(1.0, 1.0, 1.0), howmany=3, fe_type="HEX8", precision="fp64", method="cg"):
+        self.lib = C.load()
+        d = C.Desc()
+        d.n[:] = [int(v) for v in n]
+        d.L[:] = [float(v) for v in L]
+        d.howmany = int(howmany)
+        d.fe_type = C.FE_TYPES[fe_type] if isinstance(fe_type, str) else int(fe_type)
+        d.precision = {"fp64": C.FP64, "mixed": C.MIXED}[precision] if isinstance(precision, str) else int(precision)
+        d.method = {"cg": C.CG, "fp": C.FP}[method] if isinstance(method, str) else int(method)
+        ptr = ctypes.c_void_p()
+        rc = self.lib.fansgpu_create(ctypes.byref(d), ctypes.byref(ptr))
+        if rc != C.OK:
+            raise C.FansGpuError(rc, self.lib.fansgpu_last_error(None).decode())
+        self.ctx = ptr
+        self.n = tuple(int(v) for v in n)
+        self.howmany = int(howmany)
+        self.n_str = 3 if howmany == 1 else 6
+        self.N = self.n[0] * self.n[1] * self.n[2]
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.fansgpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, rc, allow=()):
+        return C.check(self.ctx, rc, allow)
+
+    # -- state ---------------------------------------------------------------
+    def set_microstructure(self, ms):
+        ms = np.ascontiguousarray(ms, dtype=np.uint16)
+        assert ms.shape == self.n, (ms.shape, self.n)
+        self._chk(self.lib.fansgpu_set_microstructure(self.ctx, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))))
+
+    def set_phase_material(self, phase, law, params):
+        p = np.ascontiguousarray(params, dtype=float).ravel()
+        self._chk(self.lib.fansgpu_set_phase_material(self.ctx, int(phase), int(law), _ptr(p), p.size))
+
+    def set_reference(self, kapparef):
+        k = np.ascontiguousarray(kapparef, dtype=float)
+        self._chk(self.lib.fansgpu_set_reference(self.ctx, _ptr(k)))
+
+    def set_gradient(self, g0):
+        g = np.ascontiguousarray(g0, dtype=float)
+        assert g.size == self.n_str
+        self._chk(self.lib.fansgpu_set_gradient(self.ctx, _ptr(g)))
+
+    def set_tolerance(self, measure="L2", type="relative", tolerance=1e-10, n_it=100, ls_max_iter=5, ls_tol=1e-2):
+        t = C.Tol(C.MEASURES[measure], C.ERROR_TYPES[type], float(tolerance), int(n_it), int(ls_max_iter),
+                  float(ls_tol))
+        self._chk(self.lib.fansgpu_set_tolerance(self.ctx, ctypes.byref(t)))
+
+    # -- solve ---------------------------------------------------------------
+    def solve(self):
+        st = C.Stats()
+        self._chk(self.lib.fansgpu_solve(self.ctx, ctypes.byref(st)), allow=(C.ENOTCONV,))
+        return {"iterations": st.iterations, "converged": bool(st.converged), "err0": st.err0, "err": st.err,
+                "refinements": st.refinements, "solve_ms": st.solve_ms}
+
+    def homogenized_stress(self):
+        out = np.zeros(self.n_str)
+        self._chk(self.lib.fansgpu_homogenized_stress(self.ctx, _ptr(out)))
+        return out
+
+    def homogenized_tangent(self, pert=1e-6):
+        out = np.zeros((self.n_str, self.n_str))
+        self._chk(self.lib.fansgpu_homogenized_tangent(self.ctx, float(pert), _ptr(out)))
+        return out
+
+    def postprocess_averages(self, n_phase):
+        ns = self.n_str
+        se, ss = np.zeros(ns), np.zeros(ns)
+        pe, ps = np.zeros((n_phase, ns)), np.zeros((n_phase, ns))
+        cnt = np.zeros(n_phase, dtype=np.int64)
+        self._chk(self.lib.fansgpu_postprocess_averages(self.ctx, _ptr(se), _ptr(ss), _ptr(pe), _ptr(ps),
+                                                        cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                                        int(n_phase)))
+        return dict(strain_average=se, stress_average=ss, phase_strain=pe, phase_stress=ps, phase_count=cnt)
+
+    def get_field(self, which):
+        k = self.howmany if which in (C.FIELD_U, C.FIELD_R, C.FIELD_U_PREV) else self.n_str
+        out = np.zeros(self.n + (k,))
+        self._chk(self.lib.fansgpu_get_field(self.ctx, int(which), _ptr(out)))
+        return out
+
+    def set_field(self, which, arr):
+        a = np.ascontiguousarray(arr, dtype=float)
+        assert a.shape == self.n + (self.howmany,)
+        self._chk(self.lib.fansgpu_set_field(self.ctx, int(which), _ptr(a)))
+
+    def error_history(self):
+        n = ctypes.c_int32()
+        self._chk(self.lib.fansgpu_get_error_history(self.ctx, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1))
+        self._chk(self.lib.fansgpu_get_error_history(self.ctx, _ptr(out), n.value, ctypes.byref(n)))
+        return out[: n.value]
+
+    def extrapolate_displacement(self):
+        self._chk(self.lib.fansgpu_extrapolate_displacement(self.ctx))
+
+    def commit_state(self):
+        self._chk(self.lib.fansgpu_commit_state(self.ctx))
+
+    # -- kernel-level --------------------------------------------------------
+    def _map(self, fn, x):
+        x = np.ascontiguousarray(x, dtype=float)
+        assert x.shape == self.n + (self.howmany,)
+        y = np.zeros_like(x)
+        self._chk(fn(self.ctx, _ptr(x), _ptr(y)))
+        return y
+
+    def residual(self, u):
+        return self._map(self.lib.fansgpu_residual, u)
+
+    def apply_operator(self, x):
+        return self._map(self.lib.fansgpu_apply_operator, x)
+
+    def convolve(self, r):
+        return self._map(self.lib.fansgpu_convolve, r)
+
+    def green_table(self):
+        nt = self.howmany * (self.howmany + 1) // 2
+        out = np.zeros((self.n[0], self.n[1], self.n[2] // 2 + 1, nt))
+        self._chk(self.lib.fansgpu_green_table(self.ctx, _ptr(out)))
+        return out
+
+
+class Solver:
+    """Solver<howmany, n_str> (solver.h:11-103) on the GPU.
+
+    `reader` is a fans_gb300.reader.Reader (or any object with the same
+    attributes: dims, L, problemType, FE_type, method, errorParameters, TOL,
+    n_it, ls_max_iter, ls_tol, ms, inputJson)."""
+
+    method = "cg"
+
+    def __init__(self, reader, matmanager: MaterialManager, precision="fp64"):
+        self.reader = reader
+        self.matmanager = matmanager
+        self.howmany = 1 if reader.problemType == "thermal" else 3
+        self.n_str = 3 if self.howmany == 1 else 6
+        self.ctx = Context(reader.dims, reader.L, self.howmany, reader.FE_type, precision, self.method)
+        self.ctx.set_microstructure(reader.ms)
+        matmanager.apply(self.ctx)
+        self._push_tolerance()
+        self.iter = 0
+        self.err_all = np.zeros(0)
+        self.last_stats = None
+
+    def _push_tolerance(self):
+        ep = self.reader.errorParameters
+        self.ctx.set_tolerance(ep["measure"], ep["type"], self.reader.TOL, self.reader.n_it, self.reader.ls_max_iter,
+                               self.reader.ls_tol)
+
+    def set_gradient(self, g0):
+        """MaterialManager::set_gradient (MaterialManager.h:216-221)."""
+        self.ctx.set_gradient(g0)
+
+    def solve(self):
+        """Solver::solve (solver.h:283-300)."""
+        st = self.ctx.solve()
+        self.iter = st["iterations"]
+        self.err_all = self.ctx.error_history()
+        self.last_stats = st
+        return st
+
+    @property
+    def v_u(self):
+        return self.ctx.get_field(C.FIELD_U)
+
+    @property
+    def v_r(self):
+        return self.ctx.get_field(C.FIELD_R)
+
+    def get_homogenized_stress(self):
+        return self.ctx.homogenized_stress()
+
+    def get_homogenized_tangent(self, pert_param=1e-6):
+        """solver.h:740-778, including its side effects on the error type and tolerance."""
+        C_ = self.ctx.homogenized_tangent(pert_param)
+        self.reader.errorParameters["type"] = "relative"
+        self.reader.TOL = max(1e-6, self.reader.TOL)
+        return C_
+
+    def extrapolateDisplacement(self):
+        self.ctx.extrapolate_displacement()
+
+    def close(self):
+        self.ctx.close()
+
+
+class SolverCG(Solver):
+    method = "cg"
+
+
+class SolverFP(Solver):
+    method = "fp"
+
+
+def create_solver(reader, matmanager, precision="fp64"):
+    """createSolver (setup.h:76-85)."""
+    if reader.method == "fp":
+        return SolverFP(reader, matmanager, precision)
+    if reader.method == "cg":
+        return SolverCG(reader, matmanager, precision)
+    raise ValueError(f"{reader.method} is not a valid method")

@@ -1,0 +1,201 @@
+/*
+ * fans_gb300.h -- C ABI of the GB300-native FANS solve path.
+ *
+ * One context = one FANS Solver on one GPU: a periodic voxel grid, its
+ * microstructure (phase id per voxel), the per-phase material laws, the
+ * reference material, the macroscopic gradient and the solver state.  All
+ * device memory is owned by the context; callers pass host buffers and get
+ * host results.  Every entry point returns 0 on success or a negative
+ * FANSGPU_E* code; fansgpu_last_error() gives a one-line message.
+ *
+ * Host field layout at this boundary is the reference's: nodal fields
+ * [x][y][z][c] with c fastest (solver.h:123-127, without FFTW padding),
+ * element fields [x][y][z][n_str], microstructure uint16 [x][y][z]
+ * (reader.cpp:380-398).  Strains/stresses use FANS's Mandel ordering
+ * (11, 22, 33, sqrt2*12, sqrt2*13, sqrt2*23) (matmodel.h:284-304).
+ *
+ * Each declaration names the reference interface it replaces
+ * (FANS v0.6.2, file:line).
+ */
+#ifndef FANS_GB300_H
+#define FANS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FANSGPU_OK 0
+#define FANSGPU_EINVAL -1      /* bad argument (std::invalid_argument in the reference) */
+#define FANSGPU_ENOMEM -2      /* device allocation failed (std::bad_alloc) */
+#define FANSGPU_ECUDA -3       /* CUDA runtime error */
+#define FANSGPU_ENOTCONV -4    /* n_it reached before the tolerance (reported, not fatal) */
+#define FANSGPU_ENAN -5        /* NaN/Inf found in the residual norm */
+#define FANSGPU_EUNSUPPORTED -6 /* valid FANS input this build does not handle (named in the message) */
+#define FANSGPU_ESTATE -7      /* call order violated (e.g. solve before set_microstructure) */
+
+/* FE_type (reader.cpp:121-128, matmodel.h:82-88) */
+#define FANSGPU_HEX8 0
+#define FANSGPU_HEX8R 1
+#define FANSGPU_BBAR 2
+
+/* material laws (setup.h:22-73); parameter vectors per phase:
+ *   THERMAL_ISO  {conductivity}                                   LinearThermal.h:7-50
+ *   ELASTIC_ISO  {bulk_modulus, shear_modulus}                    LinearElastic.h:7-75
+ *   J2_LINEAR    {bulk, shear, yield_stress, isotropic_hardening} J2PlasticityNew.h:7-152
+ *   THERMAL_TRI  {K (3x3 row-major)}                              LinearThermal.h:52-118
+ *   ELASTIC_TRI  {C (6x6 row-major, Mandel)}                      LinearElastic.h:77-159 */
+#define FANSGPU_LAW_THERMAL_ISO 0
+#define FANSGPU_LAW_ELASTIC_ISO 1
+#define FANSGPU_LAW_J2_LINEAR 2
+#define FANSGPU_LAW_THERMAL_TRI 3
+#define FANSGPU_LAW_ELASTIC_TRI 4
+
+/* precision of the solve */
+#define FANSGPU_FP64 0  /* all FP64: parity path against the FP64 reference */
+#define FANSGPU_MIXED 1 /* FP32 stencil + FFT preconditioner inside an FP64 reliable-update loop */
+
+/* method (setup.h:76-85) */
+#define FANSGPU_CG 0
+#define FANSGPU_FP 1
+
+/* error_parameters (solver.h:415-452) */
+#define FANSGPU_L1 0
+#define FANSGPU_L2 1
+#define FANSGPU_LINF 2
+#define FANSGPU_ABSOLUTE 0
+#define FANSGPU_RELATIVE 1
+
+/* fields for get/set (solver.h:34-38, :455-705) */
+#define FANSGPU_FIELD_U 0        /* displacement/temperature fluctuation v_u, [x][y][z][c] */
+#define FANSGPU_FIELD_R 1        /* residual v_r, [x][y][z][c] */
+#define FANSGPU_FIELD_STRAIN 2   /* element-averaged strain/gradient, [x][y][z][n_str] */
+#define FANSGPU_FIELD_STRESS 3   /* element-averaged stress/flux, [x][y][z][n_str] */
+#define FANSGPU_FIELD_U_PREV 4   /* previous step displacement (extrapolation) */
+
+typedef struct fansgpu_ctx fansgpu_ctx;
+
+/* Grid + discretisation: Reader fields dims/L/FE_type/problem_type
+ * (reader.h:24-63) and the Solver template arguments <howmany, n_str>. */
+typedef struct {
+    int32_t n[3];      /* voxels n_x, n_y, n_z (each even, 4..1024) */
+    double  L[3];      /* microstructure box lengths (reader.cpp:83) */
+    int32_t howmany;   /* 1: thermal <1,3>; 3: small-strain mechanics <3,6> (main.cpp:67-75) */
+    int32_t fe_type;   /* FANSGPU_HEX8 / HEX8R / BBAR */
+    int32_t precision; /* FANSGPU_FP64 / FANSGPU_MIXED */
+    int32_t method;    /* FANSGPU_CG / FANSGPU_FP */
+} fansgpu_desc;
+
+/* error_parameters, n_it and linesearch_parameters (reader.cpp:94-105). */
+typedef struct {
+    int32_t measure;     /* FANSGPU_L1 / L2 / LINF */
+    int32_t type;        /* FANSGPU_ABSOLUTE / RELATIVE */
+    double  tolerance;
+    int32_t n_it;
+    int32_t ls_max_iter; /* default 5 (reader.h:33) */
+    double  ls_tol;      /* default 1e-2 (reader.h:34) */
+} fansgpu_tol;
+
+typedef struct {
+    int32_t iterations;       /* Solver::iter after internalSolve */
+    int32_t converged;        /* 1 if the tolerance was met */
+    double  err0;             /* err_all[0] */
+    double  err;              /* err_all[iter] (absolute, in the configured measure) */
+    int32_t refinements;      /* MIXED: FP64 true-residual evaluations after the first */
+    double  solve_ms;         /* device time of the solve (CUDA events) */
+} fansgpu_stats;
+
+/* Solver ctor (solver.h:105-142, solverCG.h:36-50): allocates all device state.
+ * Replaces `createSolver` (setup.h:76-85) + `Solver<h,n>::Solver`. */
+int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out);
+
+/* Solver dtor (solver.h:780-805, solverCG.h:162-177). */
+int fansgpu_destroy(fansgpu_ctx *ctx);
+
+/* One-line message for the last failing call on this context (NULL ctx: last
+ * failure of fansgpu_create). */
+const char *fansgpu_last_error(const fansgpu_ctx *ctx);
+
+/* Reader::ReadMS result (reader.cpp:227-411): phase id per voxel, uint16 [x][y][z]. */
+int fansgpu_set_microstructure(fansgpu_ctx *ctx, const uint16_t *ms_xyz);
+
+/* MaterialManager phase table (MaterialManager.h:86-103): the law and
+ * parameters of one phase (see FANSGPU_LAW_*).  All phases that occur in the
+ * microstructure must be assigned before the first solve. */
+int fansgpu_set_phase_material(fansgpu_ctx *ctx, int32_t phase, int32_t law, const double *params,
+                               int32_t n_params);
+
+/* MaterialManager::compute_reference_stiffness (MaterialManager.h:177-205):
+ * kapparef_mat (n_str x n_str, row-major).  Must be set before the first solve;
+ * the host mirror computes the reference's default rule. */
+int fansgpu_set_reference(fansgpu_ctx *ctx, const double *kapparef);
+
+/* MaterialManager::set_gradient / Matmodel::setGradient (MaterialManager.h:216-221,
+ * matmodel.h:228-236): macroscopic gradient g0 (n_str). */
+int fansgpu_set_gradient(fansgpu_ctx *ctx, const double *g0);
+
+/* Reader error_parameters / n_it / linesearch_parameters (reader.cpp:94-105). */
+int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *tol);
+
+/* Solver::solve (solver.h:283-300) -> SolverCG::internalSolve (solverCG.h:62-117)
+ * or SolverFP::internalSolve (solverFP.h:33-52), then commit of internal
+ * variables (solver.h:299).  stats may be NULL.  Returns FANSGPU_ENOTCONV when
+ * n_it was reached (the state is still valid, as in the reference). */
+int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats);
+
+/* Solver::get_homogenized_stress (solver.h:708-737): volume average of the
+ * element-averaged stress/flux (n_str doubles). */
+int fansgpu_homogenized_stress(fansgpu_ctx *ctx, double *out);
+
+/* Solver::get_homogenized_tangent (solver.h:740-778): n_str x n_str,
+ * row-major, symmetrised.  Linear laws: unit-gradient solves; nonlinear: FD
+ * with pert_param.  Like the reference it leaves the context's error type
+ * relative and the tolerance at max(1e-6, tol), and v_u at the last solve. */
+int fansgpu_homogenized_tangent(fansgpu_ctx *ctx, double pert_param, double *out);
+
+/* Solver::postprocess averages (solver.h:469-574): strain/stress averages and
+ * per-phase averages (n_phase x n_str, phases in id order) with counts.
+ * Any pointer may be NULL. */
+int fansgpu_postprocess_averages(fansgpu_ctx *ctx, double *strain_avg, double *stress_avg, double *phase_strain,
+                                 double *phase_stress, int64_t *phase_count, int32_t n_phase);
+
+/* Field access (v_u, v_r, postprocess fields).  `host` holds n_x*n_y*n_z*k doubles. */
+int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host);
+int fansgpu_set_field(fansgpu_ctx *ctx, int32_t which, const double *host);
+
+/* err_all (solver.h:44, :432): up to max_n entries of the last solve's history. */
+int fansgpu_get_error_history(fansgpu_ctx *ctx, double *out, int32_t max_n, int32_t *n_out);
+
+/* Solver::extrapolateDisplacement (solver.h:303-311). */
+int fansgpu_extrapolate_displacement(fansgpu_ctx *ctx);
+
+/* MaterialManager::update_internal_variables (MaterialManager.h:207-213). */
+int fansgpu_commit_state(fansgpu_ctx *ctx);
+
+/* ---- kernel-level entry points (one hot-path stage each, FP64, host buffers) ---- */
+
+/* Solver::compute_residual (solver.h:272-280): r = R(u) with the current g0.
+ * u, r: [x][y][z][c]. */
+int fansgpu_residual(fansgpu_ctx *ctx, const double *u, double *r);
+
+/* The CG linear operator (solverCG.h:97-103): y = sum_e A_e^T K_phase(e) x_e. */
+int fansgpu_apply_operator(fansgpu_ctx *ctx, const double *x, double *y);
+
+/* Solver::convolution (solver.h:388-412): s = IFFT(G . FFT(r)), unnormalised
+ * transforms with 1/N folded into G. */
+int fansgpu_convolve(fansgpu_ctx *ctx, const double *r, double *s);
+
+/* Solver::computeFundamentalSolution (solver.h:145-204): the Green's table,
+ * [kx][ky][kz] (kz < n_z/2+1) x c(c+1)/2 lower-triangle entries (00,10,11,20,21,22). */
+int fansgpu_green_table(fansgpu_ctx *ctx, double *host);
+
+/* Library version string. */
+const char *fansgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FANS_GB300_H */

@@ -1,0 +1,316 @@
+"""Python side of the oracle: ctypes binding of fans_oracle.c plus the
+reference's host-side rules the oracle needs (reference stiffness, phase
+parameter packing).
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker for the CUDA product.
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+arm may import it; the product package never does.
+
+Parity status: the reference (FANS v0.6.2) cannot be built in this image (MPI,
+FFTW3-MPI, parallel HDF5, Eigen and nlohmann_json are absent) and its own
+tests hold no golden numbers, only invariants.  The oracle is therefore pinned
+by (1) an independent numpy restatement (numpy.fft / LAPACK eigh) of the same
+reference lines, (2) known answers (homogeneous media, laminates), and (3) the
+reference tests' invariants evaluated on the reference fixture
+test/microstructures/sphere32.h5.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfans_oracle.so")
+
+HEX8, HEX8R, BBAR = 0, 1, 2
+FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
+LAW_THERMAL_ISO, LAW_ELASTIC_ISO, LAW_J2, LAW_THERMAL_TRI, LAW_ELASTIC_TRI = 0, 1, 2, 3, 4
+L1, L2, LINF = 0, 1, 2
+ABS, REL = 0, 1
+MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}
+TYPES = {"absolute": ABS, "relative": REL}
+PARAM_STRIDE = 36
+
+
+def build(force: bool = False) -> str:
+    """Compile fans_oracle.c into libfans_oracle.so (gcc, OpenMP)."""
+    src = os.path.join(HERE, "fans_oracle.c")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+        return LIB_PATH
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-o", LIB_PATH, src, "-lm"]
+    subprocess.check_call(cmd)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_u16p = ctypes.POINTER(ctypes.c_uint16)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+
+def _declare(L):
+    i, d, sz = ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    L.fo_build_B.argtypes = [i, i, _dp, _dp]
+    L.fo_build_B.restype = i
+    L.fo_element_stiffness.argtypes = [i, i, _dp, _dp, d, _dp]
+    L.fo_green.argtypes = [i, i, i, i, _dp, _dp]
+    L.fo_rfft3.argtypes = [i, i, i, _dp, i, _dp, _dp]
+    L.fo_irfft3.argtypes = [i, i, i, _dp, _dp, _dp, i]
+    L.fo_convolve.argtypes = [i, i, i, i, _dp, _dp, _dp]
+    common = [i, i, i, i, i, d, _dp, _u16p, i, _ip, _dp, _dp, _dp, _dp, _dp, _dp]
+    L.fo_residual.argtypes = common + [_dp, _dp]
+    L.fo_apply_linear.argtypes = [i, i, i, i, _u16p, _dp, _dp, _dp]
+    L.fo_strain_stress.argtypes = common + [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _lp]
+    L.fo_norm.argtypes = [sz, _dp, i]
+    L.fo_norm.restype = d
+    L.fo_cg_solve.argtypes = common + [_dp, _dp, i, i, i, d, i, i, d, _dp, _dp, _dp]
+    L.fo_cg_solve.restype = i
+    L.fo_fp_solve.argtypes = common + [_dp, i, i, d, i, _dp, _dp, _dp]
+    L.fo_fp_solve.restype = i
+    L.fo_num_threads.restype = i
+    L.fo_set_num_threads.argtypes = [i]
+
+
+def _p(a, t=_dp):
+    if a is None:
+        return ctypes.cast(None, t)
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(t)
+
+
+# ---------------------------------------------------------------------------
+# Reference host rules restated for the oracle
+# ---------------------------------------------------------------------------
+
+def iso_elastic_C(K, G):
+    """6x6 Mandel stiffness: topLeft(3,3)=lambda, + 2 mu I (LinearElastic.h:28-35)."""
+    lam = K - 2.0 / 3.0 * G
+    C = np.zeros((6, 6))
+    C[:3, :3] = lam
+    C += 2.0 * G * np.eye(6)
+    return C
+
+
+def law_C(law, params):
+    if law == LAW_THERMAL_ISO:
+        return params[0] * np.eye(3)
+    if law in (LAW_ELASTIC_ISO, LAW_J2):
+        return iso_elastic_C(params[0], params[1])
+    if law == LAW_THERMAL_TRI:
+        return np.asarray(params[:9], dtype=float).reshape(3, 3)
+    if law == LAW_ELASTIC_TRI:
+        return np.asarray(params[:36], dtype=float).reshape(6, 6)
+    raise ValueError(law)
+
+
+def model_reference_stiffness(law, phase_params):
+    """Matmodel::get_reference_stiffness of one material group.
+
+    LinearThermalIsotropic: mean conductivity (LinearThermal.h:21-31, :49-52);
+    LinearElasticIsotropic: (max+min)/2 of lambda and mu (LinearElastic.h:55-70);
+    J2PlasticityNew: mean K and G (J2PlasticityNew.h:111-121);
+    triclinic: mean C (LinearElastic.h:146-154, LinearThermal.h:103-110)."""
+    pp = [np.asarray(p, dtype=float) for p in phase_params]
+    if law == LAW_THERMAL_ISO:
+        return np.mean([p[0] for p in pp]) * np.eye(3)
+    if law == LAW_ELASTIC_ISO:
+        lam = [p[0] - 2.0 / 3.0 * p[1] for p in pp]
+        mu = [p[1] for p in pp]
+        lr = (max(lam) + min(lam)) / 2
+        mr = (max(mu) + min(mu)) / 2
+        C = np.zeros((6, 6))
+        C[:3, :3] = lr
+        C += 2 * mr * np.eye(6)
+        return C
+    if law == LAW_J2:
+        Kb = np.mean([p[0] for p in pp])
+        Gb = np.mean([p[1] for p in pp])
+        C = np.zeros((6, 6))
+        C[:3, :3] = Kb - 2.0 * Gb / 3.0
+        C[np.diag_indices(6)] += 2.0 * Gb
+        return C
+    return np.mean([law_C(law, p) for p in pp], axis=0)
+
+
+class OracleProblem:
+    """A FANS problem as the oracle sees it (one MaterialManager + Solver).
+
+    groups: list of (law, [phase ids], [per-phase parameter vectors]) in the
+    order of the JSON 'materials' array."""
+
+    def __init__(self, ms, L, c, groups, fe_type="HEX8", kapparef=None):
+        self.ms = np.ascontiguousarray(ms, dtype=np.uint16)
+        self.nx, self.ny, self.nz = self.ms.shape
+        self.c = c
+        self.nstr = 3 if c == 1 else 6
+        self.fe = FE_TYPES[fe_type] if isinstance(fe_type, str) else fe_type
+        self.L = np.asarray(L, dtype=float)
+        self.le = np.array([self.L[0] / self.nx, self.L[1] / self.ny, self.L[2] / self.nz])
+        self.ve = float(self.le[0] * self.le[1] * self.le[2])
+        B = np.zeros(8 * 6 * 24)
+        self.ngp = lib().fo_build_B(self.fe, c, _p(self.le), _p(B))
+        self.B = np.ascontiguousarray(B[: self.ngp * self.nstr * 8 * c])
+        nphase = 1 + max(max(ph) for _, ph, _ in groups)
+        self.nphase = nphase
+        self.law = np.zeros(nphase, dtype=np.int32)
+        self.param = np.zeros((nphase, PARAM_STRIDE))
+        self.linear = True
+        refs = []
+        for law, phases, params in groups:
+            for ph, pr in zip(phases, params):
+                self.law[ph] = law
+                pr = np.asarray(pr, dtype=float).ravel()
+                self.param[ph, : pr.size] = pr
+            if law == LAW_J2:
+                self.linear = False
+            refs.append(model_reference_stiffness(law, params))
+        # MaterialManager::compute_reference_stiffness (MaterialManager.h:177-205)
+        self.kapparef = np.mean(refs, axis=0) if kapparef is None else np.asarray(kapparef, dtype=float)
+        self.Kph = np.zeros((nphase, 8 * c, 8 * c))
+        for ph in range(nphase):
+            C = np.ascontiguousarray(law_C(self.law[ph], self.param[ph]))
+            lib().fo_element_stiffness(c, self.ngp, _p(self.B), _p(C), self.ve, _p(self.Kph[ph]))
+        self.K0 = np.zeros((8 * c, 8 * c))
+        lib().fo_element_stiffness(c, self.ngp, _p(self.B), _p(np.ascontiguousarray(self.kapparef)), self.ve,
+                                   _p(self.K0))
+        nel = self.nx * self.ny * self.nz
+        self.ep_t = np.zeros((nel, self.ngp, 6)) if not self.linear else np.zeros(6)
+        self.q_t = np.zeros((nel, self.ngp)) if not self.linear else np.zeros(1)
+        self.ep = self.ep_t.copy()
+        self.q = self.q_t.copy()
+        self.g0 = np.zeros(self.nstr)
+        self.u = np.zeros((self.nx, self.ny, self.nz, c))
+        self.u_prev = np.zeros_like(self.u)
+        self._G = None
+
+    # -- pieces --------------------------------------------------------------
+    @property
+    def G(self):
+        if self._G is None:
+            nzh = self.nz // 2 + 1
+            nt = self.c * (self.c + 1) // 2
+            G = np.zeros((self.nx, self.ny, nzh, nt))
+            lib().fo_green(self.nx, self.ny, self.nz, self.c, _p(self.K0), _p(G))
+            self._G = G
+        return self._G
+
+    def _common(self):
+        return (self.nx, self.ny, self.nz, self.c, self.ngp, self.ve, _p(self.B), _p(self.ms, _u16p), self.nphase,
+                _p(self.law, _ip), _p(self.param), _p(self.g0), _p(self.ep_t), _p(self.q_t), _p(self.ep),
+                _p(self.q))
+
+    def set_gradient(self, g0):
+        self.g0 = np.ascontiguousarray(g0, dtype=float)
+
+    def residual(self, u=None):
+        u = self.u if u is None else np.ascontiguousarray(u, dtype=float)
+        r = np.zeros_like(u)
+        lib().fo_residual(*self._common(), _p(u), _p(r))
+        return r
+
+    def apply_linear(self, d):
+        d = np.ascontiguousarray(d, dtype=float)
+        out = np.zeros_like(d)
+        lib().fo_apply_linear(self.nx, self.ny, self.nz, self.c, _p(self.ms, _u16p), _p(self.Kph), _p(d), _p(out))
+        return out
+
+    def convolve(self, r):
+        r = np.ascontiguousarray(r, dtype=float)
+        s = np.zeros_like(r)
+        lib().fo_convolve(self.nx, self.ny, self.nz, self.c, _p(self.G), _p(r), _p(s))
+        return s
+
+    def strain_stress(self, u=None, fields=False):
+        u = self.u if u is None else np.ascontiguousarray(u, dtype=float)
+        N = self.nx * self.ny * self.nz
+        strain = np.zeros((N, self.nstr)) if fields else None
+        stress = np.zeros((N, self.nstr)) if fields else None
+        a_e, a_s = np.zeros(self.nstr), np.zeros(self.nstr)
+        p_e, p_s = np.zeros((self.nphase, self.nstr)), np.zeros((self.nphase, self.nstr))
+        cnt = np.zeros(self.nphase, dtype=np.int64)
+        lib().fo_strain_stress(*self._common(), _p(u), _p(strain), _p(stress), _p(a_e), _p(a_s), _p(p_e), _p(p_s),
+                               _p(cnt, _lp))
+        return dict(strain=strain, stress=stress, strain_average=a_e, stress_average=a_s, phase_strain=p_e,
+                    phase_stress=p_s, phase_count=cnt)
+
+    def homogenized_stress(self):
+        return self.strain_stress()["stress_average"]
+
+    def solve(self, method="cg", measure="L2", type="relative", tol=1e-10, n_it=100, ls_max_iter=5, ls_tol=1e-2):
+        """Solver::solve (solver.h:283-300): internalSolve then commit internal variables."""
+        r = np.zeros_like(self.u)
+        err = np.zeros(n_it + 1)
+        m, t = MEASURES[measure], TYPES[type]
+        if method == "cg":
+            it = lib().fo_cg_solve(*self._common(), _p(self.Kph), _p(self.G), int(self.linear), m, t, tol, n_it,
+                                   ls_max_iter, ls_tol, _p(self.u), _p(r), _p(err))
+        else:
+            it = lib().fo_fp_solve(*self._common(), _p(self.G), m, t, tol, n_it, _p(self.u), _p(r), _p(err))
+        self.r = r
+        self.err_all = err[: it + 1]
+        self.iterations = it
+        if not self.linear:
+            self.ep_t[...] = self.ep
+            self.q_t[...] = self.q
+        return it
+
+    def extrapolate_displacement(self):
+        """Solver::extrapolateDisplacement (solver.h:303-311)."""
+        delta = self.u - self.u_prev
+        self.u_prev[...] = self.u
+        self.u += delta
+
+    def homogenized_tangent_unit(self, **solve_kw):
+        """C_eff from explicit unit-load solves, one per column (the linear branch of
+        Solver::get_homogenized_tangent, solver.h:759-776, at the configured tolerance)."""
+        C = np.zeros((self.nstr, self.nstr))
+        for i in range(self.nstr):
+            g = np.zeros(self.nstr)
+            g[i] = 1.0
+            self.set_gradient(g)
+            self.solve(**solve_kw)
+            C[:, i] = self.homogenized_stress()
+        return 0.5 * (C + C.T)
+
+
+def rfft3(f):
+    """FFTW-convention r2c of a real [x][y][z] array via the C oracle FFT."""
+    f = np.ascontiguousarray(f, dtype=float)
+    nx, ny, nz = f.shape
+    re = np.zeros((nx, ny, nz // 2 + 1))
+    im = np.zeros_like(re)
+    lib().fo_rfft3(nx, ny, nz, _p(f), 1, _p(re), _p(im))
+    return re + 1j * im
+
+
+def irfft3(spec, nz):
+    spec = np.asarray(spec)
+    nx, ny, _ = spec.shape
+    re = np.ascontiguousarray(spec.real, dtype=float)
+    im = np.ascontiguousarray(spec.imag, dtype=float)
+    f = np.zeros((nx, ny, nz))
+    lib().fo_irfft3(nx, ny, nz, _p(re), _p(im), _p(f), 1)
+    return f
+
+
+def set_threads(n):
+    lib().fo_set_num_threads(int(n))
+
+
+def num_threads():
+    return lib().fo_num_threads()

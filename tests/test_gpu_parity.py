@@ -1,0 +1,178 @@
+"""GPU parity: each hot-path stage and the full solves through the C ABI against
+the FP64 oracle on the same seeded inputs.
+
+Tolerances (FP64 path): Green's table, operator, residual and convolution agree
+to 1e-12 relative (different summation order only); solves agree in
+iteration count within +-1, homogenized stress/flux within 1e-10 relative and
+per-voxel fields within 1e-8 relative.  Mixed path: effective stiffness within
+1e-6 relative of the FP64 oracle and the FP64 true residual below tolerance.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import ELASTIC, THERMAL, gpu_context, oracle_problem, random_ms, rel
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(8, 6, 10), (16, 16, 16), (12, 20, 8), (6, 10, 48)]
+
+
+@pytest.mark.parametrize("fe", ["HEX8", "HEX8R", "BBAR"])
+@pytest.mark.parametrize("c,groups", [(1, THERMAL), (3, ELASTIC)])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_green_operator_residual_convolution(shape, c, groups, fe):
+    ms = random_ms(shape, seed=sum(shape) + c)
+    P = oracle_problem(ms, c, groups, fe)
+    ctx = gpu_context(P)
+    rng = np.random.default_rng(7)
+    # Green's table (solver.h:145-204)
+    G = ctx.green_table()
+    assert rel(G, P.G) < 1e-12
+    # operator (solverCG.h:97-103)
+    x = rng.standard_normal(shape + (c,))
+    assert rel(ctx.apply_operator(x), P.apply_linear(x)) < 1e-12
+    # residual with g0 (solver.h:272-280)
+    g0 = rng.standard_normal(P.nstr)
+    P.set_gradient(g0)
+    ctx.set_gradient(g0)
+    assert rel(ctx.residual(x), P.residual(x)) < 1e-12
+    # convolution (solver.h:388-412)
+    assert rel(ctx.convolve(x), P.convolve(x)) < 1e-12
+    ctx.close()
+
+
+@pytest.mark.parametrize("measure,etype,tol", [("L2", "relative", 1e-10), ("Linfinity", "absolute", 1e-10),
+                                                ("L1", "relative", 1e-8)])
+@pytest.mark.parametrize("c,groups,shape", [(1, THERMAL, (16, 16, 16)), (3, ELASTIC, (16, 12, 20))])
+def test_cg_solve_fp64(c, groups, shape, measure, etype, tol):
+    ms = random_ms(shape, vf=0.3, seed=3)
+    P = oracle_problem(ms, c, groups, "HEX8")
+    ctx = gpu_context(P)
+    g0 = np.zeros(P.nstr)
+    g0[0] = 1.0
+    g0[-1] = 0.5
+    P.set_gradient(g0)
+    ctx.set_gradient(g0)
+    ctx.set_tolerance(measure, etype, tol, 300)
+    st = ctx.solve()
+    it = P.solve(measure=measure, type=etype, tol=tol, n_it=300)
+    assert st["converged"]
+    assert abs(st["iterations"] - it) <= 1
+    u = ctx.get_field(0)
+    assert rel(u, P.u) < 1e-8
+    assert rel(ctx.homogenized_stress(), P.homogenized_stress()) < 1e-10
+    hist = ctx.error_history()
+    assert rel(hist[0], P.err_all[0]) < 1e-12
+    ctx.close()
+
+
+@pytest.mark.parametrize("c,groups", [(1, THERMAL), (3, ELASTIC)])
+def test_fp_solve_fp64(c, groups):
+    shape = (12, 12, 12)
+    ms = random_ms(shape, vf=0.25, seed=11)
+    P = oracle_problem(ms, c, groups, "HEX8R")
+    ctx = gpu_context(P, method="fp")
+    g0 = np.linspace(0.5, 1.0, P.nstr)
+    P.set_gradient(g0)
+    ctx.set_gradient(g0)
+    ctx.set_tolerance("L2", "relative", 1e-8, 500)
+    st = ctx.solve()
+    it = P.solve(method="fp", measure="L2", type="relative", tol=1e-8, n_it=500)
+    assert abs(st["iterations"] - it) <= 1
+    assert rel(ctx.get_field(0), P.u) < 1e-6
+    assert rel(ctx.homogenized_stress(), P.homogenized_stress()) < 1e-8
+    ctx.close()
+
+
+def test_mixed_precision_effective_stiffness():
+    """Elastic C_eff from 6 unit-strain solves: mixed path vs FP64 oracle."""
+    shape = (24, 24, 24)
+    from fans_gb300.microstructure import spheres
+
+    ms, _ = spheres(24, 3, 0.3, seed=1)
+    P = oracle_problem(ms, 3, ELASTIC, "HEX8")
+    C_ref = P.homogenized_tangent_unit(measure="L2", type="relative", tol=1e-8, n_it=500)
+    ctx = gpu_context(P, precision="mixed")
+    ctx.set_tolerance("L2", "relative", 1e-8, 500)
+    C_mix = np.zeros((6, 6))
+    for i in range(6):
+        g = np.zeros(6)
+        g[i] = 1.0
+        ctx.set_gradient(g)
+        ctx.set_field(0, np.zeros(shape + (3,)))
+        st = ctx.solve()
+        assert st["converged"]
+        # the accepted residual is the FP64 true residual
+        r = ctx.get_field(1)
+        assert np.sqrt((r ** 2).sum()) / st["err0"] <= 1e-8 * (1 + 1e-9)
+        C_mix[:, i] = ctx.homogenized_stress()
+    C_mix = 0.5 * (C_mix + C_mix.T)
+    assert np.linalg.norm(C_mix - C_ref) / np.linalg.norm(C_ref) < 1e-6
+    ctx.close()
+
+
+def test_homogeneous_known_answer():
+    """Homogeneous medium: r0 = 0 up to round-off, C_eff = C (absolute tolerance)."""
+    ms = np.zeros((8, 8, 8), np.uint16)
+    P = oracle_problem(ms, 3, [(O.LAW_ELASTIC_ISO, [0], [[3.0, 1.5]])], "HEX8")
+    ctx = gpu_context(P)
+    ctx.set_tolerance("L2", "absolute", 1e-12, 50)
+    Cm = O.iso_elastic_C(3.0, 1.5)
+    for i in range(6):
+        g = np.zeros(6)
+        g[i] = 1.0
+        ctx.set_gradient(g)
+        st = ctx.solve()
+        assert st["iterations"] == 0
+        assert np.allclose(ctx.homogenized_stress(), Cm[:, i], rtol=1e-13, atol=1e-13)
+    ctx.close()
+
+
+def test_laminate_known_answer():
+    """Thermal laminate along x: k_xx = harmonic mean, k_yy = k_zz = arithmetic mean."""
+    from fans_gb300.microstructure import laminate
+
+    ms = laminate((16, 4, 6), axis=0)
+    P = oracle_problem(ms, 1, THERMAL, "HEX8")
+    ctx = gpu_context(P)
+    ctx.set_tolerance("L2", "absolute", 1e-12, 500)
+    K = np.zeros((3, 3))
+    for i in range(3):
+        g = np.zeros(3)
+        g[i] = 1.0
+        ctx.set_gradient(g)
+        ctx.set_field(0, np.zeros((16, 4, 6, 1)))
+        ctx.solve()
+        K[:, i] = ctx.homogenized_stress()
+    assert abs(K[0, 0] - 2.0 / (1.0 + 0.1)) < 1e-10
+    assert abs(K[1, 1] - 5.5) < 1e-10 and abs(K[2, 2] - 5.5) < 1e-10
+    assert np.abs(K - np.diag(np.diag(K))).max() < 1e-10
+    ctx.close()
+
+
+def test_not_converged_status_and_history():
+    ms = random_ms((8, 8, 8), seed=5)
+    P = oracle_problem(ms, 3, ELASTIC, "HEX8")
+    ctx = gpu_context(P)
+    ctx.set_gradient(np.eye(6)[0])
+    ctx.set_tolerance("L2", "relative", 1e-14, 3)
+    st = ctx.solve()
+    assert not st["converged"] and st["iterations"] == 3
+    assert len(ctx.error_history()) == 4
+    ctx.close()
+
+
+def test_extrapolate_displacement():
+    ms = random_ms((8, 8, 8), seed=6)
+    P = oracle_problem(ms, 1, THERMAL, "HEX8")
+    ctx = gpu_context(P)
+    rng = np.random.default_rng(0)
+    u1 = rng.standard_normal((8, 8, 8, 1))
+    u0 = rng.standard_normal((8, 8, 8, 1))
+    ctx.set_field(4, u0)
+    ctx.set_field(0, u1)
+    ctx.extrapolate_displacement()
+    assert np.allclose(ctx.get_field(0), 2 * u1 - u0, atol=1e-14)
+    assert np.allclose(ctx.get_field(4), u1, atol=0)
+    ctx.close()
