@@ -1,0 +1,407 @@
+"""Benchmark of the GB300 FANS solve path on its headline workload.
+
+Workload (one step): 256^3 two-phase linear-elastic homogenization -- periodic
+non-overlapping spheres (seed 0, radius 6 voxels, 30 % volume fraction;
+matrix E=3 GPa nu=0.35, inclusions E=70 GPa nu=0.22), HEX8 elements, six unit
+Mandel strain load cases, flexible CG with the FFT Green's preconditioner to
+relative L2 residual 1e-8 -> the 6x6 effective stiffness.  A step rebuilds the
+Green's operator (as FANS does per Solver) and runs the six solves.
+
+  value : ms per step, mixed precision, inputs resident in HBM, CUDA events on
+          the solver's stream (fields are ~0.2-0.4 GB each: inputs larger than L2)
+  e2e   : the same through the C ABI from pinned host buffers (microstructure
+          upload + parameters in, 6x6 stiffness and per-iteration scalars out)
+  fp64  : the all-FP64 GPU path on the same step
+  cpu_baseline / --impl reference: the oracle (FP64 C restatement of the
+          reference's algorithm, OpenMP, all host cores) on a bounded sample.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 256]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "256^3 elastic solve ms to 1e-8: mixed vs FP64 GPU vs CPU; kernel HBM GB/s"
+MAT = [[3.3333333333333335, 1.1111111111111112], [41.666666666666664, 28.688524590163933]]  # (K, G) from (E, nu)
+HBM_FALLBACK_GBS = 6800.0
+# FP64 CG iterations of the six load cases of the 256^3 workload (GPU FP64 path,
+# which matches the oracle's iteration counts within +-1 in the parity tests);
+# used to scale the oracle's per-iteration time in the reference arm.
+FP64_ITERS_256 = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU path")
+    ap.add_argument("--cpu-iters", type=int, default=2)
+    return ap.parse_args()
+
+
+def kapparef():
+    """LinearElasticIsotropic reference: (max+min)/2 of lambda and mu (LinearElastic.h:55-70)."""
+    from fans_gb300.materials import group_reference_stiffness
+
+    return group_reference_stiffness(1, MAT)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes from committed ncu summaries: lines 'TRAFFIC <kernel> <n> <bytes>'."""
+    out = {}
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return out
+    for fn in os.listdir(pdir):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(pdir, fn)):
+            parts = line.strip().strip("`").split()
+            if len(parts) == 4 and parts[0] == "TRAFFIC":
+                out[(parts[1], int(parts[2]))] = float(parts[3])
+    return out
+
+
+def algo_bytes(kernel, n, C=3, w=4):
+    """Algorithmic (compulsory) DRAM bytes of one launch of `kernel` on an n^3 grid
+    with C components of w-byte values (w=4: mixed precision inner loop)."""
+    N = n ** 3
+    nzh = n // 2 + 1
+    spec = C * n * n * nzh * 2 * w  # half spectrum, complex
+    nt = C * (C + 1) // 2
+    return {
+        "stencil": (4 * C * w + 1) * N,          # read s, d_old, phases; write d, Kd
+        "fft_z_fwd": C * w * N + spec,           # read r, write spectrum
+        "fft_y_fwd": 2 * spec,
+        "fft_x_green": 2 * spec + nt * n * n * nzh * w,  # + Green's table
+        "fft_y_inv": 2 * spec,
+        "fft_z_inv": spec + 2 * C * w * N,       # read spectrum + r, write s
+        "cg_update": (5 * C * w + 2 * 8 * C) * N,  # read r Kd d s, write r; u64 read+write
+        "residual64": (2 * 8 * C + 1) * N,
+        "norm": (8 * C + 4 * C) * N,
+        "strain_stress": (8 * C + 1) * N,
+    }.get(kernel)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        dev0 = rows[0][0]
+        rows = [r for r in rows if r[0] == dev0]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def build_problem(n, seed=0):
+    from fans_gb300.microstructure import spheres
+
+    ms, centres = spheres(n, 6, 0.30, seed)
+    return ms, len(centres)
+
+
+def make_ctx(ms, n, precision, tol):
+    from fans_gb300 import Context
+
+    ctx = Context((n, n, n), (1.0, 1.0, 1.0), 3, "HEX8", precision, "cg")
+    ctx.set_microstructure(ms)
+    for ph in range(2):
+        ctx.set_phase_material(ph, 1, MAT[ph])
+    ctx.set_reference(kapparef())
+    ctx.set_tolerance("L2", "relative", tol, 2000)
+    return ctx
+
+
+def homogenize(ctx, kref, stats=None):
+    """One step: Green's operator rebuild + six unit-strain solves -> C_eff (6x6)."""
+    ctx.set_reference(kref)
+    Ceff = np.zeros((6, 6))
+    for i in range(6):
+        ctx.reset()
+        g = np.zeros(6)
+        g[i] = 1.0
+        ctx.set_gradient(g)
+        st = ctx.solve()
+        if not st["converged"]:
+            raise RuntimeError(f"load case {i} did not converge: {st}")
+        if stats is not None:
+            stats.append(st)
+        Ceff[:, i] = ctx.homogenized_stress()
+    return 0.5 * (Ceff + Ceff.T)
+
+
+def timed_steps(ctx, steps, fn):
+    import torch
+
+    s = torch.cuda.ExternalStream(ctx.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    out = None
+    for _ in range(steps):
+        out = fn()
+    e1.record(s)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def cpu_baseline(ms, n, iters, threads=None):
+    """Oracle (FP64 C restatement, OpenMP) on a bounded sample of the workload:
+    setup (B, K, Green's table) + `iters` CG iterations of load case 11."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    if threads:
+        O.set_threads(threads)
+    cores = O.num_threads()
+    t0 = time.perf_counter()
+    P = O.OracleProblem(ms.astype(np.uint16), (1, 1, 1), 3, [(O.LAW_ELASTIC_ISO, [0, 1], MAT)], "HEX8")
+    _ = P.G
+    t_setup = time.perf_counter() - t0
+    P.set_gradient(np.eye(6)[0])
+    t1 = time.perf_counter()
+    P.solve(measure="L2", type="relative", tol=1e-30, n_it=iters)
+    t_solve = time.perf_counter() - t1
+    # the solve sample = initial residual + `iters` iterations; charge it all to iterations
+    return {"setup_s": t_setup, "per_iter_s": t_solve / max(1, iters), "cores": cores,
+            "sample_s": t_setup + t_solve}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n = args.n
+    ms, nsph = build_problem(n)
+    iters_total = sum(FP64_ITERS_256) if (FP64_ITERS_256 and n == 256) else None
+    vals = []
+    if args.warmup > 0:
+        cpu_baseline(ms, n, 1)
+    cb = None
+    for _ in range(args.steps):
+        cb = cpu_baseline(ms, n, args.cpu_iters)
+        vals.append(cb)
+    per_iter = statistics.median(v["per_iter_s"] for v in vals)
+    setup = statistics.median(v["setup_s"] for v in vals)
+    if iters_total is None:
+        iters_total = 6 * 60
+        note = "iteration count assumed 60 per load case"
+    else:
+        note = "scaled by the six load cases' FP64 iteration counts " + str(FP64_ITERS_256)
+    value_ms = 1e3 * (6 * setup + per_iter * iters_total)
+    sample = (f"{args.cpu_iters} FP64 CG iterations of load case 11 at {n}^3 + solver setup (Green's table), "
+              f"{cb['cores']} threads; {note}; 6 solver setups as in FANS (one Solver per load case)")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value_ms, 1), "unit": "ms", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value_ms, 1),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": f"synthetic: seeded spheres ({nsph}), seed 0, r=6, vf=0.30",
+            "config": {"workload": f"{n}^3 two-phase elastic HEX8, 6 unit load cases, CG rel L2 {args.tol}",
+                       "parallelism": "cpu-openmp"},
+            "cpu_baseline": {"value": round(value_ms, 1), "unit": "ms", "cores": cb["cores"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value_ms, 1), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n = args.n
+    ms, nsph = build_problem(n)
+    kref = kapparef()
+    ctx = make_ctx(ms, n, "mixed", args.tol)
+
+    # warm-up (W full steps)
+    for _ in range(args.warmup):
+        homogenize(ctx, kref)
+
+    # timed region: K steps, CUDA events on the solver stream, per-kernel events on
+    stats: list = []
+    ctx.set_timing(True)
+    clocks = ClockSampler()
+    barrier()
+    ms_total, Ceff = timed_steps(ctx, args.steps, lambda: homogenize(ctx, kref, stats))
+    barrier()
+    clk = clocks.stop()
+    ktimes = ctx.kernel_times()
+    ctx.set_timing(False)
+    ms_step = ms_total / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    iters = [s["iterations"] for s in stats[:6]]
+    refinements = [s["refinements"] for s in stats[:6]]
+    launches = sum(c for _, c in ktimes.values())
+
+    # e2e through the C ABI from pinned host buffers
+    pinned = torch.empty(n ** 3, dtype=torch.int16, pin_memory=True)
+    ms_host = pinned.numpy().view(np.uint16).reshape(n, n, n)
+    ms_host[...] = ms
+
+    def e2e_step():
+        ctx.set_microstructure(ms_host)
+        for ph in range(2):
+            ctx.set_phase_material(ph, 1, MAT[ph])
+        return homogenize(ctx, kref)
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_ms_dev, _ = timed_steps(ctx, args.steps, e2e_step)
+    e2e_wall = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = max(e2e_ms_dev / args.steps, 0.0)
+    scal_bytes = 144
+    h2d = 2 * n ** 3 + 2 * 2 * 8 + 36 * 8 + 6 * 6 * 8
+    d2h = 6 * 6 * 8 + scal_bytes * (sum(iters) + sum(refinements) + 6) + 4
+
+    # roofline of the dominant kernel (by device time in the timed region)
+    hbm, peak_kind = peaks()
+    dom = max((k for k in ktimes if ktimes[k][1] > 0 and algo_bytes(k, n) is not None),
+              key=lambda k: ktimes[k][0])
+    avg_ms = ktimes[dom][0] / ktimes[dom][1]
+    achieved = algo_bytes(dom, n) / (avg_ms * 1e-3) / 1e9
+    traffic = traffic_table().get((dom, n))
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 3), "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": algo_bytes(dom, n), "avg_launch_ms": round(avg_ms, 4)}
+    per_kernel = {k: {"ms": round(v[0] / args.steps, 3), "launches": v[1] // args.steps,
+                      "GBps": (round(algo_bytes(k, n) * v[1] / (v[0] * 1e-3) / 1e9, 1)
+                               if v[1] and algo_bytes(k, n) else None)}
+                  for k, v in ktimes.items() if v[1]}
+
+    # FP64 GPU path, same step, once
+    fp64 = None
+    if not args.no_fp64 and rank == 0:
+        ctx64 = make_ctx(ms, n, "fp64", args.tol)
+        ctx64.set_tolerance("L2", "relative", args.tol, 3)
+        ctx64.set_gradient(np.eye(6)[0])
+        ctx64.solve()  # builds the Green's table; 3 iterations as warm-up
+        ctx64.set_tolerance("L2", "relative", args.tol, 2000)
+        st64: list = []
+        t64, C64 = timed_steps(ctx64, 1, lambda: homogenize(ctx64, kref, st64))
+        fp64 = {"ms_per_step": round(t64, 1), "iterations": [s["iterations"] for s in st64],
+                "ceff_rel_diff_mixed_vs_fp64": float(np.linalg.norm(Ceff - C64) / np.linalg.norm(C64)),
+                "speedup_mixed_vs_fp64": round(t64 / ms_step, 2)}
+        ctx64.close()
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        iters_fp64 = fp64["iterations"] if fp64 else iters
+        cb = cpu_baseline(ms, n, args.cpu_iters)
+        cpu_ms = 1e3 * (6 * cb["setup_s"] + cb["per_iter_s"] * sum(iters_fp64))
+        cpu = {"value": round(cpu_ms, 1), "unit": "ms", "cores": cb["cores"], "kind": "port",
+               "sample": (f"oracle (FP64 C restatement, OpenMP) on {n}^3: solver setup + {args.cpu_iters} CG "
+                          f"iterations of load case 11 ({cb['sample_s']:.1f} s), scaled to 6 setups and the six "
+                          f"load cases' FP64 iteration counts {iters_fp64}")}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(ms_step, 2), "unit": "ms", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms_step, 2), "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": f"synthetic: seeded periodic spheres ({nsph}), seed 0, r=6, vf=0.30",
+                "config": {"workload": f"{n}^3 two-phase elastic HEX8, 6 unit load cases, CG rel L2 {args.tol}",
+                           "precision": "mixed: FP32 stencil+FFT inner, FP64 residual/dots/solution",
+                           "l2": "inputs larger than L2 (fields 0.2-0.4 GB each)",
+                           "parallelism": f"replicas{world}" if world > 1 else "single-gpu",
+                           "iterations": iters, "refinements": refinements},
+                "e2e": {"value": round(e2e_ms, 2), "unit": "ms", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "wall_ms": round(e2e_wall, 2)},
+                "gpu_launches": int(launches),
+                "roofline": roofline, "kernels": per_kernel, "fp64_gpu": fp64, "cpu_baseline": cpu,
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -32,8 +32,11 @@ EXPORTS = [
     "fansgpu_solve", "fansgpu_homogenized_stress", "fansgpu_homogenized_tangent", "fansgpu_postprocess_averages",
     "fansgpu_get_field", "fansgpu_set_field", "fansgpu_get_error_history", "fansgpu_extrapolate_displacement",
     "fansgpu_commit_state", "fansgpu_residual", "fansgpu_apply_operator", "fansgpu_convolve",
-    "fansgpu_green_table", "fansgpu_version",
+    "fansgpu_green_table", "fansgpu_version", "fansgpu_reset", "fansgpu_get_stream", "fansgpu_set_timing",
+    "fansgpu_kernel_times",
 ]
+KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
+                "residual64", "norm", "green_table", "strain_stress"]
 
 
 class Desc(ctypes.Structure):
@@ -102,6 +105,10 @@ def _declare(L):
     L.fansgpu_apply_operator.argtypes = [vp, dp, dp]
     L.fansgpu_convolve.argtypes = [vp, dp, dp]
     L.fansgpu_green_table.argtypes = [vp, dp]
+    L.fansgpu_reset.argtypes = [vp]
+    L.fansgpu_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.fansgpu_set_timing.argtypes = [vp, ip]
+    L.fansgpu_kernel_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_int64), ip]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

@@ -61,6 +61,18 @@ struct fansgpu_ctx {
     std::vector<double> err_all;
     int                 iter = 0;
     std::string         err_msg;
+
+    // per-kernel CUDA-event timing (fansgpu_set_timing)
+    struct Span {
+        int id, e0, e1;
+    };
+    bool                     timing = false;
+    std::vector<cudaEvent_t> tpool;
+    int                      tused = 0;
+    std::vector<Span>        spans;
+    double                   ktime[FANSGPU_K_COUNT] = {0};
+    int64_t                  kcount[FANSGPU_K_COUNT] = {0};
+    unsigned int            *max_id = nullptr;
 };
 
 namespace fansgpu {
@@ -161,11 +173,65 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
     return 0;
 }
 
+// -- per-kernel timing: events on the context stream, folded at sync points --
+int tk_mark(fansgpu_ctx *ctx)
+{
+    if (!ctx->timing)
+        return -1;
+    if (ctx->tused >= (int)ctx->tpool.size())
+        return -1;
+    cudaEventRecord(ctx->tpool[ctx->tused], ctx->st);
+    return ctx->tused++;
+}
+void tk_span(fansgpu_ctx *ctx, int id, int e0, int e1)
+{
+    if (e0 >= 0 && e1 >= 0)
+        ctx->spans.push_back({id, e0, e1});
+}
+// reserve k consecutive events (for the convolution passes); null when off
+cudaEvent_t *tk_reserve(fansgpu_ctx *ctx, int k, int *first)
+{
+    *first = -1;
+    if (!ctx->timing || ctx->tused + k > (int)ctx->tpool.size())
+        return nullptr;
+    *first = ctx->tused;
+    ctx->tused += k;
+    return &ctx->tpool[*first];
+}
+void tk_flush(fansgpu_ctx *ctx)
+{
+    if (!ctx->timing)
+        return;
+    for (const auto &sp : ctx->spans) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->tpool[sp.e0], ctx->tpool[sp.e1]) == cudaSuccess) {
+            ctx->ktime[sp.id] += ms;
+            ctx->kcount[sp.id] += 1;
+        }
+    }
+    ctx->spans.clear();
+    ctx->tused = 0;
+}
+
 int sync_scalars(fansgpu_ctx *ctx)
 {
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->scal_h, ctx->scal, sizeof(CgScalars), cudaMemcpyDeviceToHost, ctx->st));
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    tk_flush(ctx);
     return 0;
+}
+
+// timed convolution: the five passes as FANSGPU_K_FFT_* spans
+template <typename T>
+cudaError_t run_conv(fansgpu_ctx *ctx, const ConvPlan<T> &p, ConvArgs ca)
+{
+    int first;
+    ca.ev         = tk_reserve(ctx, 6, &first);
+    cudaError_t e = launch_convolution<T>(p, ca, ctx->st);
+    if (ca.ev)
+        for (int k = 0; k < 5; ++k)
+            tk_span(ctx, FANSGPU_K_FFT_Z_FWD + k, first + k, first + k + 1);
+    return e;
 }
 
 // Per-phase tables, reference stiffness and Green's operator (lazy).
@@ -245,8 +311,11 @@ int setup(fansgpu_ctx *ctx)
         ga.sz  = ga.cz + nzh;
         ga.G64 = ctx->G64;
         ga.G32 = ctx->G32;
+        int e0 = tk_mark(ctx);
         FANS_CUDA_CHECK(launch_green(ga, ctx->st));
+        tk_span(ctx, FANSGPU_K_GREEN, e0, tk_mark(ctx));
         FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        tk_flush(ctx);
         ctx->green_dirty = false;
     }
     if (ctx->force_dirty) {
@@ -280,7 +349,9 @@ int run_stencil(fansgpu_ctx *ctx, const T *x, T *y, bool with_f)
     a.scal   = ctx->scal;
     a.red    = ctx->red;
     a.red_site = SITE_STENCIL;
+    int e0     = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_stencil<T>(a, ctx->st));
+    tk_span(ctx, with_f ? FANSGPU_K_RESIDUAL : FANSGPU_K_STENCIL, e0, tk_mark(ctx));
     return 0;
 }
 
@@ -316,8 +387,10 @@ int solve_cg64(fansgpu_ctx *ctx)
     // r = R(u) (compute_residual<2>, solverCG.h:76)
     if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
         return rc;
+    { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
                                                SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
     if ((rc = sync_scalars(ctx)))
         return rc;
     ctx->iter = 0;
@@ -325,7 +398,7 @@ int solve_cg64(fansgpu_ctx *ctx)
     double err_rel = err_value(ctx, ctx->scal_h->err);
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         ConvArgs ca{ctx->r, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
-        FANS_CUDA_CHECK(launch_convolution<double>(ctx->cp64, ca, ctx->st));
+        FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
         StencilArgs sa{};
         sa.g        = ctx->g;
         sa.C        = ctx->C;
@@ -341,11 +414,15 @@ int solve_cg64(fansgpu_ctx *ctx)
         sa.scal     = ctx->scal;
         sa.red      = ctx->red;
         sa.red_site = SITE_STENCIL;
+        int e0 = tk_mark(ctx);
         FANS_CUDA_CHECK(launch_stencil<double>(sa, ctx->st));
+        tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
         ctx->cur_d ^= 1;
         UpdateArgs ua{n, ctx->r, ctx->Kd, ctx->u, ctx->dd[ctx->cur_d], ctx->s, ctx->tol.measure, 1, ctx->scal,
                       ctx->red, SITE_UPDATE};
+        int e2 = tk_mark(ctx);
         FANS_CUDA_CHECK((launch_cg_update<double, double>(ua, ctx->st)));
+        tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
         if ((rc = sync_scalars(ctx)))
             return rc;
         ctx->iter++;
@@ -373,8 +450,10 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         return rc;
     if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
         return rc;
+    { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, ctx->r32, ctx->red,
                                                SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
     if ((rc = sync_scalars(ctx)))
         return rc;
     ctx->iter = 0;
@@ -384,7 +463,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     double last_true  = ctx->scal_h->err;
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         ConvArgs ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
-        FANS_CUDA_CHECK(launch_convolution<float>(ctx->cp32, ca, ctx->st));
+        FANS_CUDA_CHECK(run_conv<float>(ctx, ctx->cp32, ca));
         StencilArgs sa{};
         sa.g        = ctx->g;
         sa.C        = ctx->C;
@@ -400,11 +479,15 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         sa.scal     = ctx->scal;
         sa.red      = ctx->red;
         sa.red_site = SITE_STENCIL;
+        int e0 = tk_mark(ctx);
         FANS_CUDA_CHECK(launch_stencil<float>(sa, ctx->st));
+        tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
         ctx->cur_d ^= 1;
         UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->u, ctx->d32[ctx->cur_d], ctx->s32, ctx->tol.measure, 1, ctx->scal,
                       ctx->red, SITE_UPDATE};
+        int e2 = tk_mark(ctx);
         FANS_CUDA_CHECK((launch_cg_update<float, double>(ua, ctx->st)));
+        tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
         if ((rc = sync_scalars(ctx)))
             return rc;
         ctx->iter++;
@@ -416,8 +499,10 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
             // reliable update: true residual in FP64, re-seed the FP32 residual
             if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
                 return rc;
-            FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
+            { int en = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
                                                        ctx->red, SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
             if ((rc = sync_scalars(ctx)))
                 return rc;
             (*refinements)++;
@@ -441,8 +526,10 @@ int solve_fp64(fansgpu_ctx *ctx)
         return rc;
     if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
         return rc;
+    { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
                                                SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
     if ((rc = sync_scalars(ctx)))
         return rc;
     ctx->iter = 0;
@@ -450,12 +537,14 @@ int solve_fp64(fansgpu_ctx *ctx)
     double err_rel = err_value(ctx, ctx->scal_h->err);
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         ConvArgs ca{ctx->r, ctx->s, 1.0, 0, ctx->scal, ctx->red, SITE_CONV};
-        FANS_CUDA_CHECK(launch_convolution<double>(ctx->cp64, ca, ctx->st));
+        FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
         FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, ctx->s, -1.0, n, ctx->st));
         if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
             return rc;
-        FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, nullptr, ctx->red,
+        { int en = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, nullptr, ctx->red,
                                                    SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
         if ((rc = sync_scalars(ctx)))
             return rc;
         ctx->iter++;
@@ -485,10 +574,13 @@ int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *
     a.out_red      = ctx->red_out;
     a.red          = ctx->red;
     a.red_site     = SITE_SS;
+    int e0 = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_strain_stress(a, ctx->st));
+    tk_span(ctx, FANSGPU_K_STRAIN_STRESS, e0, tk_mark(ctx));
     FANS_CUDA_CHECK(cudaMemcpyAsync(out, ctx->red_out, sizeof(double) * (2 * ctx->nstr + 1), cudaMemcpyDeviceToHost,
                                     ctx->st));
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    tk_flush(ctx);
     return 0;
 }
 
@@ -570,7 +662,7 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         (rc = dalloc(ctx, &ctx->scal, 1)) || (rc = dalloc(ctx, &ctx->red.partials, (size_t)max_reduction_blocks(ctx->g, ctx->C) * kMaxRed)) ||
         (rc = dalloc(ctx, &ctx->red.counter, kRedSites)) || (rc = dalloc(ctx, &ctx->red_out, 64)) ||
         (rc = dalloc(ctx, &ctx->K0c, NC * NC)) || (rc = dalloc(ctx, &ctx->Bbar_d, ns * NC)) ||
-        (rc = dalloc(ctx, &ctx->g0_d, ns)) ||
+        (rc = dalloc(ctx, &ctx->g0_d, ns)) || (rc = dalloc(ctx, &ctx->max_id, 1)) ||
         (rc = dalloc(ctx, &ctx->trig, 2 * (ctx->g.nx + ctx->g.ny + nzh))))
         return bail(rc);
     if (mixed) {
@@ -639,7 +731,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32,       ctx->K64,
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
-                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out};
+                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -649,6 +741,8 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
         cudaEventDestroy(ctx->ev0);
     if (ctx->ev1)
         cudaEventDestroy(ctx->ev1);
+    for (auto e : ctx->tpool)
+        cudaEventDestroy(e);
     if (ctx->st)
         cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -659,19 +753,73 @@ int fansgpu_set_microstructure(fansgpu_ctx *ctx, const uint16_t *ms)
 {
     if (!ctx || !ms)
         return ctx ? fail(ctx, FANSGPU_EINVAL, "null microstructure") : FANSGPU_EINVAL;
-    std::vector<uint8_t> m8(ctx->N);
-    int                  mx = 0;
-    for (long long i = 0; i < ctx->N; ++i) {
-        if (ms[i] > 255)
-            return fail(ctx, FANSGPU_EUNSUPPORTED, "phase id %u > 255 at voxel %lld", (unsigned)ms[i], i);
-        m8[i] = (uint8_t)ms[i];
-        mx    = std::max(mx, (int)ms[i]);
-    }
-    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->d_ms, m8.data(), ctx->N, cudaMemcpyHostToDevice, ctx->st));
+    // upload as uint16 into the staging buffer, narrow to uint8 on the device
+    uint16_t *ms16 = reinterpret_cast<uint16_t *>(ctx->staging);
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ms16, ms, sizeof(uint16_t) * ctx->N, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->max_id, 0, sizeof(unsigned int), ctx->st));
+    FANS_CUDA_CHECK(launch_ms_convert(ms16, ctx->d_ms, ctx->N, ctx->max_id, ctx->st));
+    unsigned int mx = 0;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(&mx, ctx->max_id, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->st));
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
-    ctx->ms_max       = mx;
+    if (mx > 255) {
+        ctx->have_ms = false;
+        return fail(ctx, FANSGPU_EUNSUPPORTED, "phase id %u > 255: at most 256 phase ids in this build", mx);
+    }
+    ctx->ms_max       = (int)mx;
     ctx->have_ms      = true;
     ctx->tables_dirty = true;
+    return 0;
+}
+
+int fansgpu_reset(fansgpu_ctx *ctx)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->u, 0, sizeof(double) * ctx->n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * ctx->n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->r, 0, sizeof(double) * ctx->n, ctx->st));
+    ctx->err_all.clear();
+    ctx->iter = 0;
+    return 0;
+}
+
+int fansgpu_get_stream(fansgpu_ctx *ctx, void **stream)
+{
+    if (!ctx || !stream)
+        return FANSGPU_EINVAL;
+    *stream = (void *)ctx->st;
+    return 0;
+}
+
+int fansgpu_set_timing(fansgpu_ctx *ctx, int32_t on)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (on && ctx->tpool.empty()) {
+        ctx->tpool.resize(64);
+        for (auto &e : ctx->tpool)
+            FANS_CUDA_CHECK(cudaEventCreate(&e));
+    }
+    ctx->timing = on != 0;
+    for (int k = 0; k < FANSGPU_K_COUNT; ++k) {
+        ctx->ktime[k]  = 0.0;
+        ctx->kcount[k] = 0;
+    }
+    ctx->spans.clear();
+    ctx->tused = 0;
+    return 0;
+}
+
+int fansgpu_kernel_times(fansgpu_ctx *ctx, double *ms_total, int64_t *launches, int32_t n)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    for (int k = 0; k < std::min((int)n, (int)FANSGPU_K_COUNT); ++k) {
+        if (ms_total)
+            ms_total[k] = ctx->ktime[k];
+        if (launches)
+            launches[k] = ctx->kcount[k];
+    }
     return 0;
 }
 

@@ -360,17 +360,24 @@ cudaError_t launch_convolution(const ConvPlan<T> &p, const ConvArgs &a, cudaStre
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
     const int       rz    = z_rows_per_cta(p);
     const int       nbz   = (int)((nrows + rz - 1) / rz);
+    auto mark = [&](int i) {
+        if (a.ev)
+            cudaEventRecord(a.ev[i], st);
+    };
+    mark(0);
     // z forward
     size_t s0 = conv_smem_bytes(p, 0);
     if ((e = set_smem<T>((const void *)k_z_fwd<T>, s0)) != cudaSuccess)
         return e;
     k_z_fwd<T><<<nbz, kFftThreads, s0, st>>>(p, reinterpret_cast<const T *>(a.r), rz);
+    mark(1);
     // y forward
     size_t s1 = conv_smem_bytes(p, 1);
     dim3   gy((p.nzh + p.kc_y - 1) / p.kc_y, p.g.nx, p.C);
     if ((e = set_smem<T>((const void *)k_y<T, false>, s1)) != cudaSuccess)
         return e;
     k_y<T, false><<<gy, kFftThreads, s1, st>>>(p);
+    mark(2);
     // x + Green + x inverse
     size_t s2 = conv_smem_bytes(p, 2);
     dim3   gx((p.nzh + p.kc_x - 1) / p.kc_x, p.g.ny);
@@ -383,15 +390,18 @@ cudaError_t launch_convolution(const ConvPlan<T> &p, const ConvArgs &a, cudaStre
             return e;
         k_x_green<T, 3><<<gx, kFftThreads, s2, st>>>(p);
     }
+    mark(3);
     // y inverse
     if ((e = set_smem<T>((const void *)k_y<T, true>, s1)) != cudaSuccess)
         return e;
     k_y<T, true><<<gy, kFftThreads, s1, st>>>(p);
+    mark(4);
     // z inverse
     size_t s3 = conv_smem_bytes(p, 3);
     if ((e = set_smem<T>((const void *)k_z_inv<T>, s3)) != cudaSuccess)
         return e;
     k_z_inv<T><<<nbz, kFftThreads, s3, st>>>(p, a, rz);
+    mark(5);
     return cudaGetLastError();
 }
 

@@ -102,7 +102,28 @@ __global__ void k_fold(double *__restrict__ u, float *__restrict__ e, long long 
         e[i] = 0.0f;
     }
 }
+__global__ void k_ms_convert(const uint16_t *__restrict__ in, uint8_t *__restrict__ out, long long n,
+                             unsigned int *max_id)
+{
+    unsigned int mx = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned int v = in[i];
+        out[i]               = (uint8_t)(v & 0xffu);
+        mx                   = v > mx ? v : mx;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMax(max_id, mx);
+}
 } // namespace
+
+cudaError_t launch_ms_convert(const uint16_t *in, uint8_t *out, long long n, unsigned int *max_id, cudaStream_t st)
+{
+    k_ms_convert<<<grid_blocks_for(n), kVecThreads, 0, st>>>(in, out, n, max_id);
+    return cudaGetLastError();
+}
 
 template <typename T, typename TU>
 cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st)

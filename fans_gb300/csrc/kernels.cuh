@@ -93,6 +93,7 @@ struct ConvArgs {
     CgScalars  *scal;
     GridRed     red;
     int         red_site;
+    cudaEvent_t *ev; // optional: 6 events recorded around the 5 passes
 };
 template <typename T>
 cudaError_t launch_convolution(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st);
@@ -144,6 +145,10 @@ cudaError_t launch_extrapolate(double *u, double *u_prev, long long n, cudaStrea
 
 // u64 += e32 (mixed precision: fold the FP32 correction into the FP64 solution).
 cudaError_t launch_fold(double *u, float *e, long long n, cudaStream_t st);
+
+// uint16 phase ids -> uint8 on the device, atomically folding the maximum id
+// into *max_id (caller zeroes it).
+cudaError_t launch_ms_convert(const uint16_t *in, uint8_t *out, long long n, unsigned int *max_id, cudaStream_t st);
 
 int grid_blocks_for(long long n);
 

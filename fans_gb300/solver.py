@@ -135,6 +135,28 @@ class Context:
     def extrapolate_displacement(self):
         self._chk(self.lib.fansgpu_extrapolate_displacement(self.ctx))
 
+    def reset(self):
+        """Solver ctor state for a new load case: v_u = v_u_prev = v_r = 0."""
+        self._chk(self.lib.fansgpu_reset(self.ctx))
+
+    def stream(self):
+        """cudaStream_t (as int) of this context."""
+        p = ctypes.c_void_p()
+        self._chk(self.lib.fansgpu_get_stream(self.ctx, ctypes.byref(p)))
+        return p.value or 0
+
+    def set_timing(self, on=True):
+        self._chk(self.lib.fansgpu_set_timing(self.ctx, int(bool(on))))
+
+    def kernel_times(self):
+        """{kernel name: (total ms, launches)} since set_timing(True)."""
+        n = len(C.KERNEL_NAMES)
+        ms = np.zeros(n)
+        cnt = np.zeros(n, dtype=np.int64)
+        self._chk(self.lib.fansgpu_kernel_times(self.ctx, _ptr(ms), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                                n))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(C.KERNEL_NAMES)}
+
     def commit_state(self):
         self._chk(self.lib.fansgpu_commit_state(self.ctx))
 

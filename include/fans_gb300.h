@@ -192,6 +192,34 @@ int fansgpu_convolve(fansgpu_ctx *ctx, const double *r, double *s);
  * [kx][ky][kz] (kz < n_z/2+1) x c(c+1)/2 lower-triangle entries (00,10,11,20,21,22). */
 int fansgpu_green_table(fansgpu_ctx *ctx, double *host);
 
+/* Solver ctor state for a new load case (solver.h:133-137, main.cpp:15-16):
+ * zero v_u, v_u_prev and v_r without reallocating. */
+int fansgpu_reset(fansgpu_ctx *ctx);
+
+/* The CUDA stream (cudaStream_t) all work of this context is ordered on, so a
+ * caller can order its own work or CUDA events against it.  No reference
+ * counterpart (the reference has no device work). */
+int fansgpu_get_stream(fansgpu_ctx *ctx, void **stream);
+
+/* Per-kernel device time.  With timing on, every launch of the solve path is
+ * bracketed by CUDA events on the context stream and accumulated per kernel id
+ * (FANSGPU_K_*).  The reference prints per-iteration FFT and total CPU times
+ * (solver.h:286-298); this is its device-side counterpart. */
+#define FANSGPU_K_STENCIL 0   /* fused d = s + beta d; K d; <d, K d> */
+#define FANSGPU_K_FFT_Z_FWD 1 /* r2c along z */
+#define FANSGPU_K_FFT_Y_FWD 2
+#define FANSGPU_K_FFT_X_GREEN 3 /* x FFT, Green multiply, inverse x FFT */
+#define FANSGPU_K_FFT_Y_INV 4
+#define FANSGPU_K_FFT_Z_INV 5 /* c2r along z, negation, <r, s> */
+#define FANSGPU_K_UPDATE 6    /* r -= a Kd, u -= a d, ||r||, <r, s> */
+#define FANSGPU_K_RESIDUAL 7  /* FP64 R(u) = K u + F */
+#define FANSGPU_K_NORM 8      /* ||r|| (and FP32 re-seed) */
+#define FANSGPU_K_GREEN 9     /* Green's table build */
+#define FANSGPU_K_STRAIN_STRESS 10 /* element strain/stress + volume averages */
+#define FANSGPU_K_COUNT 11
+int fansgpu_set_timing(fansgpu_ctx *ctx, int32_t on);
+int fansgpu_kernel_times(fansgpu_ctx *ctx, double *ms_total, int64_t *launches, int32_t n);
+
 /* Library version string. */
 const char *fansgpu_version(void);
 

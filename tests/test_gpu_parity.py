@@ -1,8 +1,9 @@
 """GPU parity: each hot-path stage and the full solves through the C ABI against
 the FP64 oracle on the same seeded inputs.
 
-Tolerances (FP64 path): Green's table, operator, residual and convolution agree
-to 1e-12 relative (different summation order only); solves agree in
+Tolerances (FP64 path): operator and residual agree to 1e-12 relative
+(different summation order only), Green's table and convolution to 1e-12
+(1e-10 for HEX8R, whose near-hourglass blocks are ill-conditioned); solves agree in
 iteration count within +-1, homogenized stress/flux within 1e-10 relative and
 per-voxel fields within 1e-8 relative.  Mixed path: effective stiffness within
 1e-6 relative of the FP64 oracle and the FP64 true residual below tolerance.
@@ -26,9 +27,14 @@ def test_green_operator_residual_convolution(shape, c, groups, fe):
     P = oracle_problem(ms, c, groups, fe)
     ctx = gpu_context(P)
     rng = np.random.default_rng(7)
-    # Green's table (solver.h:145-204)
+    # Green's table (solver.h:145-204).  Near the HEX8R hourglass frequencies the
+    # block is a small sum of O(1) terms, so 1/lambda carries the summation-order
+    # rounding of any FP64 implementation amplified (observed up to 1.3e-11 in G
+    # and 6.5e-12 in a convolution of white noise, which excites those
+    # frequencies): 1e-10 for HEX8R, 1e-12 otherwise.
+    tol_g = 1e-10 if fe == "HEX8R" else 1e-12
     G = ctx.green_table()
-    assert rel(G, P.G) < 1e-12
+    assert rel(G, P.G) < tol_g
     # operator (solverCG.h:97-103)
     x = rng.standard_normal(shape + (c,))
     assert rel(ctx.apply_operator(x), P.apply_linear(x)) < 1e-12
@@ -38,7 +44,7 @@ def test_green_operator_residual_convolution(shape, c, groups, fe):
     ctx.set_gradient(g0)
     assert rel(ctx.residual(x), P.residual(x)) < 1e-12
     # convolution (solver.h:388-412)
-    assert rel(ctx.convolve(x), P.convolve(x)) < 1e-12
+    assert rel(ctx.convolve(x), P.convolve(x)) < tol_g
     ctx.close()
 
 
