@@ -19,6 +19,11 @@
  *     threshold: for the real symmetric c x c blocks used here the singular
  *     values are |eigenvalues|, computed by cyclic Jacobi rotations.
  *
+ * Parity unpinned: the reference itself cannot be built or run here and its
+ * tests hold no golden values, so this oracle is anchored by an independent
+ * numpy restatement (oracle/numpy_ref.py), known answers (homogeneous media,
+ * laminates) and the invariants the reference's own tests check.
+ *
  * Layouts follow the reference: nodal fields are [x][y][z][c] (c fastest,
  * solver.h:123-127 without the FFTW z padding), the microstructure is
  * uint16 [x][y][z] (reader.cpp:380-398), element index = index of its node 0

@@ -6,7 +6,7 @@ TEST INFRASTRUCTURE ONLY.  This module is the checker for the CUDA product.
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
 arm may import it; the product package never does.
 
-Parity status: the reference (FANS v0.6.2) cannot be built in this image (MPI,
+Parity unpinned: the reference (FANS v0.6.2) cannot be built in this image (MPI,
 FFTW3-MPI, parallel HDF5, Eigen and nlohmann_json are absent) and its own
 tests hold no golden numbers, only invariants.  The oracle is therefore pinned
 by (1) an independent numpy restatement (numpy.fft / LAPACK eigh) of the same
