@@ -116,7 +116,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out);
 int fansgpu_destroy(fansgpu_ctx *ctx);
 
 /* One-line message for the last failing call on this context (NULL ctx: last
- * failure of fansgpu_create). */
+ * failure of a call made without a context: fansgpu_create or
+ * fansgpu_residual_norm_noalloc). */
 const char *fansgpu_last_error(const fansgpu_ctx *ctx);
 
 /* Reader::ReadMS result (reader.cpp:227-411): phase id per voxel, uint16 [x][y][z]. */
@@ -219,6 +220,23 @@ int fansgpu_get_stream(fansgpu_ctx *ctx, void **stream);
 #define FANSGPU_K_COUNT 11
 int fansgpu_set_timing(fansgpu_ctx *ctx, int32_t on);
 int fansgpu_kernel_times(fansgpu_ctx *ctx, double *ms_total, int64_t *launches, int32_t n);
+
+/* Residual norm (the measure of Solver::compute_error) of a field that already
+ * lives in device memory, with no device allocation: no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc -- e.g. a process whose
+ * device memory is all held by another allocator, or code that must not
+ * trigger the device synchronisation cudaMalloc/cudaFree can cause.  Needs no
+ * context.  r_dev: n doubles on the current device; *out_dev (device memory)
+ * receives ||r|| in `measure` (FANSGPU_L1 / L2 / LINF), ordered on `stream`
+ * (a cudaStream_t, NULL = default stream).  The scratch is a static array of
+ * 256 KiB + 256 B that every GPU loading the library holds until exit; n is
+ * limited to FANSGPU_NOALLOC_MAX_VALUES (FANSGPU_EINVAL beyond).  The first
+ * call on a device looks the array's device address up (cudaGetSymbolAddress)
+ * and should come before any stream capture.  All calls on a GPU share the
+ * array: calls that overlap on the GPU race and must be serialised.  Errors are
+ * reported through fansgpu_last_error(NULL). */
+#define FANSGPU_NOALLOC_MAX_VALUES 268435456LL
+int fansgpu_residual_norm_noalloc(const double *r_dev, int64_t n, int32_t measure, double *out_dev, void *stream);
 
 /* Library version string. */
 const char *fansgpu_version(void);
