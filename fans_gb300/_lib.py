@@ -33,7 +33,7 @@ EXPORTS = [
     "fansgpu_get_field", "fansgpu_set_field", "fansgpu_get_error_history", "fansgpu_extrapolate_displacement",
     "fansgpu_commit_state", "fansgpu_residual", "fansgpu_apply_operator", "fansgpu_convolve",
     "fansgpu_green_table", "fansgpu_version", "fansgpu_reset", "fansgpu_get_stream", "fansgpu_set_timing",
-    "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc",
+    "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc", "fansgpu_set_refresh",
 ]
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
                 "residual64", "norm", "green_table", "strain_stress"]
@@ -110,6 +110,7 @@ def _declare(L):
     L.fansgpu_set_timing.argtypes = [vp, ip]
     L.fansgpu_kernel_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_int64), ip]
     L.fansgpu_residual_norm_noalloc.argtypes = [vp, ctypes.c_int64, ip, vp, vp]
+    L.fansgpu_set_refresh.argtypes = [vp, ctypes.c_double]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

@@ -36,13 +36,17 @@ struct fansgpu_ctx {
     bool all_linear = true;
     std::vector<double> kapparef, g0;
     fansgpu_tol tol{FANSGPU_L2, FANSGPU_RELATIVE, 1e-10, 100, 5, 1e-2};
-    double      reliable_delta = 1e-2; // MIXED: true-residual refresh when the FP32 residual fell by this factor
+    double      reliable_delta = 1e-4; // MIXED: true-residual refresh when the FP32 residual fell by this factor
 
     cudaStream_t st = nullptr;
     cudaEvent_t  ev0 = nullptr, ev1 = nullptr;
     uint8_t     *d_ms = nullptr;
     double *u = nullptr, *r = nullptr, *s = nullptr, *dd[2] = {nullptr, nullptr}, *Kd = nullptr, *uprev = nullptr;
-    float  *r32 = nullptr, *s32 = nullptr, *d32[2] = {nullptr, nullptr}, *Kd32 = nullptr;
+    float  *r32 = nullptr, *s32 = nullptr, *d32[2] = {nullptr, nullptr}, *Kd32 = nullptr, *e32 = nullptr;
+    std::vector<double> K64h, f64h; // host copies of the per-phase tables (kernel-parameter path)
+    float              *Kdf = nullptr, *fdf = nullptr; // double-float [hi | lo] tables (mixed refresh)
+    std::vector<float>  K32h;
+    bool                u_zero = true; // v_u known to be zero (fresh context / reset): R(u) = F
     double *K64 = nullptr, *f64 = nullptr, *Cph = nullptr, *Bbar_d = nullptr, *g0_d = nullptr, *K0c = nullptr;
     float  *K32 = nullptr;
     double *G64 = nullptr;
@@ -283,6 +287,23 @@ int setup(fansgpu_ctx *ctx)
         if (!ctx->all_linear)
             return fail(ctx, FANSGPU_EUNSUPPORTED,
                         "J2PlasticityNew (nonlinear CG with secant line search) is not in this build yet");
+        ctx->K64h = K64;
+        ctx->K32h = K32;
+        {
+            std::vector<float> kdf(2 * K64.size());
+            for (size_t i = 0; i < K64.size(); ++i) {
+                const float hi        = (float)K64[i];
+                kdf[i]                = hi;
+                kdf[K64.size() + i]   = (float)(K64[i] - (double)hi);
+            }
+            if (ctx->Kdf)
+                cudaFree(ctx->Kdf);
+            ctx->Kdf = nullptr;
+            int rc2;
+            if ((rc2 = dalloc(ctx, &ctx->Kdf, kdf.size())))
+                return rc2;
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Kdf, kdf.data(), sizeof(float) * kdf.size(), cudaMemcpyHostToDevice, ctx->st));
+        }
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->K64, K64.data(), sizeof(double) * K64.size(), cudaMemcpyHostToDevice, ctx->st));
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->K32, K32.data(), sizeof(float) * K32.size(), cudaMemcpyHostToDevice, ctx->st));
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Cph, Cph.data(), sizeof(double) * Cph.size(), cudaMemcpyHostToDevice, ctx->st));
@@ -325,7 +346,23 @@ int setup(fansgpu_ctx *ctx)
             fe::law_C(ctx->law[ph], ctx->prm[ph], nstr, Cm.data());
             fe::element_force(C, ctx->ngp, ctx->B, Cm.data(), ctx->g0.data(), ctx->ve, &f[ph * NC]);
         }
+        ctx->f64h = f;
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->f64, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice, ctx->st));
+        {
+            std::vector<float> fdf(2 * f.size());
+            for (size_t i = 0; i < f.size(); ++i) {
+                const float hi    = (float)f[i];
+                fdf[i]            = hi;
+                fdf[f.size() + i] = (float)(f[i] - (double)hi);
+            }
+            if (ctx->fdf)
+                cudaFree(ctx->fdf);
+            ctx->fdf = nullptr;
+            int rc2;
+            if ((rc2 = dalloc(ctx, &ctx->fdf, fdf.size())))
+                return rc2;
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->fdf, fdf.data(), sizeof(float) * fdf.size(), cudaMemcpyHostToDevice, ctx->st));
+        }
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->g0_d, ctx->g0.data(), sizeof(double) * nstr, cudaMemcpyHostToDevice, ctx->st));
         FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
         ctx->force_dirty = false;
@@ -345,6 +382,9 @@ int run_stencil(fansgpu_ctx *ctx, const T *x, T *y, bool with_f)
     a.ms     = ctx->d_ms;
     a.Kph    = std::is_same<T, double>::value ? (const void *)ctx->K64 : (const void *)ctx->K32;
     a.fph    = with_f ? ctx->f64 : nullptr;
+    a.Kph_host = std::is_same<T, double>::value ? (const void *)ctx->K64h.data() : (const void *)ctx->K32h.data();
+    a.fph_host = with_f ? ctx->f64h.data() : nullptr;
+    a.force_only = (with_f && (const void *)x == (const void *)ctx->u && ctx->u_zero) ? 1 : 0;
     a.nph    = ctx->nph;
     a.scal   = ctx->scal;
     a.red    = ctx->red;
@@ -352,6 +392,26 @@ int run_stencil(fansgpu_ctx *ctx, const T *x, T *y, bool with_f)
     int e0     = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_stencil<T>(a, ctx->st));
     tk_span(ctx, with_f ? FANSGPU_K_RESIDUAL : FANSGPU_K_STENCIL, e0, tk_mark(ctx));
+    return 0;
+}
+
+// r = R(u) = K u + F with FP64 accuracy from FP32 arithmetic (mixed-path refresh).
+int run_residual_df(fansgpu_ctx *ctx)
+{
+    if (ctx->u_zero)
+        return run_stencil<double>(ctx, ctx->u, ctx->r, true); // r = F, no arithmetic on u
+    StencilArgs a{};
+    a.g        = ctx->g;
+    a.C        = ctx->C;
+    a.x        = ctx->u;
+    a.y        = ctx->r;
+    a.ms       = ctx->d_ms;
+    a.Kph      = ctx->Kdf;
+    a.fph      = ctx->fdf;
+    a.nph      = ctx->nph;
+    int e0     = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_residual_df(a, ctx->st));
+    tk_span(ctx, FANSGPU_K_RESIDUAL, e0, tk_mark(ctx));
     return 0;
 }
 
@@ -396,6 +456,8 @@ int solve_cg64(fansgpu_ctx *ctx)
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
     double err_rel = err_value(ctx, ctx->scal_h->err);
+    if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
+        ctx->u_zero = false; // u is updated from here on
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         ConvArgs ca{ctx->r, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
         FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
@@ -408,6 +470,7 @@ int solve_cg64(fansgpu_ctx *ctx)
         sa.y        = ctx->Kd;
         sa.ms       = ctx->d_ms;
         sa.Kph      = ctx->K64;
+        sa.Kph_host = ctx->K64h.data();
         sa.nph      = ctx->nph;
         sa.fuse_d   = 1;
         sa.reduce   = 1;
@@ -445,10 +508,11 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     int             rc;
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s32, 0, sizeof(float) * n, ctx->st));
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->d32[0], 0, sizeof(float) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->e32, 0, sizeof(float) * n, ctx->st));
     ctx->cur_d = 0;
     if ((rc = init_scalars(ctx)))
         return rc;
-    if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+    if ((rc = run_residual_df(ctx)))
         return rc;
     { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, ctx->r32, ctx->red,
@@ -473,6 +537,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         sa.y        = ctx->Kd32;
         sa.ms       = ctx->d_ms;
         sa.Kph      = ctx->K32;
+        sa.Kph_host = ctx->K32h.data();
         sa.nph      = ctx->nph;
         sa.fuse_d   = 1;
         sa.reduce   = 1;
@@ -483,10 +548,10 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         FANS_CUDA_CHECK(launch_stencil<float>(sa, ctx->st));
         tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
         ctx->cur_d ^= 1;
-        UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->u, ctx->d32[ctx->cur_d], ctx->s32, ctx->tol.measure, 1, ctx->scal,
+        UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->e32, ctx->d32[ctx->cur_d], ctx->s32, ctx->tol.measure, 1, ctx->scal,
                       ctx->red, SITE_UPDATE};
         int e2 = tk_mark(ctx);
-        FANS_CUDA_CHECK((launch_cg_update<float, double>(ua, ctx->st)));
+        FANS_CUDA_CHECK((launch_cg_update<float, float>(ua, ctx->st)));
         tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
         if ((rc = sync_scalars(ctx)))
             return rc;
@@ -496,8 +561,11 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         double est     = ctx->scal_h->err;
         double est_rel = err_value(ctx, est);
         if (est_rel <= ctx->tol.tolerance || est <= ctx->reliable_delta * last_true) {
-            // reliable update: true residual in FP64, re-seed the FP32 residual
-            if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+            // reliable update: fold the FP32 correction into u, true residual in
+            // FP64, re-seed the FP32 residual
+            FANS_CUDA_CHECK(launch_fold(ctx->u, ctx->e32, n, ctx->st));
+            ctx->u_zero = false;
+            if ((rc = run_residual_df(ctx)))
                 return rc;
             { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
@@ -514,6 +582,8 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
             err_rel = std::max(est_rel, ctx->tol.tolerance * (1.0 + 1e-12)); // never accept an estimate
         }
     }
+    // corrections since the last reliable update (n_it reached) belong to u too
+    FANS_CUDA_CHECK(launch_fold(ctx->u, ctx->e32, n, ctx->st));
     return 0;
 }
 
@@ -535,6 +605,8 @@ int solve_fp64(fansgpu_ctx *ctx)
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
     double err_rel = err_value(ctx, ctx->scal_h->err);
+    if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
+        ctx->u_zero = false; // u is updated from here on
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         ConvArgs ca{ctx->r, ctx->s, 1.0, 0, ctx->scal, ctx->red, SITE_CONV};
         FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
@@ -668,7 +740,7 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     if (mixed) {
         if ((rc = dalloc(ctx, &ctx->r32, nn)) || (rc = dalloc(ctx, &ctx->s32, nn)) ||
             (rc = dalloc(ctx, &ctx->d32[0], nn)) || (rc = dalloc(ctx, &ctx->d32[1], nn)) ||
-            (rc = dalloc(ctx, &ctx->Kd32, nn)) || (rc = dalloc(ctx, &ctx->spec32, nspec)) ||
+            (rc = dalloc(ctx, &ctx->Kd32, nn)) || (rc = dalloc(ctx, &ctx->e32, nn)) || (rc = dalloc(ctx, &ctx->spec32, nspec)) ||
             (rc = dalloc(ctx, &ctx->G32, F * NT)))
             return bail(rc);
     }
@@ -728,7 +800,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
     if (ctx->st)
         cudaStreamSynchronize(ctx->st);
     void *ptrs[] = {ctx->d_ms, ctx->u,    ctx->r,      ctx->s,      ctx->dd[0],  ctx->dd[1],      ctx->Kd,
-                    ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32,       ctx->K64,
+                    ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id};
@@ -779,7 +851,18 @@ int fansgpu_reset(fansgpu_ctx *ctx)
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * ctx->n, ctx->st));
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->r, 0, sizeof(double) * ctx->n, ctx->st));
     ctx->err_all.clear();
-    ctx->iter = 0;
+    ctx->iter   = 0;
+    ctx->u_zero = true;
+    return 0;
+}
+
+int fansgpu_set_refresh(fansgpu_ctx *ctx, double factor)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (!(factor > 0.0 && factor < 1.0))
+        return fail(ctx, FANSGPU_EINVAL, "refresh factor must lie in (0, 1)");
+    ctx->reliable_delta = factor;
     return 0;
 }
 
@@ -927,6 +1010,7 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
         rc = solve_cg64(ctx);
     if (rc)
         return rc;
+    ctx->u_zero = ctx->u_zero && ctx->iter == 0;
     FANS_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->st));
     FANS_CUDA_CHECK(cudaEventSynchronize(ctx->ev1));
     float ms = 0;
@@ -1069,6 +1153,8 @@ int fansgpu_set_field(fansgpu_ctx *ctx, int32_t which, const double *host)
         return fail(ctx, FANSGPU_EINVAL, "field %d cannot be set", which);
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, host, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
     FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, dst, ctx->N, ctx->C, ctx->st)));
+    if (which == FANSGPU_FIELD_U)
+        ctx->u_zero = false;
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
     return 0;
 }
@@ -1091,6 +1177,7 @@ int fansgpu_extrapolate_displacement(fansgpu_ctx *ctx)
     if (!ctx)
         return FANSGPU_EINVAL;
     FANS_CUDA_CHECK(launch_extrapolate(ctx->u, ctx->uprev, ctx->n, ctx->st));
+    ctx->u_zero = false;
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
     return 0;
 }

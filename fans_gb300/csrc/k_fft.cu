@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(kFftThreads) k_z_inv(ConvPlan<T> p, ConvArgs a
     cplx<T> *sout = reinterpret_cast<cplx<T> *>(a.s);
     const cplx<T> *rin = reinterpret_cast<const cplx<T> *>(a.r);
     const T  sg  = (T)a.sign;
-    double   dot = 0.0;
+    T        dot = (T)0; // per-thread partial (a few elements), folded into FP64 below
     for (int i = threadIdx.x; i < nl * M; i += blockDim.x) {
         const long long gi = (row0 + i / M) * M + (i % M);
         cplx<T>         z  = Z[(i / M) * M + (i % M)];
@@ -191,11 +191,11 @@ __global__ void __launch_bounds__(kFftThreads) k_z_inv(ConvPlan<T> p, ConvArgs a
         sout[gi] = z;
         if (a.reduce) {
             cplx<T> rv = rin[gi];
-            dot += (double)rv.x * (double)z.x + (double)rv.y * (double)z.y;
+            dot += rv.x * z.x + rv.y * z.y;
         }
     }
     if (a.reduce) {
-        double    v[1]   = {dot};
+        double    v[1]   = {(double)dot};
         const int ops[1] = {RED_SUM};
         block_reduce<1>(v, ops, red_smem);
         if (grid_partial_commit<1>(v, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {

@@ -12,27 +12,42 @@ __device__ __forceinline__ double norm_term(double v, int measure)
     return measure == 1 ? a * a : a; // L2: squares; L1 / Linf: |v|
 }
 
-// r -= alpha*Kd; u -= alpha*d; partial ||r|| and <r, s>  (solverCG.h:105-113, solver.h:415-430)
+// r -= alpha*Kd; u -= alpha*d; partial ||r|| and <r, s>  (solverCG.h:105-113, solver.h:415-430).
+// Element arithmetic in T (FP32 in the mixed inner loop, where u is the FP32
+// correction since the last reliable update, or FP64); partial sums of four
+// strided elements are formed in T and accumulated in FP64.
 template <typename T, typename TU>
 __global__ void __launch_bounds__(kVecThreads) k_cg_update(UpdateArgs a)
 {
     __shared__ double red_smem[32 * 2];
-    const double alpha = a.scal->alpha;
+    const T      alpha = (T)a.scal->alpha;
     T           *r  = reinterpret_cast<T *>(a.r);
     const T     *Kd = reinterpret_cast<const T *>(a.Kd);
     TU          *u  = reinterpret_cast<TU *>(a.u);
     const T     *d  = reinterpret_cast<const T *>(a.d);
     const T     *s  = reinterpret_cast<const T *>(a.s);
     double       nrm = 0.0, rs = 0.0;
-    const bool   mx  = a.measure == 2;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.n; i += (long long)gridDim.x * blockDim.x) {
-        T rv = (T)((double)r[i] - alpha * (double)Kd[i]);
-        r[i] = rv;
-        if (a.do_u)
-            u[i] = (TU)((double)u[i] - alpha * (double)d[i]);
-        double t = norm_term((double)rv, a.measure);
-        nrm      = mx ? fmax(nrm, t) : nrm + t;
-        rs += (double)rv * (double)s[i];
+    const int    measure = a.measure;
+    const bool   mx  = measure == 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = blockIdx.x * (long long)blockDim.x + threadIdx.x; base < a.n; base += 4 * stride) {
+        T cn = (T)0, crs = (T)0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long i = base + j * stride;
+            if (i < a.n) {
+                const T rv = r[i] - alpha * Kd[i];
+                r[i]       = rv;
+                if (a.do_u)
+                    u[i] = u[i] - (TU)alpha * (TU)d[i];
+                const T av = rv < (T)0 ? -rv : rv;
+                const T t  = measure == 1 ? av * av : av;
+                cn         = mx ? (t > cn ? t : cn) : cn + t;
+                crs += rv * s[i];
+            }
+        }
+        nrm = mx ? fmax(nrm, (double)cn) : nrm + (double)cn;
+        rs += (double)crs;
     }
     double v[2]   = {nrm, rs};
     int    ops[2] = {mx ? RED_MAX : RED_SUM, RED_SUM};
@@ -132,7 +147,6 @@ cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 template cudaError_t launch_cg_update<double, double>(const UpdateArgs &, cudaStream_t);
-template cudaError_t launch_cg_update<float, double>(const UpdateArgs &, cudaStream_t);
 template cudaError_t launch_cg_update<float, float>(const UpdateArgs &, cudaStream_t);
 
 template <typename T, typename TO>

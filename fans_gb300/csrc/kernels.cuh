@@ -29,17 +29,25 @@ struct StencilArgs {
     void          *d_new;  // fuse_d only
     void          *y;
     const uint8_t *ms;
-    const void    *Kph;    // nph * 64*C*C
-    const void    *fph;    // nph * 8C, or null
+    const void    *Kph;    // nph * 64*C*C (device)
+    const void    *fph;    // nph * 8C, or null (device)
+    const void    *Kph_host; // host copies of the same tables (kernel-parameter path)
+    const void    *fph_host;
     int            nph;
     int            fuse_d;
     int            reduce; // 1: <x,y> -> scal (dAd, alpha)
+    int            force_only; // y = F only (x known to be zero)
     CgScalars     *scal;
     GridRed        red;
     int            red_site;
 };
 template <typename T>
 cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st);
+
+// R(u) = K u + F in double-float (FP32 pairs with error-free transformations):
+// x = u (FP64 SoA), y = r (FP64), Kph = FP32 [hi | lo] tables (2 x nph x 64C^2),
+// fph = FP64 force table.  FP64-accurate true residual at FP32 issue rates.
+cudaError_t launch_residual_df(const StencilArgs &a, cudaStream_t st);
 
 // Element-averaged strain/stress of linear laws (matmodel.h:203-225,
 // solver.h:708-737): eps_e = Bbar u_e + g0, sig_e = C_ph eps_e.  Sums over the

@@ -145,6 +145,10 @@ class Context:
         self._chk(self.lib.fansgpu_get_stream(self.ctx, ctypes.byref(p)))
         return p.value or 0
 
+    def set_refresh(self, factor):
+        """Mixed precision: FP32-residual reduction that triggers an FP64 refresh."""
+        self._chk(self.lib.fansgpu_set_refresh(self.ctx, float(factor)))
+
     def set_timing(self, on=True):
         self._chk(self.lib.fansgpu_set_timing(self.ctx, int(bool(on))))
 

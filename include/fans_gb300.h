@@ -238,6 +238,11 @@ int fansgpu_kernel_times(fansgpu_ctx *ctx, double *ms_total, int64_t *launches, 
 #define FANSGPU_NOALLOC_MAX_VALUES 268435456LL
 int fansgpu_residual_norm_noalloc(const double *r_dev, int64_t n, int32_t measure, double *out_dev, void *stream);
 
+/* MIXED precision: the factor by which the FP32 residual must fall since the
+ * last FP64 true-residual refresh before the next one (default 1e-4; (0, 1)).
+ * No reference counterpart (the reference runs in FP64 only). */
+int fansgpu_set_refresh(fansgpu_ctx *ctx, double factor);
+
 /* Library version string. */
 const char *fansgpu_version(void);
 
