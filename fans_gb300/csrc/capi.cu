@@ -171,8 +171,9 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
     kc     = 16;
     while (kc > 1 && cs * (2 * (size_t)p.C * g.nx * kc + g.nx) > budget)
         kc /= 2;
-    p.kc_x = kc;
-    if (cs * (2 * (size_t)p.C * g.nx * p.kc_x + g.nx) > 200 * 1024)
+    p.kc_x    = kc;
+    p.use_reg = conv_reg_supported(g) ? 1 : 0;
+    if (!p.use_reg && cs * (2 * (size_t)p.C * g.nx * p.kc_x + g.nx) > 200 * 1024)
         return fail(ctx, FANSGPU_EUNSUPPORTED, "n_x=%d too large for the shared-memory x pass", g.nx);
     return 0;
 }

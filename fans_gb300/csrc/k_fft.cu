@@ -356,6 +356,8 @@ size_t conv_smem_bytes(const ConvPlan<T> &p, int pass)
 template <typename T>
 cudaError_t launch_convolution(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
 {
+    if (p.use_reg)
+        return launch_convolution_reg<T>(p, a, st);
     cudaError_t     e;
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
     const int       rz    = z_rows_per_cta(p);

@@ -1,0 +1,394 @@
+// k_fft_reg.cu -- register-resident convolution passes (two-phase line FFTs).
+//
+// Same five passes and spectrum layout as k_fft.cu, but each line lives in
+// registers: threads load their strided values straight from global memory
+// (128-byte rows), transform in registers, and meet once in shared memory per
+// line transform.  Shared memory holds one copy of the tile (no ping-pong), so
+// more CTAs are resident.  Used for line lengths with a register plan
+// (reg_n1(n) != 0); other sizes use the shared-memory Stockham passes.
+#include "fft_reg.cuh"
+#include "kernels.cuh"
+
+namespace fansgpu {
+
+namespace {
+
+template <typename T>
+struct KCol {
+    static constexpr int value = 128 / (int)sizeof(cplx<T>); // kz columns per CTA: one 128-byte row segment
+};
+
+// ------------------------------------------------------------------ y pass ---
+template <typename T, int N1, int N2, bool INV>
+__global__ void __launch_bounds__(KCol<T>::value * N1) k_y_reg(ConvPlan<T> p)
+{
+    constexpr int KC = KCol<T>::value, n = N1 * N2;
+    __shared__ cplx<T> S[n * KC];
+    const int t = threadIdx.x, l = t % KC, w = t / KC;
+    const int kz0 = blockIdx.x * KC, x = blockIdx.y, comp = blockIdx.z;
+    const bool valid = l < p.nzh - kz0;
+    cplx<T> *base = p.spec + ((long long)comp * p.g.nx + x) * (long long)p.g.ny * p.nzp + kz0 + l;
+    cplx<T>  v[N2];
+#pragma unroll
+    for (int j2 = 0; j2 < N2; ++j2)
+        v[j2] = valid ? base[(long long)(w + N1 * j2) * p.nzp] : cplx<T>{0, 0};
+    line_phase1<T, N1, N2, INV>(v, w, p.tw_y);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2)
+        S[(k2 * N1 + w) * KC + l] = v[k2];
+    __syncthreads();
+    if (w < N2) {
+        cplx<T> u[N1];
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1)
+            u[j1] = S[(w * N1 + j1) * KC + l];
+        Dft<T, N1, INV>::run(u);
+        if (valid)
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1)
+                base[(long long)(w + N2 * k1) * p.nzp] = u[k1];
+    }
+}
+
+// ----------------------------------------------------- x pass + Green's op ---
+template <typename T, int N1, int N2, int C>
+__global__ void __launch_bounds__(C * KCol<T>::value * N1) k_x_green_reg(ConvPlan<T> p)
+{
+    constexpr int KC = KCol<T>::value, n = N1 * N2, NT = C * (C + 1) / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T>  *F  = reinterpret_cast<cplx<T> *>(smem_raw); // [C][n][KC]
+    const int nx = n, ny = p.g.ny;
+    const int t = threadIdx.x, comp = t / (KC * N1), rem = t % (KC * N1), w = rem / KC, l = rem % KC;
+    const int kz0 = blockIdx.x * KC, ky = blockIdx.y;
+    const int nk  = min(KC, p.nzh - kz0);
+    const bool valid = l < nk;
+    cplx<T> *gbase = p.spec + ((long long)comp * nx * ny + ky) * p.nzp + kz0 + l; // + x * ny * nzp
+    const long long xstride = (long long)ny * p.nzp;
+    cplx<T> *Fc = F + (size_t)comp * n * KC;
+
+    // forward FFT along x
+    cplx<T> v[N2];
+#pragma unroll
+    for (int j2 = 0; j2 < N2; ++j2)
+        v[j2] = valid ? gbase[(w + N1 * j2) * xstride] : cplx<T>{0, 0};
+    line_phase1<T, N1, N2, false>(v, w, p.tw_x);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2)
+        Fc[(k2 * N1 + w) * KC + l] = v[k2];
+    __syncthreads();
+    cplx<T> u[N1];
+    if (w < N2)
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1)
+            u[j1] = Fc[(w * N1 + j1) * KC + l];
+    __syncthreads();
+    if (w < N2) {
+        Dft<T, N1, false>::run(u);
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1)
+            Fc[(w + N2 * k1) * KC + l] = u[k1];
+    }
+    __syncthreads();
+
+    // Green's operator: C x C real symmetric per frequency (solver.h:400-406)
+    for (int i = t; i < n * KC; i += blockDim.x) {
+        const int kx = i / KC, ll = i % KC;
+        if (ll >= nk)
+            continue;
+        const T *g = p.G + (((long long)kx * ny + ky) * p.nzh + kz0 + ll) * NT;
+        T        gm[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q)
+            gm[q] = g[q];
+        cplx<T> a[C], o[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            a[c] = F[((size_t)c * n + kx) * KC + ll];
+#pragma unroll
+        for (int r = 0; r < C; ++r) {
+            cplx<T> acc = {0, 0};
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int ia = r > c ? r : c, ib = r > c ? c : r;
+                const T   gv = gm[ia * (ia + 1) / 2 + ib];
+                acc.x += gv * a[c].x;
+                acc.y += gv * a[c].y;
+            }
+            o[r] = acc;
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            F[((size_t)c * n + kx) * KC + ll] = o[c];
+    }
+    __syncthreads();
+
+    // inverse FFT along x
+#pragma unroll
+    for (int j2 = 0; j2 < N2; ++j2)
+        v[j2] = Fc[(w + N1 * j2) * KC + l];
+    __syncthreads();
+    line_phase1<T, N1, N2, true>(v, w, p.tw_x);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2)
+        Fc[(k2 * N1 + w) * KC + l] = v[k2];
+    __syncthreads();
+    if (w < N2) {
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1)
+            u[j1] = Fc[(w * N1 + j1) * KC + l];
+        Dft<T, N1, true>::run(u);
+        if (valid)
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1)
+                gbase[(w + N2 * k1) * xstride] = u[k1];
+    }
+}
+
+// ------------------------------------------------------------------ z fwd ---
+// r2c of R rows per CTA: complex half-length line (z_m = x_2m + i x_2m+1), then
+// X_k = (Z_k + conj Z_{M-k})/2 - i W^k (Z_k - conj Z_{M-k})/2, k = 0..M.
+template <typename T, int N1, int N2, int R>
+__global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__restrict__ r)
+{
+    constexpr int M = N1 * N2, EP = N1 + 1; // exchange row padded against bank conflicts
+    __shared__ cplx<T> E[R * N2 * EP];
+    __shared__ cplx<T> Z[R * M];
+    const int       t = threadIdx.x, L = t / N1, w = t % N1;
+    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    const long long row   = (long long)blockIdx.x * R + L;
+    const bool      valid = row < nrows;
+    const cplx<T>  *rin   = reinterpret_cast<const cplx<T> *>(r) + row * M;
+    cplx<T>         v[N2];
+#pragma unroll
+    for (int j2 = 0; j2 < N2; ++j2)
+        v[j2] = valid ? rin[w + N1 * j2] : cplx<T>{0, 0};
+    line_phase1<T, N1, N2, false>(v, w, p.tw_z);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2)
+        E[(L * N2 + k2) * EP + w] = v[k2];
+    __syncthreads();
+    if (w < N2) {
+        cplx<T> u[N1];
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1)
+            u[j1] = E[(L * N2 + w) * EP + j1];
+        Dft<T, N1, false>::run(u);
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1)
+            Z[L * M + w + N2 * k1] = u[k1];
+    }
+    __syncthreads();
+    // unpack to the half spectrum, k = 0..M, coalesced over k
+    const long long row0 = (long long)blockIdx.x * R;
+    for (int i = t; i < R * (M + 1); i += blockDim.x) {
+        const int Lr = i / (M + 1), k = i % (M + 1);
+        if (row0 + Lr >= nrows)
+            continue;
+        cplx<T> zk = Z[Lr * M + (k == M ? 0 : k)];
+        cplx<T> zm = Z[Lr * M + (k == 0 ? 0 : M - k)];
+        zm.y       = -zm.y;
+        cplx<T> Ev = {(T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y + zm.y)};
+        cplx<T> Od = {(T)0.5 * (zk.x - zm.x), (T)0.5 * (zk.y - zm.y)};
+        cplx<T> P  = cmul(p.tw_r2c[k], Od);
+        p.spec[(row0 + Lr) * p.nzp + k] = cplx<T>{Ev.x + P.y, Ev.y - P.x};
+    }
+}
+
+// ------------------------------------------------------------------ z inv ---
+// Hermitian pack of the half spectrum, half-length inverse, real rows scaled by
+// `sign`; fused partial <r, s> (solverCG.h:90-92) with delta/beta in the last block.
+template <typename T, int N1, int N2, int R>
+__global__ void __launch_bounds__(R * N1) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
+{
+    constexpr int M = N1 * N2, EP = N1 + 1;
+    __shared__ cplx<T> X[R * (M + N2)]; // spectrum rows (stride M+1), then the exchange (R*N2*EP)
+    __shared__ cplx<T> Zp[R * M];
+    __shared__ double  red_smem[32];
+    const int       t = threadIdx.x, L = t / N1, w = t % N1;
+    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    const long long row0  = (long long)blockIdx.x * R;
+    for (int i = t; i < R * (M + 1); i += blockDim.x) {
+        const int Lr = i / (M + 1), k = i % (M + 1);
+        X[i] = (row0 + Lr < nrows) ? p.spec[(row0 + Lr) * p.nzp + k] : cplx<T>{0, 0};
+    }
+    __syncthreads();
+    for (int i = t; i < R * M; i += blockDim.x) {
+        const int Lr = i / M, k = i % M;
+        cplx<T>   xk = X[Lr * (M + 1) + k];
+        cplx<T>   xm = X[Lr * (M + 1) + (M - k)];
+        if (k == 0) {
+            xk.y = 0;
+            xm.y = 0;
+        }
+        xm.y      = -xm.y;
+        cplx<T> Ev = cadd(xk, xm);
+        cplx<T> Od = cmulc(csub(xk, xm), p.tw_r2c[k]);
+        Zp[i]      = cplx<T>{Ev.x - Od.y, Ev.y + Od.x};
+    }
+    __syncthreads();
+    cplx<T> *E = X; // reuse as the exchange buffer: R * N2 * EP = R * (M + N2)
+    cplx<T>  v[N2];
+#pragma unroll
+    for (int j2 = 0; j2 < N2; ++j2)
+        v[j2] = Zp[L * M + w + N1 * j2];
+    line_phase1<T, N1, N2, true>(v, w, p.tw_z);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2)
+        E[(L * N2 + k2) * EP + w] = v[k2];
+    __syncthreads();
+    const long long row   = row0 + L;
+    const bool      valid = row < nrows && w < N2;
+    T               dot   = (T)0;
+    if (valid) {
+        cplx<T> u[N1];
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1)
+            u[j1] = E[(L * N2 + w) * EP + j1];
+        Dft<T, N1, true>::run(u);
+        cplx<T>       *sout = reinterpret_cast<cplx<T> *>(a.s) + row * M;
+        const cplx<T> *rin  = reinterpret_cast<const cplx<T> *>(a.r) + row * M;
+        const T        sg   = (T)a.sign;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) {
+            const int m = w + N2 * k1;
+            cplx<T>   z = {sg * u[k1].x, sg * u[k1].y};
+            sout[m]     = z;
+            if (a.reduce) {
+                const cplx<T> rv = rin[m];
+                dot += rv.x * z.x + rv.y * z.y;
+            }
+        }
+    }
+    if (a.reduce) {
+        double    vv[1]  = {(double)dot};
+        const int ops[1] = {RED_SUM};
+        block_reduce<1>(vv, ops, red_smem);
+        if (grid_partial_commit<1>(vv, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+            grid_final<1>(vv, ops, a.red.partials, gridDim.x, red_smem);
+            if (threadIdx.x == 0) {
+                CgScalars *s = a.scal;
+                s->delta0    = s->delta;
+                s->delta     = vv[0];
+                double beta  = (s->delta - s->deltamid) / s->delta0;
+                s->beta      = beta > 0.0 ? beta : 0.0;
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------- dispatch ---
+template <typename T, int N1, int N2, bool INV>
+void go_y(const ConvPlan<T> &p, cudaStream_t st)
+{
+    constexpr int KC = KCol<T>::value;
+    dim3          g((p.nzh + KC - 1) / KC, p.g.nx, p.C);
+    k_y_reg<T, N1, N2, INV><<<g, KC * N1, 0, st>>>(p);
+}
+
+template <typename T, int N1, int N2>
+cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
+{
+    constexpr int KC = KCol<T>::value;
+    dim3          g((p.nzh + KC - 1) / KC, p.g.ny);
+    if (p.C == 1) {
+        const size_t sm = sizeof(cplx<T>) * (size_t)N1 * N2 * KC;
+        cudaError_t  e  = cudaFuncSetAttribute(k_x_green_reg<T, N1, N2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess)
+            return e;
+        k_x_green_reg<T, N1, N2, 1><<<g, KC * N1, sm, st>>>(p);
+    } else {
+        const size_t sm = sizeof(cplx<T>) * (size_t)3 * N1 * N2 * KC;
+        cudaError_t  e  = cudaFuncSetAttribute(k_x_green_reg<T, N1, N2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess)
+            return e;
+        k_x_green_reg<T, N1, N2, 3><<<g, 3 * KC * N1, sm, st>>>(p);
+    }
+    return cudaSuccess;
+}
+
+// rows per CTA of the z passes: 256 (FP32) or 128 (FP64) threads
+template <typename T, int N1>
+struct ZRows {
+    static constexpr int value = (sizeof(T) == 4 ? 256 : 128) / N1;
+};
+
+template <typename T, int N1, int N2>
+void go_zf(const ConvPlan<T> &p, const T *r, cudaStream_t st)
+{
+    constexpr int   R     = ZRows<T, N1>::value;
+    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    k_z_fwd_reg<T, N1, N2, R><<<(int)((nrows + R - 1) / R), R * N1, 0, st>>>(p, r);
+}
+
+template <typename T, int N1, int N2>
+void go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
+{
+    constexpr int   R     = ZRows<T, N1>::value;
+    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    k_z_inv_reg<T, N1, N2, R><<<(int)((nrows + R - 1) / R), R * N1, 0, st>>>(p, a);
+}
+
+// call F<N1, N2>() for the register plan of length n; false if none
+template <typename Fn>
+bool with_plan(int n, Fn &&f)
+{
+    switch (n) {
+    case 16: f.template operator()<4, 4>(); return true;
+    case 24: f.template operator()<8, 3>(); return true;
+    case 32: f.template operator()<8, 4>(); return true;
+    case 40: f.template operator()<8, 5>(); return true;
+    case 48: f.template operator()<8, 6>(); return true;
+    case 64: f.template operator()<8, 8>(); return true;
+    case 80: f.template operator()<16, 5>(); return true;
+    case 96: f.template operator()<16, 6>(); return true;
+    case 128: f.template operator()<16, 8>(); return true;
+    case 256: f.template operator()<16, 16>(); return true;
+    default: return false;
+    }
+}
+
+// z-pass plans (M <= 128)
+template <typename Fn>
+bool with_plan_z(int n, Fn &&f)
+{
+    return n <= 128 && with_plan(n, f);
+}
+
+} // namespace
+
+bool conv_reg_supported(const Grid3 &g)
+{
+    // z passes keep R rows of M complex twice in static shared memory: M <= 128
+    return reg_n1(g.nx) && reg_n1(g.ny) && reg_n1(g.nz / 2) && g.nz / 2 <= 128;
+}
+
+template <typename T>
+cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
+{
+    if (!conv_reg_supported(p.g))
+        return cudaErrorNotSupported;
+    auto mark = [&](int i) {
+        if (a.ev)
+            cudaEventRecord(a.ev[i], st);
+    };
+    cudaError_t e = cudaSuccess;
+    mark(0);
+    with_plan_z(p.M, [&]<int N1, int N2>() { go_zf<T, N1, N2>(p, reinterpret_cast<const T *>(a.r), st); });
+    mark(1);
+    with_plan(p.g.ny, [&]<int N1, int N2>() { go_y<T, N1, N2, false>(p, st); });
+    mark(2);
+    with_plan(p.g.nx, [&]<int N1, int N2>() { e = go_x<T, N1, N2>(p, st); });
+    if (e != cudaSuccess)
+        return e;
+    mark(3);
+    with_plan(p.g.ny, [&]<int N1, int N2>() { go_y<T, N1, N2, true>(p, st); });
+    mark(4);
+    with_plan_z(p.M, [&]<int N1, int N2>() { go_zi<T, N1, N2>(p, a, st); });
+    mark(5);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_convolution_reg<double>(const ConvPlan<double> &, const ConvArgs &, cudaStream_t);
+template cudaError_t launch_convolution_reg<float>(const ConvPlan<float> &, const ConvArgs &, cudaStream_t);
+
+} // namespace fansgpu

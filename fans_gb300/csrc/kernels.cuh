@@ -89,6 +89,7 @@ struct ConvPlan {
     cplx<T>       *spec;           // C * nx * ny * nzp
     const T       *G;              // nx*ny*nzh*C(C+1)/2
     int            kc_y, kc_x;     // kz columns per CTA in the y / x passes
+    int            use_reg;        // register-resident passes (conv_reg_supported)
 };
 
 // s = sign * IFFT(G . FFT(r)); with reduce, <r, s> -> scal (delta0, delta,
@@ -107,6 +108,10 @@ template <typename T>
 cudaError_t launch_convolution(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st);
 template <typename T>
 size_t conv_smem_bytes(const ConvPlan<T> &p, int pass);
+// register-resident passes (line lengths with a two-phase register plan)
+bool conv_reg_supported(const Grid3 &g);
+template <typename T>
+cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st);
 
 // Green's table (solver.h:145-204) in FP64, optionally also rounded to FP32.
 struct GreenArgs {

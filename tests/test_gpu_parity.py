@@ -16,7 +16,9 @@ from helpers import ELASTIC, THERMAL, gpu_context, oracle_problem, random_ms, re
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(8, 6, 10), (16, 16, 16), (12, 20, 8), (6, 10, 48)]
+# the first four use the shared-memory Stockham passes, the last three the
+# register-resident passes (line lengths 16..256 with a two-phase plan)
+SHAPES = [(8, 6, 10), (16, 16, 16), (12, 20, 8), (6, 10, 48), (16, 24, 32), (24, 32, 48), (48, 16, 64)]
 
 
 @pytest.mark.parametrize("fe", ["HEX8", "HEX8R", "BBAR"])
@@ -50,7 +52,8 @@ def test_green_operator_residual_convolution(shape, c, groups, fe):
 
 @pytest.mark.parametrize("measure,etype,tol", [("L2", "relative", 1e-10), ("Linfinity", "absolute", 1e-10),
                                                 ("L1", "relative", 1e-8)])
-@pytest.mark.parametrize("c,groups,shape", [(1, THERMAL, (16, 16, 16)), (3, ELASTIC, (16, 12, 20))])
+@pytest.mark.parametrize("c,groups,shape", [(1, THERMAL, (16, 16, 16)), (3, ELASTIC, (16, 12, 20)),
+                                            (3, ELASTIC, (32, 32, 32))])
 def test_cg_solve_fp64(c, groups, shape, measure, etype, tol):
     ms = random_ms(shape, vf=0.3, seed=3)
     P = oracle_problem(ms, c, groups, "HEX8")
@@ -91,12 +94,13 @@ def test_fp_solve_fp64(c, groups):
     ctx.close()
 
 
-def test_mixed_precision_effective_stiffness():
+@pytest.mark.parametrize("n", [24, 32])
+def test_mixed_precision_effective_stiffness(n):
     """Elastic C_eff from 6 unit-strain solves: mixed path vs FP64 oracle."""
-    shape = (24, 24, 24)
+    shape = (n, n, n)
     from fans_gb300.microstructure import spheres
 
-    ms, _ = spheres(24, 3, 0.3, seed=1)
+    ms, _ = spheres(n, 3, 0.3, seed=1)
     P = oracle_problem(ms, 3, ELASTIC, "HEX8")
     C_ref = P.homogenized_tangent_unit(measure="L2", type="relative", tol=1e-8, n_it=500)
     ctx = gpu_context(P, precision="mixed")
