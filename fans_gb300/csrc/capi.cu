@@ -516,7 +516,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     if ((rc = run_residual_df(ctx)))
         return rc;
     { int en = tk_mark(ctx);
-    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, ctx->r32, ctx->red,
+    FANS_CUDA_CHECK(launch_norm_fast(ctx->r, n, ctx->tol.measure, ctx->scal, 1, ctx->r32, ctx->red,
                                                SITE_NORM, ctx->st));
     tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
     if ((rc = sync_scalars(ctx)))
@@ -569,7 +569,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
             if ((rc = run_residual_df(ctx)))
                 return rc;
             { int en = tk_mark(ctx);
-    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
+    FANS_CUDA_CHECK(launch_norm_fast(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
                                                        ctx->red, SITE_NORM, ctx->st));
     tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
             if ((rc = sync_scalars(ctx)))
@@ -637,7 +637,8 @@ int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *
     a.nstr         = ctx->nstr;
     a.u            = ctx->u;
     a.ms           = ctx->d_ms;
-    a.Bbar         = ctx->Bbar_d;
+    for (int d = 0; d < 3; ++d)
+        a.inv4l[d] = 0.25 / ctx->le[d];
     a.Cph          = ctx->Cph;
     a.g0           = ctx->g0_d;
     a.nph          = ctx->nph;

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kStencilThreads) k_stencil(StencilArgs a)
     const T     *xin  = reinterpret_cast<const T *>(a.x);
     const T     *dold = reinterpret_cast<const T *>(a.d_old);
     const double beta = a.fuse_d ? a.scal->beta : 0.0;
-    for (int i = tid; i < HX * HY * HZ; i += blockDim.x) {
+    for (int i = tid; i < (a.force_only ? 0 : HX * HY * HZ); i += blockDim.x) {
         int hz = i % HZ, hy = (i / HZ) % HY, hx = i / (HZ * HY);
         int gx = pmod(x0 - 1 + hx, nx), gy = pmod(y0 - 1 + hy, ny), gz = pmod(z0 - 1 + hz, nz);
         long long gi = ((long long)gx * ny + gy) * nz + gz;
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kStencilThreads) k_stencil(StencilArgs a)
         T         ctr[C];
 #pragma unroll
         for (int c = 0; c < C; ++c)
-            ctr[c] = xs[c * HX * HY * HZ + hc];
+            ctr[c] = a.force_only ? (T)0 : xs[c * HX * HY * HZ + hc];
         T acc[C];
 #pragma unroll
         for (int c = 0; c < C; ++c)
@@ -99,17 +99,19 @@ __global__ void __launch_bounds__(kStencilThreads) k_stencil(StencilArgs a)
             const int ex = tx - a0 + 1, ey = ty - b0 + 1, ez = tz - c0 + 1; // element-tile coords
             const int ph = mss[(ex * EY + ey) * EZ + ez];
             const T  *Kr = Ks + (size_t)ph * NC * NC + (size_t)(p * C) * NC;
+            if (!a.force_only) {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int qa = q & 1, qb = (q >> 1) & 1, qc = (q >> 2) & 1;
-                // node e + q in halo coordinates: (tx - a0 + qa + 1, ...)
-                const int hq = ((tx - a0 + qa + 1) * HY + (ty - b0 + qb + 1)) * HZ + (tz - c0 + qc + 1);
+                for (int q = 0; q < 8; ++q) {
+                    const int qa = q & 1, qb = (q >> 1) & 1, qc = (q >> 2) & 1;
+                    // node e + q in halo coordinates: (tx - a0 + qa + 1, ...)
+                    const int hq = ((tx - a0 + qa + 1) * HY + (ty - b0 + qb + 1)) * HZ + (tz - c0 + qc + 1);
 #pragma unroll
-                for (int cb = 0; cb < C; ++cb) {
-                    const T v = xs[cb * HX * HY * HZ + hq] - ctr[cb];
+                    for (int cb = 0; cb < C; ++cb) {
+                        const T v = xs[cb * HX * HY * HZ + hq] - ctr[cb];
 #pragma unroll
-                    for (int cr = 0; cr < C; ++cr)
-                        acc[cr] += Kr[cr * NC + q * C + cb] * v;
+                        for (int cr = 0; cr < C; ++cr)
+                            acc[cr] += Kr[cr * NC + q * C + cb] * v;
+                    }
                 }
             }
             if (a.fph) {
@@ -343,13 +345,10 @@ cudaError_t launch_stencil_c(const StencilArgs &a, cudaStream_t st)
 template <int C, int NSTR>
 __global__ void __launch_bounds__(256) k_strain_stress(StrainStressArgs a)
 {
-    __shared__ double Bs[NSTR * 8 * C];
     __shared__ double Cs[16 * NSTR * NSTR];
     __shared__ double red_smem[32 * (2 * NSTR + 1)];
     const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
     const long long N = (long long)nx * ny * nz;
-    for (int i = threadIdx.x; i < NSTR * 8 * C; i += blockDim.x)
-        Bs[i] = a.Bbar[i];
     for (int i = threadIdx.x; i < a.nph * NSTR * NSTR; i += blockDim.x)
         Cs[i] = a.Cph[i];
     __syncthreads();
@@ -373,19 +372,33 @@ __global__ void __launch_bounds__(256) k_strain_stress(StrainStressArgs a)
         idx[5] = ((long long)x1 * ny + y) * nz + z1;
         idx[6] = ((long long)x * ny + y1) * nz + z1;
         idx[7] = ((long long)x1 * ny + y1) * nz + z1;
+        // GP-averaged gradient = gradient at the element centre (true for HEX8,
+        // HEX8R and BBAR): mean of the four edge differences per direction.
+        double g[C][3];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            double u[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                u[q] = a.u[c * N + idx[q]];
+            g[c][0] = ((u[1] - u[0]) + (u[3] - u[2]) + (u[5] - u[4]) + (u[7] - u[6])) * a.inv4l[0];
+            g[c][1] = ((u[2] - u[0]) + (u[3] - u[1]) + (u[6] - u[4]) + (u[7] - u[5])) * a.inv4l[1];
+            g[c][2] = ((u[4] - u[0]) + (u[5] - u[1]) + (u[6] - u[2]) + (u[7] - u[3])) * a.inv4l[2];
+        }
         double eps[NSTR];
+        if (C == 1) {
 #pragma unroll
-        for (int i = 0; i < NSTR; ++i)
-            eps[i] = 0.0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                const double uq = a.u[c * N + idx[q]];
-#pragma unroll
-                for (int i = 0; i < NSTR; ++i)
-                    eps[i] += Bs[i * 8 * C + q * C + c] * uq;
-            }
+            for (int i = 0; i < 3; ++i)
+                eps[i] = g[0][i];
+        } else {
+            const double sh = 7.071067811865476e-01; // sqrt(1/2), matmodel.h:288
+            eps[0] = g[0][0];
+            eps[1] = g[C > 1 ? 1 : 0][1];
+            eps[2] = g[C > 2 ? 2 : 0][2];
+            eps[3] = sh * (g[0][1] + g[C > 1 ? 1 : 0][0]);
+            eps[4] = sh * (g[0][2] + g[C > 2 ? 2 : 0][0]);
+            eps[5] = sh * (g[C > 1 ? 1 : 0][2] + g[C > 2 ? 2 : 0][1]);
+        }
         double sig[NSTR];
 #pragma unroll
         for (int i = 0; i < NSTR; ++i)
@@ -541,6 +554,13 @@ __global__ void __launch_bounds__(kStencilThreads) k_residual_df(StencilArgs a)
             const int    ph = mss[((tx - a0 + 1) * EY + (ty - b0 + 1)) * EZ + (tz - c0 + 1)];
             const float *kh = Kh + (size_t)ph * NC * NC + (size_t)(p * C) * NC;
             const float *kl = Kl + (size_t)ph * NC * NC + (size_t)(p * C) * NC;
+            // element-local double-float accumulators: independent chains per element
+            float Eh[C], El[C];
+#pragma unroll
+            for (int cr = 0; cr < C; ++cr) {
+                Eh[cr] = 0.f;
+                El[cr] = 0.f;
+            }
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int qa = q & 1, qb = (q >> 1) & 1, qc = (q >> 2) & 1;
@@ -557,11 +577,18 @@ __global__ void __launch_bounds__(kStencilThreads) k_residual_df(StencilArgs a)
                         const float pe = fmaf(k1, dh, -pr);
                         const float lo = fmaf(k1, dl, fmaf(k2, dh, pe));
                         float       t, e;
-                        two_sum(Sh[cr], pr, t, e);
-                        Sh[cr] = t;
-                        Sl[cr] += e + lo;
+                        two_sum(Eh[cr], pr, t, e);
+                        Eh[cr] = t;
+                        El[cr] += e + lo;
                     }
                 }
+            }
+#pragma unroll
+            for (int cr = 0; cr < C; ++cr) {
+                float t, e;
+                two_sum(Sh[cr], Eh[cr], t, e);
+                Sh[cr] = t;
+                Sl[cr] += e + El[cr];
             }
             if (fg)
 #pragma unroll

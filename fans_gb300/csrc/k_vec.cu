@@ -1,6 +1,8 @@
 // k_vec.cu -- streaming CG vector kernels with fused FP64 reductions.
 #include "kernels.cuh"
 
+#include <type_traits>
+
 namespace fansgpu {
 
 namespace {
@@ -59,6 +61,106 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(UpdateArgs a)
             a.scal->deltamid = v[1];
             if (!isfinite(a.scal->err))
                 a.scal->converged = -1;
+        }
+    }
+}
+
+// FP32 inner-loop update with 16-byte accesses (n is a multiple of 8: even grid
+// dimensions); same arithmetic and FP64 partials as k_cg_update<float, float>.
+__global__ void __launch_bounds__(kVecThreads) k_cg_update_f4(UpdateArgs a)
+{
+    __shared__ double red_smem[32 * 2];
+    const float   alpha = (float)a.scal->alpha;
+    float4       *r  = reinterpret_cast<float4 *>(a.r);
+    const float4 *Kd = reinterpret_cast<const float4 *>(a.Kd);
+    float4       *u  = reinterpret_cast<float4 *>(a.u);
+    const float4 *d  = reinterpret_cast<const float4 *>(a.d);
+    const float4 *s  = reinterpret_cast<const float4 *>(a.s);
+    const int     measure = a.measure;
+    const bool    mx = measure == 2;
+    const long long nv = a.n / 4;
+    double        nrm = 0.0, rs = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
+        float4       rv = r[i];
+        const float4 k = Kd[i], sv = s[i];
+        rv.x -= alpha * k.x;
+        rv.y -= alpha * k.y;
+        rv.z -= alpha * k.z;
+        rv.w -= alpha * k.w;
+        r[i] = rv;
+        if (a.do_u) {
+            float4       uv = u[i];
+            const float4 dv = d[i];
+            uv.x -= alpha * dv.x;
+            uv.y -= alpha * dv.y;
+            uv.z -= alpha * dv.z;
+            uv.w -= alpha * dv.w;
+            u[i] = uv;
+        }
+        float cn;
+        if (measure == 1)
+            cn = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+        else if (mx)
+            cn = fmaxf(fmaxf(fabsf(rv.x), fabsf(rv.y)), fmaxf(fabsf(rv.z), fabsf(rv.w)));
+        else
+            cn = fabsf(rv.x) + fabsf(rv.y) + fabsf(rv.z) + fabsf(rv.w);
+        nrm = mx ? fmax(nrm, (double)cn) : nrm + (double)cn;
+        rs += (double)(rv.x * sv.x + rv.y * sv.y + rv.z * sv.z + rv.w * sv.w);
+    }
+    double v[2]   = {nrm, rs};
+    int    ops[2] = {mx ? RED_MAX : RED_SUM, RED_SUM};
+    block_reduce<2>(v, ops, red_smem);
+    if (grid_partial_commit<2>(v, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+        grid_final<2>(v, ops, a.red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0) {
+            a.scal->err      = a.measure == 1 ? sqrt(v[0]) : v[0];
+            a.scal->deltamid = v[1];
+            if (!isfinite(a.scal->err))
+                a.scal->converged = -1;
+        }
+    }
+}
+
+// ||r|| of an FP64 field with the re-seed copy to FP32; `fast`: squares and
+// short partial sums in FP32 (relative accuracy ~1e-7 of the norm, enough for
+// the mixed path's refresh test), FP64 otherwise.
+template <typename T, typename TO>
+__global__ void __launch_bounds__(kVecThreads) k_norm_fast(const T *__restrict__ r, long long n, int measure,
+                                                           CgScalars *scal, int set_err0, TO *r_out, GridRed red,
+                                                           int site)
+{
+    __shared__ double red_smem[32];
+    const bool mx = measure == 2;
+    double     nrm = 0.0;
+    const long long nv = n / 2;
+    const double2 *r2 = reinterpret_cast<const double2 *>(r);
+    float2        *o2 = reinterpret_cast<float2 *>(r_out);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
+        const double2 v = r2[i];
+        const float2  f = make_float2((float)v.x, (float)v.y);
+        if (o2)
+            o2[i] = f;
+        float cn;
+        if (measure == 1)
+            cn = f.x * f.x + f.y * f.y;
+        else if (mx)
+            cn = fmaxf(fabsf(f.x), fabsf(f.y));
+        else
+            cn = fabsf(f.x) + fabsf(f.y);
+        nrm = mx ? fmax(nrm, (double)cn) : nrm + (double)cn;
+    }
+    double v[1]   = {nrm};
+    int    ops[1] = {mx ? RED_MAX : RED_SUM};
+    block_reduce<1>(v, ops, red_smem);
+    if (grid_partial_commit<1>(v, red.partials, red.counter + site, gridDim.x)) {
+        grid_final<1>(v, ops, red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0) {
+            double e  = measure == 1 ? sqrt(v[0]) : v[0];
+            scal->err = e;
+            if (set_err0)
+                scal->err0 = e;
+            if (!isfinite(e))
+                scal->converged = -1;
         }
     }
 }
@@ -143,7 +245,18 @@ cudaError_t launch_ms_convert(const uint16_t *in, uint8_t *out, long long n, uns
 template <typename T, typename TU>
 cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st)
 {
-    k_cg_update<T, TU><<<grid_blocks_for(a.n), kVecThreads, 0, st>>>(a);
+    if (std::is_same<T, float>::value && std::is_same<TU, float>::value && a.n % 4 == 0)
+        k_cg_update_f4<<<grid_blocks_for(a.n / 4), kVecThreads, 0, st>>>(a);
+    else
+        k_cg_update<T, TU><<<grid_blocks_for(a.n), kVecThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_fast(const double *r, long long n, int measure, CgScalars *scal, int set_err0, float *r_out,
+                             GridRed red, int site, cudaStream_t st)
+{
+    k_norm_fast<double, float><<<grid_blocks_for(n / 2), kVecThreads, 0, st>>>(r, n, measure, scal, set_err0, r_out,
+                                                                              red, site);
     return cudaGetLastError();
 }
 template cudaError_t launch_cg_update<double, double>(const UpdateArgs &, cudaStream_t);

@@ -50,7 +50,8 @@ cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st);
 cudaError_t launch_residual_df(const StencilArgs &a, cudaStream_t st);
 
 // Element-averaged strain/stress of linear laws (matmodel.h:203-225,
-// solver.h:708-737): eps_e = Bbar u_e + g0, sig_e = C_ph eps_e.  Sums over the
+// solver.h:708-737): eps_e = Bbar u_e + g0 with Bbar (the Gauss-point mean of
+// B) = B at the element centre, sig_e = C_ph eps_e.  Sums over the
 // elements whose phase matches `phase_filter` (-1: all) land in out_red:
 // [0,nstr) sum eps, [nstr,2nstr) sum sig, [2nstr] count.  Optional AoS fields.
 struct StrainStressArgs {
@@ -58,7 +59,7 @@ struct StrainStressArgs {
     int            C, nstr;
     const double  *u;      // SoA FP64
     const uint8_t *ms;
-    const double  *Bbar;   // nstr x 8C (GP-averaged B)
+    double         inv4l[3]; // 1 / (4 l_e) per direction (centre gradient = mean edge difference / l_e)
     const double  *Cph;    // nph x nstr x nstr
     const double  *g0;     // nstr
     int            nph;
@@ -148,6 +149,11 @@ cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st);
 template <typename T, typename TO>
 cudaError_t launch_norm(const T *r, long long n, int measure, CgScalars *scal, int set_err0, TO *r_out, GridRed red,
                         int red_site, cudaStream_t st);
+
+// Mixed path: ||r|| of the FP64 true residual with FP32 squares / short partial
+// sums (FP64 accumulation across them) and the FP32 re-seed copy.
+cudaError_t launch_norm_fast(const double *r, long long n, int measure, CgScalars *scal, int set_err0, float *r_out,
+                             GridRed red, int site, cudaStream_t st);
 
 // u -= s (fixed-point update, solverFP.h:38).
 template <typename T>
