@@ -39,7 +39,7 @@ HBM_FALLBACK_GBS = 6800.0
 # FP64 CG iterations of the six load cases of the 256^3 workload (GPU FP64 path,
 # which matches the oracle's iteration counts within +-1 in the parity tests);
 # used to scale the oracle's per-iteration time in the reference arm.
-FP64_ITERS_256 = None
+FP64_ITERS_256 = [44, 44, 44, 45, 45, 45]  # FP64 GPU CG iterations of the six 256^3 load cases (measured)
 
 
 def parse():

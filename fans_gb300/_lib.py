@@ -20,6 +20,8 @@ CG, FP = 0, 1
 L1, L2, LINF = 0, 1, 2
 ABSOLUTE, RELATIVE = 0, 1
 FIELD_U, FIELD_R, FIELD_STRAIN, FIELD_STRESS, FIELD_U_PREV = 0, 1, 2, 3, 4
+FIELD_PLASTIC_STRAIN, FIELD_HARDENING = 5, 6
+FIELD_STRAIN_GP, FIELD_STRESS_GP, FIELD_PLASTIC_STRAIN_GP, FIELD_HARDENING_GP = 7, 8, 9, 10
 
 FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
 MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}

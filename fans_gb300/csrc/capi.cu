@@ -48,6 +48,7 @@ struct fansgpu_ctx {
     std::vector<float>  K32h;
     bool                u_zero = true; // v_u known to be zero (fresh context / reset): R(u) = F
     double *K64 = nullptr, *f64 = nullptr, *Cph = nullptr, *Bbar_d = nullptr, *g0_d = nullptr, *K0c = nullptr;
+    double *Bgp_d = nullptr; // Gauss-point B matrices, ngp x n_str x 8C
     float  *K32 = nullptr;
     double *G64 = nullptr;
     float  *G32 = nullptr;
@@ -77,6 +78,13 @@ struct fansgpu_ctx {
     double                   ktime[FANSGPU_K_COUNT] = {0};
     int64_t                  kcount[FANSGPU_K_COUNT] = {0};
     unsigned int            *max_id = nullptr;
+
+    // nonlinear laws (J2PlasticityNew): internal variables SoA eps_p [6][ngp][N], q [ngp][N],
+    // committed (_t) and trial copies; element-row scratch [8C][N] for the residual gather
+    double *ep_t = nullptr, *q_t = nullptr, *ep = nullptr, *q = nullptr, *rows = nullptr;
+    int    *law_d = nullptr;
+    double *prm_d = nullptr;
+    double  alpha_warm = 0.1;
 };
 
 namespace fansgpu {
@@ -99,7 +107,7 @@ namespace {
 
 constexpr int kMaxBlocks = 152 * 16;
 constexpr int kRedSites  = 16;
-enum { SITE_NORM = 0, SITE_CONV = 1, SITE_STENCIL = 2, SITE_UPDATE = 3, SITE_SS = 4 };
+enum { SITE_NORM = 0, SITE_CONV = 1, SITE_STENCIL = 2, SITE_UPDATE = 3, SITE_SS = 4, SITE_DOT = 5, SITE_EL = 6 };
 
 template <typename P>
 int dalloc(fansgpu_ctx *ctx, P **p, size_t count)
@@ -239,6 +247,50 @@ cudaError_t run_conv(fansgpu_ctx *ctx, const ConvPlan<T> &p, ConvArgs ca)
     return e;
 }
 
+// Internal variables (zero: the virgin state of initializeInternalVariables,
+// J2PlasticityNew.h:29-35) and the element-row scratch.
+int alloc_nonlinear(fansgpu_ctx *ctx)
+{
+    const long long N = ctx->N, nep = 6LL * ctx->ngp * N, nq = (long long)ctx->ngp * N;
+    int             rc;
+    if (!ctx->ep_t) {
+        if ((rc = dalloc(ctx, &ctx->ep_t, nep)) || (rc = dalloc(ctx, &ctx->ep, nep)) ||
+            (rc = dalloc(ctx, &ctx->q_t, nq)) || (rc = dalloc(ctx, &ctx->q, nq)) ||
+            (rc = dalloc(ctx, &ctx->rows, 8LL * ctx->C * N)))
+            return rc;
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep_t, 0, sizeof(double) * nep, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep, 0, sizeof(double) * nep, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q_t, 0, sizeof(double) * nq, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q, 0, sizeof(double) * nq, ctx->st));
+    }
+    return 0;
+}
+
+// Per-phase law ids and J2 parameters for the element kernel.
+int upload_law_tables(fansgpu_ctx *ctx)
+{
+    int rc;
+    if (ctx->law_d)
+        cudaFree(ctx->law_d);
+    if (ctx->prm_d)
+        cudaFree(ctx->prm_d);
+    ctx->law_d = nullptr;
+    ctx->prm_d = nullptr;
+    if ((rc = dalloc(ctx, &ctx->law_d, ctx->nph)) || (rc = dalloc(ctx, &ctx->prm_d, 4 * ctx->nph)))
+        return rc;
+    std::vector<int>    lw(ctx->nph);
+    std::vector<double> pr(4 * ctx->nph, 0.0);
+    for (int ph = 0; ph < ctx->nph; ++ph) {
+        lw[ph] = ctx->law[ph];
+        for (int i = 0; i < (int)std::min<size_t>(4, ctx->prm[ph].size()); ++i)
+            pr[4 * ph + i] = ctx->prm[ph][i];
+    }
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->law_d, lw.data(), sizeof(int) * lw.size(), cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->prm_d, pr.data(), sizeof(double) * pr.size(), cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
 // Per-phase tables, reference stiffness and Green's operator (lazy).
 int setup(fansgpu_ctx *ctx)
 {
@@ -285,9 +337,11 @@ int setup(fansgpu_ctx *ctx)
                 K32[ph * NC * NC + i] = (float)Ke[i];
             }
         }
-        if (!ctx->all_linear)
-            return fail(ctx, FANSGPU_EUNSUPPORTED,
-                        "J2PlasticityNew (nonlinear CG with secant line search) is not in this build yet");
+        {
+            int rc3;
+            if ((rc3 = upload_law_tables(ctx)) || (!ctx->all_linear && (rc3 = alloc_nonlinear(ctx))))
+                return rc3;
+        }
         ctx->K64h = K64;
         ctx->K32h = K32;
         {
@@ -412,6 +466,47 @@ int run_residual_df(fansgpu_ctx *ctx)
     a.nph      = ctx->nph;
     int e0     = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_residual_df(a, ctx->st));
+    tk_span(ctx, FANSGPU_K_RESIDUAL, e0, tk_mark(ctx));
+    return 0;
+}
+
+ElementArgs element_args(fansgpu_ctx *ctx, const double *u, int mode)
+{
+    ElementArgs a{};
+    a.g     = ctx->g;
+    a.C     = ctx->C;
+    a.nstr  = ctx->nstr;
+    a.ngp   = ctx->ngp;
+    a.mode  = mode;
+    a.u     = u;
+    a.ms    = ctx->d_ms;
+    a.B     = ctx->Bgp_d;
+    a.g0    = ctx->g0_d;
+    a.law   = ctx->law_d;
+    a.Cph   = ctx->Cph;
+    a.prm   = ctx->prm_d;
+    a.ep_t  = ctx->ep_t;
+    a.q_t   = ctx->q_t;
+    a.ep    = ctx->ep;
+    a.q     = ctx->q;
+    a.ve    = ctx->ve;
+    a.rows  = ctx->rows;
+    a.red   = ctx->red;
+    a.red_site     = SITE_EL;
+    a.phase_filter = -1;
+    return a;
+}
+
+// r = R(u) in FP64 (compute_residual, solver.h:231-270).  Linear laws: the
+// fused stencil with the g0 force; nonlinear laws: the element kernel (which
+// writes the trial internal variables, as get_sigma does) and the node gather.
+int run_residual64(fansgpu_ctx *ctx, const double *u, double *r)
+{
+    if (ctx->all_linear)
+        return run_stencil<double>(ctx, u, r, true);
+    int e0 = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_element(element_args(ctx, u, ELEM_RESIDUAL), ctx->st));
+    FANS_CUDA_CHECK(launch_gather(ctx->rows, r, ctx->g, ctx->C, ctx->st));
     tk_span(ctx, FANSGPU_K_RESIDUAL, e0, tk_mark(ctx));
     return 0;
 }
@@ -595,7 +690,7 @@ int solve_fp64(fansgpu_ctx *ctx)
     int             rc;
     if ((rc = init_scalars(ctx)))
         return rc;
-    if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+    if ((rc = run_residual64(ctx, ctx->u, ctx->r)))
         return rc;
     { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
@@ -612,7 +707,7 @@ int solve_fp64(fansgpu_ctx *ctx)
         ConvArgs ca{ctx->r, ctx->s, 1.0, 0, ctx->scal, ctx->red, SITE_CONV};
         FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
         FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, ctx->s, -1.0, n, ctx->st));
-        if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+        if ((rc = run_residual64(ctx, ctx->u, ctx->r)))
             return rc;
         { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, nullptr, ctx->red,
@@ -629,8 +724,131 @@ int solve_fp64(fansgpu_ctx *ctx)
     return 0;
 }
 
-int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *stress_f, double *out)
+// <a, b> on the device into *slot (a CgScalars member); read on the next sync.
+int dot_to(fansgpu_ctx *ctx, const double *a, const double *b, double *slot)
 {
+    FANS_CUDA_CHECK(launch_dot(a, b, ctx->n, slot, ctx->red, SITE_DOT, ctx->st));
+    return 0;
+}
+
+int host_dot(fansgpu_ctx *ctx, const double *a, const double *b, double *out)
+{
+    int rc;
+    if ((rc = dot_to(ctx, a, b, &ctx->scal->aux[0])) || (rc = sync_scalars(ctx)))
+        return rc;
+    *out = ctx->scal_h->aux[0];
+    return 0;
+}
+
+// SolverCG::internalSolve with nonlinear laws (solverCG.h:62-117): the flexible
+// CG direction, then LineSearchSecant (solverCG.h:120-160) on u along d, with
+// r replaced by the last line-search residual.  FP64 throughout; the scalar
+// secant logic runs on the host between device dot products.
+int solve_cg_nl(fansgpu_ctx *ctx)
+{
+    const long long n = ctx->n;
+    double         *d = ctx->dd[0], *rnew = ctx->Kd;
+    int             rc;
+    ctx->alpha_warm = 0.1; // solverCG.h:68
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s, 0, sizeof(double) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(d, 0, sizeof(double) * n, ctx->st));
+    if ((rc = init_scalars(ctx)))
+        return rc;
+    if ((rc = run_residual64(ctx, ctx->u, ctx->r)))
+        return rc;
+    { int en = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
+                                               SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
+    if ((rc = sync_scalars(ctx)))
+        return rc;
+    ctx->iter = 0;
+    ctx->err_all.assign(1, ctx->scal_h->err);
+    double err_rel = err_value(ctx, ctx->scal_h->err);
+    if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
+        ctx->u_zero = false;
+    while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
+        // deltamid = <r, s>; s = -G*r; delta = <r, s>; beta (solverCG.h:85-94)
+        if ((rc = dot_to(ctx, ctx->r, ctx->s, &ctx->scal->deltamid)))
+            return rc;
+        ConvArgs ca{ctx->r, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+        FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
+        FANS_CUDA_CHECK(launch_direction(d, ctx->s, n, ctx->scal, ctx->st));
+        // LineSearchSecant
+        const int    max_it = ctx->tol.ls_max_iter;
+        const double ls_tol = ctx->tol.ls_tol;
+        double       err = 10.0, alpha_prev = 0.0, alpha_curr = ctx->alpha_warm, rpd, r1pd;
+        int          it  = 0;
+        if ((rc = host_dot(ctx, ctx->r, d, &rpd)))
+            return rc;
+        FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, d, alpha_curr, n, ctx->st));
+        if ((rc = run_residual64(ctx, ctx->u, rnew)) || (rc = host_dot(ctx, rnew, d, &r1pd)))
+            return rc;
+        while (it < max_it && err > ls_tol) {
+            const double denom = r1pd - rpd;
+            if (std::fabs(denom) < 1e-14 * (std::fabs(r1pd) + std::fabs(rpd)))
+                break;
+            double alpha_next = alpha_curr - r1pd * (alpha_curr - alpha_prev) / denom;
+            if (alpha_next <= 0.0)
+                alpha_next = 0.5 * (alpha_prev + alpha_curr);
+            err = std::fabs(alpha_next - alpha_curr);
+            FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, d, alpha_next - alpha_curr, n, ctx->st));
+            alpha_prev = alpha_curr;
+            rpd        = r1pd;
+            alpha_curr = alpha_next;
+            ++it;
+            if ((rc = run_residual64(ctx, ctx->u, rnew)) || (rc = host_dot(ctx, rnew, d, &r1pd)))
+                return rc;
+        }
+        ctx->alpha_warm = (it == max_it && err > ls_tol) ? 0.1 : alpha_curr;
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->r, rnew, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+        { int en = tk_mark(ctx);
+        FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, nullptr, ctx->red,
+                                                   SITE_NORM, ctx->st));
+        tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
+        if ((rc = sync_scalars(ctx)))
+            return rc;
+        ctx->iter++;
+        ctx->err_all.push_back(ctx->scal_h->err);
+        if (ctx->scal_h->converged < 0 || !std::isfinite(alpha_curr))
+            return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at iteration %d", ctx->iter);
+        err_rel = err_value(ctx, ctx->scal_h->err);
+    }
+    return 0;
+}
+
+// MaterialManager::update_internal_variables (MaterialManager.h:207-213).
+int commit_ivars(fansgpu_ctx *ctx)
+{
+    if (ctx->all_linear || !ctx->ep_t)
+        return 0;
+    const long long nep = 6LL * ctx->ngp * ctx->N, nq = (long long)ctx->ngp * ctx->N;
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->ep_t, ctx->ep, sizeof(double) * nep, cudaMemcpyDeviceToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->q_t, ctx->q, sizeof(double) * nq, cudaMemcpyDeviceToDevice, ctx->st));
+    return 0;
+}
+
+int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *stress_f, double *out,
+                  double *strain_gp = nullptr, double *stress_gp = nullptr)
+{
+    if (!ctx->all_linear || strain_gp || stress_gp) {
+        // per-Gauss-point law evaluation (Matmodel::getStrainStress, matmodel.h:203-225)
+        ElementArgs a  = element_args(ctx, ctx->u, ELEM_AVERAGES);
+        a.phase_filter = phase_filter;
+        a.strain       = strain_f;
+        a.stress       = stress_f;
+        a.strain_gp    = strain_gp;
+        a.stress_gp    = stress_gp;
+        a.out_red      = ctx->red_out;
+        int e0         = tk_mark(ctx);
+        FANS_CUDA_CHECK(launch_element(a, ctx->st));
+        tk_span(ctx, FANSGPU_K_STRAIN_STRESS, e0, tk_mark(ctx));
+        FANS_CUDA_CHECK(cudaMemcpyAsync(out, ctx->red_out, sizeof(double) * (2 * ctx->nstr + 1),
+                                        cudaMemcpyDeviceToHost, ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        tk_flush(ctx);
+        return 0;
+    }
     StrainStressArgs a{};
     a.g            = ctx->g;
     a.C            = ctx->C;
@@ -736,6 +954,7 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         (rc = dalloc(ctx, &ctx->scal, 1)) || (rc = dalloc(ctx, &ctx->red.partials, (size_t)max_reduction_blocks(ctx->g, ctx->C) * kMaxRed)) ||
         (rc = dalloc(ctx, &ctx->red.counter, kRedSites)) || (rc = dalloc(ctx, &ctx->red_out, 64)) ||
         (rc = dalloc(ctx, &ctx->K0c, NC * NC)) || (rc = dalloc(ctx, &ctx->Bbar_d, ns * NC)) ||
+        (rc = dalloc(ctx, &ctx->Bgp_d, (size_t)ctx->ngp * ns * NC)) ||
         (rc = dalloc(ctx, &ctx->g0_d, ns)) || (rc = dalloc(ctx, &ctx->max_id, 1)) ||
         (rc = dalloc(ctx, &ctx->trig, 2 * (ctx->g.nx + ctx->g.ny + nzh))))
         return bail(rc);
@@ -755,6 +974,7 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * nn, ctx->st);
     cudaMemsetAsync(ctx->r, 0, sizeof(double) * nn, ctx->st);
     cudaMemcpyAsync(ctx->Bbar_d, ctx->Bbar.data(), sizeof(double) * ns * NC, cudaMemcpyHostToDevice, ctx->st);
+    cudaMemcpyAsync(ctx->Bgp_d, ctx->B.data(), sizeof(double) * ctx->B.size(), cudaMemcpyHostToDevice, ctx->st);
     // trig tables for the Green's operator (solver.h:156-158)
     {
         std::vector<double> t;
@@ -805,7 +1025,8 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
-                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id};
+                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d,
+                    ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -852,6 +1073,13 @@ int fansgpu_reset(fansgpu_ctx *ctx)
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->u, 0, sizeof(double) * ctx->n, ctx->st));
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * ctx->n, ctx->st));
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->r, 0, sizeof(double) * ctx->n, ctx->st));
+    if (ctx->ep_t) {
+        const long long nep = 6LL * ctx->ngp * ctx->N, nq = (long long)ctx->ngp * ctx->N;
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep_t, 0, sizeof(double) * nep, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep, 0, sizeof(double) * nep, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q_t, 0, sizeof(double) * nq, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q, 0, sizeof(double) * nq, ctx->st));
+    }
     ctx->err_all.clear();
     ctx->iter   = 0;
     ctx->u_zero = true;
@@ -1006,11 +1234,16 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
     int refinements = 0;
     if (ctx->desc.method == FANSGPU_FP)
         rc = solve_fp64(ctx);
+    else if (!ctx->all_linear)
+        rc = solve_cg_nl(ctx); // nonlinear laws run the FP64 path at either precision setting
     else if (ctx->desc.precision == FANSGPU_MIXED)
         rc = solve_cg_mixed(ctx, &refinements);
     else
         rc = solve_cg64(ctx);
     if (rc)
+        return rc;
+    // internal variables are committed at the end of every solve (solver.h:299)
+    if ((rc = commit_ivars(ctx)))
         return rc;
     ctx->u_zero = ctx->u_zero && ctx->iter == 0;
     FANS_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->st));
@@ -1028,7 +1261,6 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
         stats->refinements = refinements;
         stats->solve_ms    = ms;
     }
-    // internal variables are committed here (solver.h:299); linear laws have none
     return conv ? 0 : FANSGPU_ENOTCONV;
 }
 
@@ -1094,15 +1326,21 @@ int fansgpu_homogenized_tangent(fansgpu_ctx *ctx, double pert, double *out)
     int rc = setup(ctx);
     if (rc)
         return rc;
-    const int ns = ctx->nstr;
+    const int  ns     = ctx->nstr;
+    const bool linear = ctx->all_linear;
+    if (!linear && !(pert != 0.0 && std::isfinite(pert)))
+        return fail(ctx, FANSGPU_EINVAL, "nonlinear tangent needs a finite, non-zero perturbation");
+    std::vector<double> g_save = ctx->g0, T(ns * ns), sig(ns), sig0(ns);
+    if (!linear && (rc = fansgpu_homogenized_stress(ctx, sig0.data()))) // unperturbed stress (solver.h:743)
+        return rc;
     // solver.h:749-750: relative error type and TOL >= 1e-6 for the rest of the run
     ctx->tol.type      = FANSGPU_RELATIVE;
     ctx->tol.tolerance = std::max(1e-6, ctx->tol.tolerance);
-    std::vector<double> g_save = ctx->g0, T(ns * ns), sig(ns);
     for (int i = 0; i < ns; ++i) {
-        std::vector<double> g(ns, 0.0);
-        g[i] = 1.0; // linear laws: unit gradients (solver.h:760-762)
-        (void)pert;
+        // linear: unit gradients; nonlinear: g0 + pert e_i (solver.h:758-765).  Each solve
+        // commits internal variables, as the reference's does.
+        std::vector<double> g = linear ? std::vector<double>(ns, 0.0) : g_save;
+        g[i] += linear ? 1.0 : pert;
         if ((rc = fansgpu_set_gradient(ctx, g.data())))
             return rc;
         rc = fansgpu_solve(ctx, nullptr);
@@ -1111,7 +1349,7 @@ int fansgpu_homogenized_tangent(fansgpu_ctx *ctx, double pert, double *out)
         if ((rc = fansgpu_homogenized_stress(ctx, sig.data())))
             return rc;
         for (int k = 0; k < ns; ++k)
-            T[k * ns + i] = sig[k];
+            T[k * ns + i] = linear ? sig[k] : (sig[k] - sig0[k]) / pert;
     }
     for (int i = 0; i < ns; ++i)
         for (int j = 0; j < ns; ++j)
@@ -1142,6 +1380,52 @@ int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host)
         FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N * ctx->nstr, cudaMemcpyDeviceToHost, ctx->st));
         FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
         return 0;
+    }
+    if (which == FANSGPU_FIELD_PLASTIC_STRAIN || which == FANSGPU_FIELD_HARDENING) {
+        int rc = setup(ctx);
+        if (rc)
+            return rc;
+        if (ctx->all_linear || !ctx->ep_t)
+            return fail(ctx, FANSGPU_EINVAL, "field %d: no material with internal variables", which);
+        // J2PlasticityNew::postprocess (J2PlasticityNew.h:171-177): Gauss-point means of the committed state
+        const bool ps = which == FANSGPU_FIELD_PLASTIC_STRAIN;
+        FANS_CUDA_CHECK(launch_ivar_mean(ctx->ep_t, ctx->q_t, ctx->ngp, N, ps ? ctx->staging : nullptr,
+                                         ps ? nullptr : ctx->staging, ctx->st));
+        FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N * (ps ? 6 : 1), cudaMemcpyDeviceToHost,
+                                        ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        return 0;
+    }
+    if (which >= FANSGPU_FIELD_STRAIN_GP && which <= FANSGPU_FIELD_HARDENING_GP) {
+        int rc = setup(ctx);
+        if (rc)
+            return rc;
+        const bool ivar = which >= FANSGPU_FIELD_PLASTIC_STRAIN_GP;
+        if (ivar && (ctx->all_linear || !ctx->ep_t))
+            return fail(ctx, FANSGPU_EINVAL, "field %d: no material with internal variables", which);
+        const long long per = which == FANSGPU_FIELD_HARDENING_GP ? 1 : which == FANSGPU_FIELD_PLASTIC_STRAIN_GP ? 6 : ctx->nstr;
+        const long long cnt = N * ctx->ngp * per;
+        double         *tmp = nullptr; // postprocess only: a temporary of n_gp x the staging size
+        if ((rc = dalloc(ctx, &tmp, cnt)))
+            return rc;
+        double red[16];
+        if (!ivar) {
+            rc = strain_stress(ctx, -1, nullptr, nullptr, red, which == FANSGPU_FIELD_STRAIN_GP ? tmp : nullptr,
+                               which == FANSGPU_FIELD_STRESS_GP ? tmp : nullptr);
+        } else {
+            const cudaError_t e = launch_ivar_gp(ctx->ep_t, ctx->q_t, ctx->ngp, N,
+                                                 which == FANSGPU_FIELD_PLASTIC_STRAIN_GP ? tmp : nullptr,
+                                                 which == FANSGPU_FIELD_HARDENING_GP ? tmp : nullptr, ctx->st);
+            rc = e == cudaSuccess ? 0 : fail(ctx, FANSGPU_ECUDA, "ivar gather: %s", cudaGetErrorString(e));
+        }
+        if (!rc) {
+            const cudaError_t e1 = cudaMemcpyAsync(host, tmp, sizeof(double) * cnt, cudaMemcpyDeviceToHost, ctx->st);
+            const cudaError_t e2 = cudaStreamSynchronize(ctx->st);
+            if (e1 != cudaSuccess || e2 != cudaSuccess)
+                rc = fail(ctx, FANSGPU_ECUDA, "field copy: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        }
+        cudaFree(tmp);
+        return rc;
     }
     return fail(ctx, FANSGPU_EINVAL, "unknown field %d", which);
 }
@@ -1186,7 +1470,13 @@ int fansgpu_extrapolate_displacement(fansgpu_ctx *ctx)
 
 int fansgpu_commit_state(fansgpu_ctx *ctx)
 {
-    return ctx ? 0 : FANSGPU_EINVAL;
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    int rc = commit_ivars(ctx);
+    if (rc)
+        return rc;
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
 }
 
 int fansgpu_residual(fansgpu_ctx *ctx, const double *u, double *r)
@@ -1199,7 +1489,7 @@ int fansgpu_residual(fansgpu_ctx *ctx, const double *u, double *r)
     const long long N = ctx->N;
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, u, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
     FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, ctx->Kd, N, ctx->C, ctx->st)));
-    if ((rc = run_stencil<double>(ctx, ctx->Kd, ctx->s, true)))
+    if ((rc = run_residual64(ctx, ctx->Kd, ctx->s)))
         return rc;
     FANS_CUDA_CHECK((launch_soa_to_aos<double, double>(ctx->s, ctx->staging, N, ctx->C, ctx->st)));
     FANS_CUDA_CHECK(cudaMemcpyAsync(r, ctx->staging, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));

@@ -1,0 +1,400 @@
+// k_element.cu -- element-centric kernels for constitutive laws with internal
+// variables (J2PlasticityNew) and the general residual R(u) of any law.
+//
+// k_element: one thread per (element, Gauss point).  u_e relative to the
+// element's node 0 (solver.h:252), eps_gp = B_gp u_e + g0 (matmodel.h:194),
+// sigma_gp from the phase's law (linear C, or the J2 radial return of
+// J2PlasticityNew.h:43-108 writing trial internal variables), then either
+//   mode RESIDUAL: r_e = sum_gp B_gp^T sigma_gp v_e/n_gp (matmodel.h:199) into a
+//                  row-plane scratch [8C][N] for the node gather, or
+//   mode AVERAGES: element means of eps and sigma (matmodel.h:203-225) summed
+//                  into FP64 block partials (phase-filtered), optional fields.
+// k_gather: r_node = sum over the 8 elements around the node of their rows for
+// that node -- the scatter of solver.h:257-261 as a deterministic gather.
+// Internal variables are SoA: eps_p[6][n_gp][N], q[n_gp][N] (trial and
+// committed copies), in FP64.
+#include "../../include/fans_gb300.h"
+#include "kernels.cuh"
+
+namespace fansgpu {
+
+namespace {
+
+constexpr int kElThreads = 128;
+
+__device__ __forceinline__ void elem_nodes(int nx, int ny, int nz, long long e, long long idx[8])
+{
+    const int z = (int)(e % nz), y = (int)((e / nz) % ny), x = (int)(e / ((long long)nz * ny));
+    const int x1 = x + 1 == nx ? 0 : x + 1, y1 = y + 1 == ny ? 0 : y + 1, z1 = z + 1 == nz ? 0 : z + 1;
+    idx[0] = ((long long)x * ny + y) * nz + z;
+    idx[1] = ((long long)x1 * ny + y) * nz + z;
+    idx[2] = ((long long)x * ny + y1) * nz + z;
+    idx[3] = ((long long)x1 * ny + y1) * nz + z;
+    idx[4] = ((long long)x * ny + y) * nz + z1;
+    idx[5] = ((long long)x1 * ny + y) * nz + z1;
+    idx[6] = ((long long)x * ny + y1) * nz + z1;
+    idx[7] = ((long long)x1 * ny + y1) * nz + z1;
+}
+
+// J2PlasticityNew::get_sigma (J2PlasticityNew.h:43-108), one Gauss point.
+__device__ __forceinline__ void j2_sigma(const double *prm, const double (&e)[6], const double (&ep_in)[6], double q_in,
+                                         double (&sig)[6], double (&ep_out)[6], double &q_out)
+{
+    const double K = prm[0], G = prm[1], sy0 = prm[2], h = prm[3];
+    const double c23 = sqrt(2.0 / 3.0);
+    double       s[6], st[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        s[i] = 2.0 * G * (e[i] - ep_in[i]);
+    const double lam = K - 2.0 / 3.0 * G;
+    const double tr  = e[0] + e[1] + e[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        s[i] += lam * tr;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        st[i] = s[i];
+    const double mean = (s[0] + s[1] + s[2]) / 3.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        st[i] -= mean;
+    double n2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        n2 += st[i] * st[i];
+    const double s_t    = sqrt(n2);
+    const double sy     = sy0 + q_in * h;
+    const double phi    = s_t - c23 * sy;
+    double       dgamma = phi / (2.0 * G + 2.0 / 3.0 * h);
+    if (dgamma < 0.0)
+        dgamma = 0.0;
+    const bool on = s_t > 1e-12;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        ep_out[i] = on ? ep_in[i] + dgamma * st[i] / s_t : ep_in[i];
+        sig[i]    = on ? s[i] - dgamma * 2.0 * G * st[i] / s_t : s[i];
+    }
+    q_out = q_in + c23 * dgamma;
+}
+
+// One thread per (element, Gauss point): the NGP threads of an element are
+// adjacent lanes of one warp.  Each computes eps, sigma (and the J2 update) of
+// its Gauss point; the element row B^T sigma is summed over the group by a
+// butterfly reduce-scatter, after which lane gp holds NCOL/NGP of the sums.
+// The loop runs whole warps (the trip count is rounded up to 32) so that every
+// shuffle sees all lanes; lanes past the end compute on zeros and store nothing.
+template <int C, int NGP, int MODE>
+__global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
+{
+    constexpr int NSTR = C == 1 ? 3 : 6, NCOL = 8 * C;
+    static_assert(32 % NGP == 0 && NCOL % NGP == 0, "group layout");
+    __shared__ double Bs[NGP * NSTR * NCOL];
+    for (int i = threadIdx.x; i < NGP * NSTR * NCOL; i += blockDim.x)
+        Bs[i] = a.B[i];
+    __syncthreads();
+    const int       nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const long long N  = (long long)nx * ny * nz;
+    const long long T  = (N * NGP + 31) / 32 * 32;
+    const int       gp = (int)(threadIdx.x % NGP);
+    const double   *Bg = Bs + gp * NSTR * NCOL;
+    double          se[MODE == ELEM_AVERAGES ? NSTR : 1], ss[MODE == ELEM_AVERAGES ? NSTR : 1], cnt = 0.0;
+    if constexpr (MODE == ELEM_AVERAGES) {
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i)
+            se[i] = ss[i] = 0.0;
+    }
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T; t += (long long)gridDim.x * blockDim.x) {
+        const long long el    = t / NGP;
+        const bool      valid = el < N;
+        const int       ph    = valid ? a.ms[el] : 0;
+        double          e[6], sig[6];
+        {
+            double ue[NCOL];
+            if (valid) {
+                long long idx[8];
+                elem_nodes(nx, ny, nz, el, idx);
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const double u0 = MODE == ELEM_RESIDUAL ? a.u[c * N + idx[0]] : 0.0;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        ue[q * C + c] = a.u[c * N + idx[q]] - u0;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < NCOL; ++k)
+                    ue[k] = 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i) {
+                double acc = 0.0;
+#pragma unroll
+                for (int k = 0; k < NCOL; ++k)
+                    acc += Bg[i * NCOL + k] * ue[k];
+                e[i] = acc + a.g0[i];
+            }
+        }
+        if (valid && C == 3 && a.law[ph] == FANSGPU_LAW_J2_LINEAR) {
+            double          ep_in[6], ep_out[6], q_out;
+            const long long base = (long long)gp * N + el;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                ep_in[i] = a.ep_t[(long long)i * NGP * N + base];
+            j2_sigma(a.prm + ph * 4, e, ep_in, a.q_t[base], sig, ep_out, q_out);
+            if (a.ep) {
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+                    a.ep[(long long)i * NGP * N + base] = ep_out[i];
+                a.q[base] = q_out;
+            }
+        } else {
+            const double *Cm = a.Cph + ph * NSTR * NSTR;
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i) {
+                double acc = 0.0;
+#pragma unroll
+                for (int k = 0; k < NSTR; ++k)
+                    acc += Cm[i * NSTR + k] * e[k];
+                sig[i] = acc;
+            }
+        }
+        if constexpr (MODE == ELEM_RESIDUAL) {
+            double v[NCOL];
+#pragma unroll
+            for (int k = 0; k < NCOL; ++k) {
+                double acc = 0.0;
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i)
+                    acc += Bg[i * NCOL + k] * sig[i];
+                v[k] = acc;
+            }
+            // reduce-scatter over the NGP lanes of the element
+            int kb = 0;
+#pragma unroll
+            for (int m = NGP / 2, cntv = NCOL; m >= 1; m /= 2, cntv /= 2) {
+                const bool hi = (gp & m) != 0;
+#pragma unroll
+                for (int j = 0; j < cntv / 2; ++j) {
+                    const double keep = hi ? v[cntv / 2 + j] : v[j];
+                    const double send = hi ? v[j] : v[cntv / 2 + j];
+                    v[j]              = keep + __shfl_xor_sync(0xffffffffu, send, m);
+                }
+                if (hi)
+                    kb += cntv / 2;
+            }
+            if (valid) {
+                const double sc = a.ve / NGP;
+#pragma unroll
+                for (int j = 0; j < NCOL / NGP; ++j)
+                    a.rows[(long long)(kb + j) * N + el] = v[j] * sc;
+            }
+        } else {
+            if (valid && a.strain_gp)
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i)
+                    a.strain_gp[(el * NGP + gp) * NSTR + i] = e[i];
+            if (valid && a.stress_gp)
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i)
+                    a.stress_gp[(el * NGP + gp) * NSTR + i] = sig[i];
+#pragma unroll
+            for (int m = NGP / 2; m >= 1; m /= 2)
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i) {
+                    e[i] += __shfl_xor_sync(0xffffffffu, e[i], m);
+                    sig[i] += __shfl_xor_sync(0xffffffffu, sig[i], m);
+                }
+            if (valid && gp == 0) {
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i) {
+                    e[i] /= NGP;
+                    sig[i] /= NGP;
+                }
+                if (a.strain)
+#pragma unroll
+                    for (int i = 0; i < NSTR; ++i)
+                        a.strain[el * NSTR + i] = e[i];
+                if (a.stress)
+#pragma unroll
+                    for (int i = 0; i < NSTR; ++i)
+                        a.stress[el * NSTR + i] = sig[i];
+                if (a.phase_filter < 0 || a.phase_filter == ph) {
+#pragma unroll
+                    for (int i = 0; i < NSTR; ++i) {
+                        se[i] += e[i];
+                        ss[i] += sig[i];
+                    }
+                    cnt += 1.0;
+                }
+            }
+        }
+    }
+    if constexpr (MODE == ELEM_AVERAGES) {
+        __shared__ double red_smem[32 * (2 * NSTR + 1)];
+        double            v[2 * NSTR + 1];
+        int               ops[2 * NSTR + 1];
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i) {
+            v[i]        = se[i];
+            v[NSTR + i] = ss[i];
+        }
+        v[2 * NSTR] = cnt;
+#pragma unroll
+        for (int i = 0; i < 2 * NSTR + 1; ++i)
+            ops[i] = RED_SUM;
+        block_reduce<2 * NSTR + 1>(v, ops, red_smem);
+        if (grid_partial_commit<2 * NSTR + 1>(v, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+            grid_final<2 * NSTR + 1>(v, ops, a.red.partials, gridDim.x, red_smem);
+            if (threadIdx.x == 0)
+                for (int i = 0; i < 2 * NSTR + 1; ++i)
+                    a.out_red[i] = v[i];
+        }
+    }
+}
+
+// r[c][node] = sum_p rows[p*C + c][element whose local node p is this node]
+template <int C>
+__global__ void __launch_bounds__(256) k_gather(const double *__restrict__ rows, double *__restrict__ r, Grid3 g)
+{
+    const long long N = g.N();
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(n % g.nz), y = (int)((n / g.nz) % g.ny), x = (int)(n / ((long long)g.nz * g.ny));
+        double    acc[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            acc[c] = 0.0;
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            const int ex = (p & 1) ? (x == 0 ? g.nx - 1 : x - 1) : x;
+            const int ey = (p & 2) ? (y == 0 ? g.ny - 1 : y - 1) : y;
+            const int ez = (p & 4) ? (z == 0 ? g.nz - 1 : z - 1) : z;
+            const long long e = ((long long)ex * g.ny + ey) * g.nz + ez;
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                acc[c] += rows[(long long)(p * C + c) * N + e];
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            r[c * N + n] = acc[c];
+    }
+}
+
+// <a, b> in FP64 -> *out (deterministic grid reduction)
+__global__ void __launch_bounds__(256) k_dot(const double *__restrict__ a, const double *__restrict__ b, long long n,
+                                             double *out, GridRed red, int site)
+{
+    __shared__ double red_smem[32];
+    double            s = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s += a[i] * b[i];
+    double    v[1]   = {s};
+    const int ops[1] = {RED_SUM};
+    block_reduce<1>(v, ops, red_smem);
+    if (grid_partial_commit<1>(v, red.partials, red.counter + site, gridDim.x)) {
+        grid_final<1>(v, ops, red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0)
+            *out = v[0];
+    }
+}
+
+// d = s + beta*d (beta from scal), the direction update of solverCG.h:94
+__global__ void k_direction(double *__restrict__ d, const double *__restrict__ s, long long n, const CgScalars *scal)
+{
+    const double beta = scal->beta;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = s[i] + beta * d[i];
+}
+
+__global__ void k_ivar_mean(const double *__restrict__ ep_t, const double *__restrict__ q_t, int ngp, long long N,
+                            double *__restrict__ ep_out, double *__restrict__ q_out)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N; e += (long long)gridDim.x * blockDim.x) {
+        if (ep_out)
+            for (int i = 0; i < 6; ++i) {
+                double s = 0.0;
+                for (int gp = 0; gp < ngp; ++gp)
+                    s += ep_t[((long long)i * ngp + gp) * N + e];
+                ep_out[e * 6 + i] = s / ngp;
+            }
+        if (q_out) {
+            double s = 0.0;
+            for (int gp = 0; gp < ngp; ++gp)
+                s += q_t[(long long)gp * N + e];
+            q_out[e] = s / ngp;
+        }
+    }
+}
+
+// Gauss-point values of the committed variables in element-major order:
+// ep_out[(e*ngp + gp)*6 + i], q_out[e*ngp + gp] (J2PlasticityNew.h:179-188).
+__global__ void k_ivar_gp(const double *__restrict__ ep_t, const double *__restrict__ q_t, int ngp, long long N,
+                          double *__restrict__ ep_out, double *__restrict__ q_out)
+{
+    const long long total = N * ngp;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const long long e  = t / ngp;
+        const int       gp = (int)(t % ngp);
+        if (ep_out)
+            for (int i = 0; i < 6; ++i)
+                ep_out[t * 6 + i] = ep_t[((long long)i * ngp + gp) * N + e];
+        if (q_out)
+            q_out[t] = q_t[(long long)gp * N + e];
+    }
+}
+
+} // namespace
+
+cudaError_t launch_ivar_gp(const double *ep_t, const double *q_t, int ngp, long long N, double *ep_out, double *q_out,
+                           cudaStream_t st)
+{
+    k_ivar_gp<<<grid_blocks_for(N * ngp), 256, 0, st>>>(ep_t, q_t, ngp, N, ep_out, q_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ivar_mean(const double *ep_t, const double *q_t, int ngp, long long N, double *ep_out,
+                             double *q_out, cudaStream_t st)
+{
+    k_ivar_mean<<<grid_blocks_for(N), 256, 0, st>>>(ep_t, q_t, ngp, N, ep_out, q_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_element(const ElementArgs &a, cudaStream_t st)
+{
+    // one (element, Gauss point) per thread, at most 152*16 blocks (the reduction partials are sized for that)
+    const long long want = (a.g.N() * a.ngp + kElThreads - 1) / kElThreads;
+    const int       nb   = (int)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
+    const bool      res  = a.mode == ELEM_RESIDUAL;
+#define FANSGPU_EL(C_, G_)                                                                                   \
+    (res ? (k_element<C_, G_, ELEM_RESIDUAL><<<nb, kElThreads, 0, st>>>(a), 0)                                 \
+         : (k_element<C_, G_, ELEM_AVERAGES><<<nb, kElThreads, 0, st>>>(a), 0))
+    if (a.C == 1)
+        a.ngp == 8 ? FANSGPU_EL(1, 8) : FANSGPU_EL(1, 1);
+    else
+        a.ngp == 8 ? FANSGPU_EL(3, 8) : FANSGPU_EL(3, 1);
+#undef FANSGPU_EL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const double *rows, double *r, const Grid3 &g, int C, cudaStream_t st)
+{
+    if (C == 1)
+        k_gather<1><<<grid_blocks_for(g.N()), 256, 0, st>>>(rows, r, g);
+    else
+        k_gather<3><<<grid_blocks_for(g.N()), 256, 0, st>>>(rows, r, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dot(const double *a, const double *b, long long n, double *out, GridRed red, int site,
+                       cudaStream_t st)
+{
+    k_dot<<<grid_blocks_for(n), 256, 0, st>>>(a, b, n, out, red, site);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_direction(double *d, const double *s, long long n, const CgScalars *scal, cudaStream_t st)
+{
+    k_direction<<<grid_blocks_for(n), 256, 0, st>>>(d, s, n, scal);
+    return cudaGetLastError();
+}
+
+} // namespace fansgpu

@@ -10,7 +10,7 @@ namespace fansgpu {
 
 struct Grid3 {
     int nx, ny, nz;
-    long long N() const { return (long long)nx * ny * nz; }
+    __host__ __device__ long long N() const { return (long long)nx * ny * nz; }
 };
 
 // ---------------------------------------------------------------- stencil ---
@@ -71,6 +71,41 @@ struct StrainStressArgs {
     int            red_site;
 };
 cudaError_t launch_strain_stress(const StrainStressArgs &a, cudaStream_t st);
+
+// -------------------------------------------------------- element kernels ---
+enum ElemMode { ELEM_RESIDUAL = 0, ELEM_AVERAGES = 1 };
+struct ElementArgs {
+    Grid3          g;
+    int            C, nstr, ngp, mode;
+    const double  *u;     // SoA FP64
+    const uint8_t *ms;
+    const double  *B;     // ngp x nstr x 8C
+    const double  *g0;    // nstr
+    const int     *law;   // per phase
+    const double  *Cph;   // per phase nstr x nstr (linear laws)
+    const double  *prm;   // per phase {K, G, sigma_y, h} (J2)
+    const double  *ep_t, *q_t; // committed internal variables [6][ngp][N], [ngp][N]
+    double        *ep, *q;     // trial internal variables (written)
+    double         ve;
+    double        *rows;  // RESIDUAL: [8C][N] element rows
+    // AVERAGES:
+    int            phase_filter;
+    double        *strain, *stress; // [N][nstr] or null
+    double        *strain_gp, *stress_gp; // [N][ngp][nstr] or null
+    double        *out_red;         // [0,nstr) sum eps, [nstr,2nstr) sum sig, [2nstr] count
+    GridRed        red;
+    int            red_site;
+};
+cudaError_t launch_element(const ElementArgs &a, cudaStream_t st);
+cudaError_t launch_gather(const double *rows, double *r, const Grid3 &g, int C, cudaStream_t st);
+cudaError_t launch_dot(const double *a, const double *b, long long n, double *out, GridRed red, int site,
+                       cudaStream_t st);
+cudaError_t launch_direction(double *d, const double *s, long long n, const CgScalars *scal, cudaStream_t st);
+// element means over Gauss points of the committed J2 variables (J2PlasticityNew.h:171-177)
+cudaError_t launch_ivar_gp(const double *ep_t, const double *q_t, int ngp, long long N, double *ep_out, double *q_out,
+                           cudaStream_t st);
+cudaError_t launch_ivar_mean(const double *ep_t, const double *q_t, int ngp, long long N, double *ep_out,
+                             double *q_out, cudaStream_t st);
 
 // ----------------------------------------------------------------- layout ---
 template <typename TI, typename TO>

@@ -41,6 +41,7 @@ class Context:
         self.n = tuple(int(v) for v in n)
         self.howmany = int(howmany)
         self.n_str = 3 if howmany == 1 else 6
+        self.n_gp = 1 if d.fe_type == C.FE_TYPES["HEX8R"] else 8
         self.N = self.n[0] * self.n[1] * self.n[2]
 
     def close(self):
@@ -115,8 +116,21 @@ class Context:
         return dict(strain_average=se, stress_average=ss, phase_strain=pe, phase_stress=ps, phase_count=cnt)
 
     def get_field(self, which):
-        k = self.howmany if which in (C.FIELD_U, C.FIELD_R, C.FIELD_U_PREV) else self.n_str
-        out = np.zeros(self.n + (k,))
+        if which in (C.FIELD_U, C.FIELD_R, C.FIELD_U_PREV):
+            shape = (self.howmany,)
+        elif which == C.FIELD_PLASTIC_STRAIN:
+            shape = (6,)
+        elif which == C.FIELD_HARDENING:
+            shape = (1,)
+        elif which in (C.FIELD_STRAIN_GP, C.FIELD_STRESS_GP):
+            shape = (self.n_gp, self.n_str)
+        elif which == C.FIELD_PLASTIC_STRAIN_GP:
+            shape = (self.n_gp, 6)
+        elif which == C.FIELD_HARDENING_GP:
+            shape = (self.n_gp,)
+        else:
+            shape = (self.n_str,)
+        out = np.zeros(self.n + shape)
         self._chk(self.lib.fansgpu_get_field(self.ctx, int(which), _ptr(out)))
         return out
 

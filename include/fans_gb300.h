@@ -75,6 +75,12 @@ extern "C" {
 #define FANSGPU_FIELD_STRAIN 2   /* element-averaged strain/gradient, [x][y][z][n_str] */
 #define FANSGPU_FIELD_STRESS 3   /* element-averaged stress/flux, [x][y][z][n_str] */
 #define FANSGPU_FIELD_U_PREV 4   /* previous step displacement (extrapolation) */
+#define FANSGPU_FIELD_PLASTIC_STRAIN 5 /* J2: Gauss-point mean of committed eps_p, [x][y][z][6] (get_field only) */
+#define FANSGPU_FIELD_HARDENING 6      /* J2: Gauss-point mean of committed q, [x][y][z] (get_field only) */
+#define FANSGPU_FIELD_STRAIN_GP 7          /* strain at every Gauss point, [x][y][z][n_gp][n_str] (get_field only) */
+#define FANSGPU_FIELD_STRESS_GP 8          /* stress at every Gauss point, [x][y][z][n_gp][n_str] (get_field only) */
+#define FANSGPU_FIELD_PLASTIC_STRAIN_GP 9  /* J2: committed eps_p, [x][y][z][n_gp][6] (get_field only) */
+#define FANSGPU_FIELD_HARDENING_GP 10      /* J2: committed q, [x][y][z][n_gp] (get_field only) */
 
 typedef struct fansgpu_ctx fansgpu_ctx;
 
