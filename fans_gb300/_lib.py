@@ -15,6 +15,7 @@ OK = 0
 EINVAL, ENOMEM, ECUDA, ENOTCONV, ENAN, EUNSUPPORTED, ESTATE = -1, -2, -3, -4, -5, -6, -7
 HEX8, HEX8R, BBAR = 0, 1, 2
 LAW_THERMAL_ISO, LAW_ELASTIC_ISO, LAW_J2_LINEAR, LAW_THERMAL_TRI, LAW_ELASTIC_TRI = 0, 1, 2, 3, 4
+LAW_PSEUDO_LINEAR, LAW_PSEUDO_NONLINEAR = 5, 6
 FP64, MIXED = 0, 1
 CG, FP = 0, 1
 L1, L2, LINF = 0, 1, 2
@@ -22,6 +23,8 @@ ABSOLUTE, RELATIVE = 0, 1
 FIELD_U, FIELD_R, FIELD_STRAIN, FIELD_STRESS, FIELD_U_PREV = 0, 1, 2, 3, 4
 FIELD_PLASTIC_STRAIN, FIELD_HARDENING = 5, 6
 FIELD_STRAIN_GP, FIELD_STRESS_GP, FIELD_PLASTIC_STRAIN_GP, FIELD_HARDENING_GP = 7, 8, 9, 10
+FIELD_PLASTIC_FLAG = 11
+VOXEL_STIFFNESS_SCALE = 0
 
 FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
 MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}
@@ -36,6 +39,8 @@ EXPORTS = [
     "fansgpu_commit_state", "fansgpu_residual", "fansgpu_apply_operator", "fansgpu_convolve",
     "fansgpu_green_table", "fansgpu_version", "fansgpu_reset", "fansgpu_get_stream", "fansgpu_set_timing",
     "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc", "fansgpu_set_refresh",
+    "fansgpu_enable_mixed_bc", "fansgpu_disable_mixed_bc", "fansgpu_get_gradient", "fansgpu_set_voxel_field",
+    "fansgpu_store_solution", "fansgpu_stiffness_gradient",
 ]
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
                 "residual64", "norm", "green_table", "strain_stress"]
@@ -113,6 +118,13 @@ def _declare(L):
     L.fansgpu_kernel_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_int64), ip]
     L.fansgpu_residual_norm_noalloc.argtypes = [vp, ctypes.c_int64, ip, vp, vp]
     L.fansgpu_set_refresh.argtypes = [vp, ctypes.c_double]
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    L.fansgpu_enable_mixed_bc.argtypes = [vp, ip, i32p, dp, ip, i32p, dp, ip]
+    L.fansgpu_disable_mixed_bc.argtypes = [vp]
+    L.fansgpu_get_gradient.argtypes = [vp, dp]
+    L.fansgpu_set_voxel_field.argtypes = [vp, ip, dp]
+    L.fansgpu_store_solution.argtypes = [vp, ip]
+    L.fansgpu_stiffness_gradient.argtypes = [vp, ip, dp, dp]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -85,6 +86,21 @@ struct fansgpu_ctx {
     int    *law_d = nullptr;
     double *prm_d = nullptr;
     double  alpha_warm = 0.1;
+
+    // per-voxel stiffness scale and stored solutions for the stiffness sensitivity
+    double             *vscale = nullptr, *zero_g0 = nullptr, *stored_u = nullptr;
+    std::vector<double> stored_g0;
+    std::vector<char>   stored_ok;
+
+    // mixed stress/strain boundary conditions (MixedBCController, mixedBCs.h:149-227)
+    bool                mixed_active = false;
+    std::vector<int>    idxE, idxF;
+    std::vector<double> PF, Mmix, g0_prev;
+
+    // tensor-core CG operator (mixed path): packed per-phase stiffness, hi/lo tf32 split
+    float *Wtc    = nullptr;
+    bool   use_tc = false;
+    bool   tc_allowed = true; // FANSGPU_STENCIL=simt at create time selects the CUDA-core operator
 };
 
 namespace fansgpu {
@@ -128,6 +144,7 @@ long long max_reduction_blocks(const Grid3 &g, int C)
 {
     long long b = std::max<long long>(kMaxBlocks, stencil_blocks(g));
     b           = std::max<long long>(b, (long long)C * g.nx * g.ny); // z passes: at least one row per CTA
+    b           = std::max<long long>(b, stencil_tc_blocks(g));
     return b;
 }
 
@@ -249,14 +266,20 @@ cudaError_t run_conv(fansgpu_ctx *ctx, const ConvPlan<T> &p, ConvArgs ca)
 
 // Internal variables (zero: the virgin state of initializeInternalVariables,
 // J2PlasticityNew.h:29-35) and the element-row scratch.
+int ensure_rows(fansgpu_ctx *ctx)
+{
+    return ctx->rows ? 0 : dalloc(ctx, &ctx->rows, 8LL * ctx->C * ctx->N);
+}
+
 int alloc_nonlinear(fansgpu_ctx *ctx)
 {
     const long long N = ctx->N, nep = 6LL * ctx->ngp * N, nq = (long long)ctx->ngp * N;
     int             rc;
+    if ((rc = ensure_rows(ctx)))
+        return rc;
     if (!ctx->ep_t) {
         if ((rc = dalloc(ctx, &ctx->ep_t, nep)) || (rc = dalloc(ctx, &ctx->ep, nep)) ||
-            (rc = dalloc(ctx, &ctx->q_t, nq)) || (rc = dalloc(ctx, &ctx->q, nq)) ||
-            (rc = dalloc(ctx, &ctx->rows, 8LL * ctx->C * N)))
+            (rc = dalloc(ctx, &ctx->q_t, nq)) || (rc = dalloc(ctx, &ctx->q, nq)))
             return rc;
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep_t, 0, sizeof(double) * nep, ctx->st));
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep, 0, sizeof(double) * nep, ctx->st));
@@ -276,14 +299,31 @@ int upload_law_tables(fansgpu_ctx *ctx)
         cudaFree(ctx->prm_d);
     ctx->law_d = nullptr;
     ctx->prm_d = nullptr;
-    if ((rc = dalloc(ctx, &ctx->law_d, ctx->nph)) || (rc = dalloc(ctx, &ctx->prm_d, 4 * ctx->nph)))
+    constexpr int kPrm = 8;
+    if ((rc = dalloc(ctx, &ctx->law_d, ctx->nph)) || (rc = dalloc(ctx, &ctx->prm_d, kPrm * ctx->nph)))
         return rc;
     std::vector<int>    lw(ctx->nph);
-    std::vector<double> pr(4 * ctx->nph, 0.0);
+    std::vector<double> pr(kPrm * ctx->nph, 0.0);
     for (int ph = 0; ph < ctx->nph; ++ph) {
-        lw[ph] = ctx->law[ph];
-        for (int i = 0; i < (int)std::min<size_t>(4, ctx->prm[ph].size()); ++i)
-            pr[4 * ph + i] = ctx->prm[ph][i];
+        lw[ph]                 = ctx->law[ph];
+        const auto &p          = ctx->prm[ph];
+        double     *o          = &pr[kPrm * ph];
+        auto        opt        = [&](size_t i, double d) { return p.size() > i ? p[i] : d; };
+        if (lw[ph] == FANSGPU_LAW_PSEUDO_LINEAR) { // PseudoPlastic.h:84-90
+            const double G = p[1], sy = p[2], h = p[3];
+            const double mi = opt(4, 0.0), nm = opt(5, 1.0);
+            const double v[8] = {p[0], G, sy, h, std::sqrt(2. / 3.) * sy / (2. * G), (3. * G) / (3. * G + h), mi, nm + mi};
+            std::copy(v, v + 8, o);
+        } else if (lw[ph] == FANSGPU_LAW_PSEUDO_NONLINEAR) { // PseudoPlastic.h:133-136
+            const double G = p[1], sy = p[2], n = p[3], e0 = p[4];
+            const double mi = opt(5, 0.0), nm = opt(6, 1.0);
+            const double ec = e0 * std::pow(sy / (3.0 * G * e0), 1.0 / (1.0 - n));
+            const double v[8] = {p[0], G, sy, n, e0, ec, mi, nm + mi};
+            std::copy(v, v + 8, o);
+        } else {
+            for (size_t i = 0; i < std::min<size_t>(kPrm, p.size()); ++i)
+                o[i] = p[i];
+        }
     }
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->law_d, lw.data(), sizeof(int) * lw.size(), cudaMemcpyHostToDevice, ctx->st));
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->prm_d, pr.data(), sizeof(double) * pr.size(), cudaMemcpyHostToDevice, ctx->st));
@@ -326,7 +366,8 @@ int setup(fansgpu_ctx *ctx)
         std::vector<double> K64(ctx->nph * NC * NC), Cph(ctx->nph * nstr * nstr), Ke;
         std::vector<float>  K32(ctx->nph * NC * NC);
         for (int ph = 0; ph < ctx->nph; ++ph) {
-            if (ctx->law[ph] == FANSGPU_LAW_J2_LINEAR)
+            if (ctx->law[ph] == FANSGPU_LAW_J2_LINEAR || ctx->law[ph] == FANSGPU_LAW_PSEUDO_LINEAR ||
+                ctx->law[ph] == FANSGPU_LAW_PSEUDO_NONLINEAR)
                 ctx->all_linear = false;
             if (!fe::law_C(ctx->law[ph], ctx->prm[ph], nstr, &Cph[ph * nstr * nstr]))
                 return fail(ctx, FANSGPU_EINVAL, "phase %d: law %d does not fit problem with n_str=%d", ph,
@@ -344,6 +385,19 @@ int setup(fansgpu_ctx *ctx)
         }
         ctx->K64h = K64;
         ctx->K32h = K32;
+        ctx->use_tc = false;
+        if (ctx->tc_allowed && ctx->desc.precision == FANSGPU_MIXED && stencil_tc_supported(ctx->g, C, ctx->nph)) {
+            std::vector<float> w(stencil_tc_weights(C, ctx->nph));
+            stencil_tc_pack_weights(C, ctx->nph, K32.data(), w.data());
+            if (ctx->Wtc)
+                cudaFree(ctx->Wtc);
+            ctx->Wtc = nullptr;
+            int rc4;
+            if ((rc4 = dalloc(ctx, &ctx->Wtc, w.size())))
+                return rc4;
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Wtc, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, ctx->st));
+            ctx->use_tc = true;
+        }
         {
             std::vector<float> kdf(2 * K64.size());
             for (size_t i = 0; i < K64.size(); ++i) {
@@ -494,6 +548,7 @@ ElementArgs element_args(fansgpu_ctx *ctx, const double *u, int mode)
     a.red   = ctx->red;
     a.red_site     = SITE_EL;
     a.phase_filter = -1;
+    a.scale        = ctx->vscale;
     return a;
 }
 
@@ -502,12 +557,26 @@ ElementArgs element_args(fansgpu_ctx *ctx, const double *u, int mode)
 // writes the trial internal variables, as get_sigma does) and the node gather.
 int run_residual64(fansgpu_ctx *ctx, const double *u, double *r)
 {
-    if (ctx->all_linear)
+    if (ctx->all_linear && !ctx->vscale)
         return run_stencil<double>(ctx, u, r, true);
     int e0 = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_element(element_args(ctx, u, ELEM_RESIDUAL), ctx->st));
     FANS_CUDA_CHECK(launch_gather(ctx->rows, r, ctx->g, ctx->C, ctx->st));
     tk_span(ctx, FANSGPU_K_RESIDUAL, e0, tk_mark(ctx));
+    return 0;
+}
+
+// y = K x through the element kernel with g0 = 0 (linear laws with a per-voxel scale).
+int run_operator_elem(fansgpu_ctx *ctx, const double *x, double *y)
+{
+    ElementArgs a = element_args(ctx, x, ELEM_RESIDUAL);
+    a.g0          = ctx->zero_g0;
+    a.ep          = nullptr;
+    a.q           = nullptr;
+    int e0        = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_element(a, ctx->st));
+    FANS_CUDA_CHECK(launch_gather(ctx->rows, y, ctx->g, ctx->C, ctx->st));
+    tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
     return 0;
 }
 
@@ -573,9 +642,21 @@ int solve_cg64(fansgpu_ctx *ctx)
         sa.scal     = ctx->scal;
         sa.red      = ctx->red;
         sa.red_site = SITE_STENCIL;
-        int e0 = tk_mark(ctx);
-        FANS_CUDA_CHECK(launch_stencil<double>(sa, ctx->st));
-        tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
+        if (ctx->vscale) {
+            // per-voxel stiffness: d = s + beta d, K d by the element kernel, <d, K d>, alpha
+            double *dn = ctx->dd[ctx->cur_d ^ 1];
+            FANS_CUDA_CHECK(cudaMemcpyAsync(dn, ctx->dd[ctx->cur_d], sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                            ctx->st));
+            FANS_CUDA_CHECK(launch_direction(dn, ctx->s, n, ctx->scal, ctx->st));
+            if ((rc = run_operator_elem(ctx, dn, ctx->Kd)))
+                return rc;
+            FANS_CUDA_CHECK(launch_dot(dn, ctx->Kd, n, &ctx->scal->dAd, ctx->red, SITE_DOT, ctx->st));
+            FANS_CUDA_CHECK(launch_set_alpha(ctx->scal, ctx->st));
+        } else {
+            int e0 = tk_mark(ctx);
+            FANS_CUDA_CHECK(launch_stencil<double>(sa, ctx->st));
+            tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
+        }
         ctx->cur_d ^= 1;
         UpdateArgs ua{n, ctx->r, ctx->Kd, ctx->u, ctx->dd[ctx->cur_d], ctx->s, ctx->tol.measure, 1, ctx->scal,
                       ctx->red, SITE_UPDATE};
@@ -641,7 +722,10 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         sa.red      = ctx->red;
         sa.red_site = SITE_STENCIL;
         int e0 = tk_mark(ctx);
-        FANS_CUDA_CHECK(launch_stencil<float>(sa, ctx->st));
+        if (ctx->use_tc)
+            FANS_CUDA_CHECK(launch_stencil_tc(sa, ctx->Wtc, ctx->nph, ctx->st));
+        else
+            FANS_CUDA_CHECK(launch_stencil<float>(sa, ctx->st));
         tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
         ctx->cur_d ^= 1;
         UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->e32, ctx->d32[ctx->cur_d], ctx->s32, ctx->tol.measure, 1, ctx->scal,
@@ -652,6 +736,9 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         if ((rc = sync_scalars(ctx)))
             return rc;
         ctx->iter++;
+        if (ctx->scal_h->converged == -3)
+            return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out at iteration %d",
+                        ctx->iter);
         if (ctx->scal_h->converged < 0)
             return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at iteration %d", ctx->iter);
         double est     = ctx->scal_h->err;
@@ -683,6 +770,8 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     return 0;
 }
 
+int mixed_update(fansgpu_ctx *ctx);
+
 // SolverFP::internalSolve: u -= G*r; r = R(u).
 int solve_fp64(fansgpu_ctx *ctx)
 {
@@ -707,7 +796,7 @@ int solve_fp64(fansgpu_ctx *ctx)
         ConvArgs ca{ctx->r, ctx->s, 1.0, 0, ctx->scal, ctx->red, SITE_CONV};
         FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
         FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, ctx->s, -1.0, n, ctx->st));
-        if ((rc = run_residual64(ctx, ctx->u, ctx->r)))
+        if ((rc = mixed_update(ctx)) || (rc = run_residual64(ctx, ctx->u, ctx->r)))
             return rc;
         { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 0, nullptr, ctx->red,
@@ -722,6 +811,32 @@ int solve_fp64(fansgpu_ctx *ctx)
         err_rel = err_value(ctx, ctx->scal_h->err);
     }
     return 0;
+}
+
+int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *stress_f, double *out,
+                  double *strain_gp = nullptr, double *stress_gp = nullptr, double *flag_f = nullptr);
+
+// MixedBCController::update (mixedBCs.h:160-177): g0_F += M (P_F - Q_F^T <sigma>).
+int mixed_update(fansgpu_ctx *ctx)
+{
+    if (!ctx->mixed_active || ctx->idxF.empty())
+        return 0;
+    int    rc;
+    double red[16];
+    if ((rc = setup(ctx)) || (rc = strain_stress(ctx, -1, nullptr, nullptr, red, nullptr, nullptr, nullptr)))
+        return rc;
+    const int nf = (int)ctx->idxF.size();
+    std::vector<double> rhs(nf);
+    for (int a = 0; a < nf; ++a)
+        rhs[a] = ctx->PF[a] - red[ctx->nstr + ctx->idxF[a]] / (double)ctx->N;
+    for (int a = 0; a < nf; ++a) {
+        double dE = 0.0;
+        for (int b = 0; b < nf; ++b)
+            dE += ctx->Mmix[a * nf + b] * rhs[b];
+        ctx->g0[ctx->idxF[a]] += dE;
+    }
+    ctx->force_dirty = true;
+    return setup(ctx);
 }
 
 // <a, b> on the device into *slot (a CgScalars member); read on the next sync.
@@ -782,7 +897,7 @@ int solve_cg_nl(fansgpu_ctx *ctx)
         if ((rc = host_dot(ctx, ctx->r, d, &rpd)))
             return rc;
         FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, d, alpha_curr, n, ctx->st));
-        if ((rc = run_residual64(ctx, ctx->u, rnew)) || (rc = host_dot(ctx, rnew, d, &r1pd)))
+        if ((rc = mixed_update(ctx)) || (rc = run_residual64(ctx, ctx->u, rnew)) || (rc = host_dot(ctx, rnew, d, &r1pd)))
             return rc;
         while (it < max_it && err > ls_tol) {
             const double denom = r1pd - rpd;
@@ -797,7 +912,8 @@ int solve_cg_nl(fansgpu_ctx *ctx)
             rpd        = r1pd;
             alpha_curr = alpha_next;
             ++it;
-            if ((rc = run_residual64(ctx, ctx->u, rnew)) || (rc = host_dot(ctx, rnew, d, &r1pd)))
+            if ((rc = mixed_update(ctx)) || (rc = run_residual64(ctx, ctx->u, rnew)) ||
+                (rc = host_dot(ctx, rnew, d, &r1pd)))
                 return rc;
         }
         ctx->alpha_warm = (it == max_it && err > ls_tol) ? 0.1 : alpha_curr;
@@ -829,9 +945,52 @@ int commit_ivars(fansgpu_ctx *ctx)
 }
 
 int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *stress_f, double *out,
-                  double *strain_gp = nullptr, double *stress_gp = nullptr)
+                  double *strain_gp, double *stress_gp, double *flag_f)
 {
-    if (!ctx->all_linear || strain_gp || stress_gp) {
+    if (ctx->all_linear && !ctx->vscale && !strain_f && !stress_f && !strain_gp && !stress_gp && !flag_f &&
+        ctx->nph <= 2) {
+        // averages only: per-phase strain sums, stresses by linearity (C_ph times the sums)
+        StrainStressArgs a{};
+        a.g     = ctx->g;
+        a.C     = ctx->C;
+        a.nstr  = ctx->nstr;
+        a.u     = ctx->u;
+        a.ms    = ctx->d_ms;
+        for (int d = 0; d < 3; ++d)
+            a.inv4l[d] = 0.25 / ctx->le[d];
+        a.g0       = ctx->g0_d;
+        a.nph      = ctx->nph;
+        a.out_red  = ctx->red_out;
+        a.red      = ctx->red;
+        a.red_site = SITE_SS;
+        const int ns = ctx->nstr, nphm = 2;
+        int       e0 = tk_mark(ctx);
+        FANS_CUDA_CHECK(launch_strain_sums(a, ctx->st));
+        tk_span(ctx, FANSGPU_K_STRAIN_STRESS, e0, tk_mark(ctx));
+        double sums[4 * 7];
+        FANS_CUDA_CHECK(cudaMemcpyAsync(sums, ctx->red_out, sizeof(double) * nphm * (ns + 1), cudaMemcpyDeviceToHost,
+                                        ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        tk_flush(ctx);
+        std::vector<double> Cm(ns * ns);
+        for (int i = 0; i < 2 * ns + 1; ++i)
+            out[i] = 0.0;
+        for (int ph = 0; ph < ctx->nph; ++ph) {
+            if (phase_filter >= 0 && ph != phase_filter)
+                continue;
+            fe::law_C(ctx->law[ph], ctx->prm[ph], ns, Cm.data());
+            for (int i = 0; i < ns; ++i) {
+                out[i] += sums[ph * ns + i];
+                double acc = 0.0;
+                for (int k = 0; k < ns; ++k)
+                    acc += Cm[i * ns + k] * sums[ph * ns + k];
+                out[ns + i] += acc;
+            }
+            out[2 * ns] += sums[nphm * ns + ph];
+        }
+        return 0;
+    }
+    if (!ctx->all_linear || ctx->vscale || strain_gp || stress_gp || flag_f) {
         // per-Gauss-point law evaluation (Matmodel::getStrainStress, matmodel.h:203-225)
         ElementArgs a  = element_args(ctx, ctx->u, ELEM_AVERAGES);
         a.phase_filter = phase_filter;
@@ -839,6 +998,7 @@ int strain_stress(fansgpu_ctx *ctx, int phase_filter, double *strain_f, double *
         a.stress       = stress_f;
         a.strain_gp    = strain_gp;
         a.stress_gp    = stress_gp;
+        a.flag         = flag_f;
         a.out_red      = ctx->red_out;
         int e0         = tk_mark(ctx);
         FANS_CUDA_CHECK(launch_element(a, ctx->st));
@@ -913,6 +1073,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
 
     fansgpu_ctx *ctx = new fansgpu_ctx();
     ctx->desc        = *desc;
+    if (const char *ev = std::getenv("FANSGPU_STENCIL"))
+        ctx->tc_allowed = std::strcmp(ev, "simt") != 0;
     ctx->g           = Grid3{n[0], n[1], n[2]};
     ctx->C           = desc->howmany;
     ctx->nstr        = nstr_of(ctx->C);
@@ -1026,7 +1188,8 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d,
-                    ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d};
+                    ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc,
+                    ctx->vscale, ctx->zero_g0, ctx->stored_u};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -1142,15 +1305,16 @@ int fansgpu_set_phase_material(fansgpu_ctx *ctx, int32_t phase, int32_t law, con
         return FANSGPU_EINVAL;
     if (phase < 0 || phase > 255)
         return fail(ctx, FANSGPU_EINVAL, "MaterialManager: Invalid or duplicate phase %d", phase);
-    if (law < 0 || law > 4 || !params || n_params < 1)
+    if (law < 0 || law > 6 || !params || n_params < 1)
         return fail(ctx, FANSGPU_EINVAL, "invalid material law %d / parameters", law);
     const bool thermal = (law == FANSGPU_LAW_THERMAL_ISO || law == FANSGPU_LAW_THERMAL_TRI);
     if (thermal != (ctx->C == 1))
         return fail(ctx, FANSGPU_EINVAL, "law %d is not valid for a %s problem", law, ctx->C == 1 ? "thermal" : "mechanical");
-    const int need[5] = {1, 2, 4, 9, 36};
+    const int need[7] = {1, 2, 4, 9, 36, 4, 5}, most[7] = {1, 2, 4, 9, 36, 6, 7};
     if (n_params < need[law])
         return fail(ctx, FANSGPU_EINVAL, "law %d needs %d parameters, got %d", law, need[law], n_params);
-    for (int i = 0; i < need[law]; ++i)
+    n_params = std::min(n_params, most[law]);
+    for (int i = 0; i < n_params; ++i)
         if (!std::isfinite(params[i]))
             return fail(ctx, FANSGPU_EINVAL, "non-finite material parameter %d of phase %d", i, phase);
     if (phase >= (int)ctx->law.size()) {
@@ -1159,7 +1323,7 @@ int fansgpu_set_phase_material(fansgpu_ctx *ctx, int32_t phase, int32_t law, con
         ctx->assigned.resize(phase + 1, 0);
     }
     ctx->law[phase]      = law;
-    ctx->prm[phase]      = std::vector<double>(params, params + need[law]);
+    ctx->prm[phase]      = std::vector<double>(params, params + n_params);
     ctx->assigned[phase] = 1;
     ctx->tables_dirty    = true;
     return 0;
@@ -1207,6 +1371,170 @@ int fansgpu_set_gradient(fansgpu_ctx *ctx, const double *g0)
     return 0;
 }
 
+int fansgpu_get_gradient(fansgpu_ctx *ctx, double *g0)
+{
+    if (!ctx || !g0)
+        return FANSGPU_EINVAL;
+    for (int i = 0; i < ctx->nstr; ++i)
+        g0[i] = ctx->g0[i];
+    return 0;
+}
+
+int fansgpu_enable_mixed_bc(fansgpu_ctx *ctx, int32_t n_e, const int32_t *idx_e, const double *strain_e, int32_t n_f,
+                            const int32_t *idx_f, const double *stress_f, int32_t step)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    const int ns = ctx->nstr;
+    if (n_e < 0 || n_f < 0 || (n_e && (!idx_e || !strain_e)) || (n_f && (!idx_f || !stress_f)) || step < 0)
+        return fail(ctx, FANSGPU_EINVAL, "mixed BC: bad arguments");
+    // MixedBC::from_json checks (mixedBCs.h:69-88)
+    std::vector<char> present(ns, 0);
+    for (int i = 0; i < n_e; ++i) {
+        if (idx_e[i] < 0 || idx_e[i] >= ns)
+            return fail(ctx, FANSGPU_EINVAL, "strain index out of range");
+        present[idx_e[i]] = 1;
+    }
+    for (int i = 0; i < n_f; ++i) {
+        if (idx_f[i] < 0 || idx_f[i] >= ns)
+            return fail(ctx, FANSGPU_EINVAL, "stress index out of range");
+        if (present[idx_f[i]])
+            return fail(ctx, FANSGPU_EINVAL, "index appears in both strain_indices and stress_indices");
+        present[idx_f[i]] = 1;
+    }
+    for (int k = 0; k < ns; ++k)
+        if (!present[k])
+            return fail(ctx, FANSGPU_EINVAL, "each component must be either strain- or stress-controlled");
+    if (!ctx->have_ref)
+        return fail(ctx, FANSGPU_ESTATE, "set_reference must be called before enabling mixed BCs");
+    // MixedBC::finalize (mixedBCs.h:30-48): M = pinv(Q_F^T C0 Q_F)
+    ctx->idxE.assign(idx_e, idx_e + n_e);
+    ctx->idxF.assign(idx_f, idx_f + n_f);
+    ctx->PF.assign(stress_f, stress_f + n_f);
+    std::vector<double> A(n_f * n_f);
+    for (int a = 0; a < n_f; ++a)
+        for (int b = 0; b < n_f; ++b)
+            A[a * n_f + b] = ctx->kapparef[idx_f[a] * ns + idx_f[b]];
+    ctx->Mmix = fe::sym_pinv(A, n_f);
+    // MixedBCController::activate (mixedBCs.h:180-226)
+    if (step == 0) {
+        ctx->g0.assign(ns, 0.0);
+        ctx->g0_prev = ctx->g0;
+    } else {
+        if (ctx->g0_prev.size() != (size_t)ns)
+            ctx->g0_prev = ctx->g0;
+        std::vector<double> delta(ns);
+        for (int i = 0; i < ns; ++i)
+            delta[i] = ctx->g0[i] - ctx->g0_prev[i];
+        ctx->g0_prev = ctx->g0;
+        for (int i = 0; i < n_f; ++i)
+            ctx->g0[idx_f[i]] += delta[idx_f[i]];
+    }
+    for (int i = 0; i < n_e; ++i)
+        ctx->g0[idx_e[i]] = strain_e[i];
+    ctx->force_dirty  = true;
+    ctx->mixed_active = true;
+    return mixed_update(ctx);
+}
+
+int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *values)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (field != FANSGPU_VOXEL_STIFFNESS_SCALE)
+        return fail(ctx, FANSGPU_EINVAL, "unknown voxel field %d", field);
+    if (!values) { // back to the phase table alone
+        if (ctx->vscale)
+            cudaFree(ctx->vscale);
+        ctx->vscale = nullptr;
+        return 0;
+    }
+    for (long long i = 0; i < ctx->N; ++i)
+        if (!(values[i] > 0.0) || !std::isfinite(values[i]))
+            return fail(ctx, FANSGPU_EINVAL, "stiffness scale must be positive and finite (voxel %lld)", i);
+    int rc;
+    if ((!ctx->vscale && (rc = dalloc(ctx, &ctx->vscale, ctx->N))) || (rc = ensure_rows(ctx)) ||
+        (!ctx->zero_g0 && (rc = dalloc(ctx, &ctx->zero_g0, 9))))
+        return rc;
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->zero_g0, 0, sizeof(double) * 9, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, values, sizeof(double) * ctx->N, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->vscale, ctx->staging, sizeof(double) * ctx->N, cudaMemcpyDeviceToDevice,
+                                    ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_store_solution(fansgpu_ctx *ctx, int32_t slot)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (slot < 0 || slot >= 6)
+        return fail(ctx, FANSGPU_EINVAL, "solution slot must be in [0, 6)");
+    int rc;
+    if (!ctx->stored_u && (rc = dalloc(ctx, &ctx->stored_u, 6 * ctx->n)))
+        return rc;
+    ctx->stored_g0.resize(6 * ctx->nstr, 0.0);
+    ctx->stored_ok.resize(6, 0);
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->stored_u + slot * ctx->n, ctx->u, sizeof(double) * ctx->n,
+                                    cudaMemcpyDeviceToDevice, ctx->st));
+    for (int i = 0; i < ctx->nstr; ++i)
+        ctx->stored_g0[slot * ctx->nstr + i] = ctx->g0[i];
+    ctx->stored_ok[slot] = 1;
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int fansgpu_stiffness_gradient(fansgpu_ctx *ctx, int32_t n, const double *W, double *grad)
+{
+    if (!ctx || !W || !grad)
+        return FANSGPU_EINVAL;
+    if (n < 1 || n > 6 || (int)ctx->stored_ok.size() < n)
+        return fail(ctx, FANSGPU_EINVAL, "stiffness gradient needs solutions stored in slots 0..n-1 (n <= 6)");
+    for (int k = 0; k < n; ++k)
+        if (!ctx->stored_ok[k])
+            return fail(ctx, FANSGPU_EINVAL, "solution slot %d not stored", k);
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    if (!ctx->all_linear)
+        return fail(ctx, FANSGPU_EUNSUPPORTED, "stiffness gradient is defined for linear laws");
+    double *g0w = nullptr;
+    if ((rc = dalloc(ctx, &g0w, n * ctx->nstr + n * n)))
+        return rc;
+    std::vector<double> h(ctx->stored_g0.begin(), ctx->stored_g0.begin() + n * ctx->nstr);
+    h.insert(h.end(), W, W + n * n);
+    SensArgs a{};
+    a.g    = ctx->g;
+    a.C    = ctx->C;
+    a.nstr = ctx->nstr;
+    a.ngp  = ctx->ngp;
+    a.n    = n;
+    a.u    = ctx->stored_u;
+    a.g0   = g0w;
+    a.W    = g0w + n * ctx->nstr;
+    a.ms   = ctx->d_ms;
+    a.B    = ctx->Bgp_d;
+    a.Cph  = ctx->Cph;
+    a.grad = ctx->staging;
+    cudaError_t e = cudaMemcpyAsync(g0w, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->st);
+    if (e == cudaSuccess)
+        e = launch_sensitivity(a, ctx->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(grad, ctx->staging, sizeof(double) * ctx->N, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->st);
+    cudaFree(g0w);
+    return e == cudaSuccess ? 0 : fail(ctx, FANSGPU_ECUDA, "stiffness gradient: %s", cudaGetErrorString(e));
+}
+
+int fansgpu_disable_mixed_bc(fansgpu_ctx *ctx)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    ctx->mixed_active = false;
+    return 0;
+}
+
 int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *t)
 {
     if (!ctx || !t)
@@ -1234,9 +1562,9 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
     int refinements = 0;
     if (ctx->desc.method == FANSGPU_FP)
         rc = solve_fp64(ctx);
-    else if (!ctx->all_linear)
-        rc = solve_cg_nl(ctx); // nonlinear laws run the FP64 path at either precision setting
-    else if (ctx->desc.precision == FANSGPU_MIXED)
+    else if (!ctx->all_linear || ctx->mixed_active)
+        rc = solve_cg_nl(ctx); // nonlinear laws and mixed BCs run the FP64 line-search path (solverCG.h:96)
+    else if (ctx->desc.precision == FANSGPU_MIXED && !ctx->vscale)
         rc = solve_cg_mixed(ctx, &refinements);
     else
         rc = solve_cg64(ctx);
@@ -1343,7 +1671,8 @@ int fansgpu_homogenized_tangent(fansgpu_ctx *ctx, double pert, double *out)
         g[i] += linear ? 1.0 : pert;
         if ((rc = fansgpu_set_gradient(ctx, g.data())))
             return rc;
-        rc = fansgpu_solve(ctx, nullptr);
+        ctx->mixed_active = false; // solver.h:769
+        rc                = fansgpu_solve(ctx, nullptr);
         if (rc && rc != FANSGPU_ENOTCONV)
             return rc;
         if ((rc = fansgpu_homogenized_stress(ctx, sig.data())))
@@ -1393,6 +1722,17 @@ int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host)
                                          ps ? nullptr : ctx->staging, ctx->st));
         FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N * (ps ? 6 : 1), cudaMemcpyDeviceToHost,
                                         ctx->st));
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        return 0;
+    }
+    if (which == FANSGPU_FIELD_PLASTIC_FLAG) {
+        int rc = setup(ctx);
+        if (rc)
+            return rc;
+        double red[16];
+        if ((rc = strain_stress(ctx, -1, nullptr, nullptr, red, nullptr, nullptr, ctx->staging)))
+            return rc;
+        FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->st));
         FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
         return 0;
     }

@@ -97,6 +97,7 @@ template <int NV>
 __device__ __forceinline__ bool grid_partial_commit(const double (&v)[NV], double *partials, unsigned int *counter,
                                                     int nblocks)
 {
+    static_assert(NV <= kMaxRed, "a block's partials must fit its kMaxRed slots");
     __shared__ bool s_last;
     const int       bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     if (threadIdx.x == 0) {

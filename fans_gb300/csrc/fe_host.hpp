@@ -2,6 +2,7 @@
 // Gauss-point B matrices, per-phase constitutive matrices, element stiffness
 // and the reference element stiffness.  One-off per context, in FP64.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -85,7 +86,7 @@ inline int gauss_B(int fe_type, int C, const double le[3], std::vector<double> &
 // Constitutive matrix of a linear law (nstr x nstr, row-major).
 // law 0 thermal iso: kappa I (LinearThermal.h:186);
 // law 1 elastic iso: lambda on the normal 3x3 block + 2 mu I (LinearElastic.h:28-35);
-// law 2 J2 (elastic part, used for the reference/tangent): as law 1;
+// laws 2, 5, 6 (J2, PseudoPlastic; their elastic part, for the reference/tangent): as law 1;
 // law 3/4 triclinic: the given matrix (LinearThermal.h:250-254, LinearElastic.h:114-129).
 inline bool law_C(int law, const std::vector<double> &prm, int nstr, double *C)
 {
@@ -95,7 +96,7 @@ inline bool law_C(int law, const std::vector<double> &prm, int nstr, double *C)
             C[i * 3 + i] = prm[0];
         return true;
     }
-    if ((law == 1 || law == 2) && nstr == 6) {
+    if ((law == 1 || law == 2 || law == 5 || law == 6) && nstr == 6) {
         const double lam = prm[0] - (2.0 / 3.0) * prm[1];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)
@@ -199,6 +200,63 @@ inline bool radix_plan(int n, int *rad, int *nrad, int maxr)
         }
     *nrad = k;
     return m == 1;
+}
+
+// Pseudo-inverse of a symmetric n x n matrix (cyclic Jacobi eigen-decomposition;
+// eigenvalues below n * eps * max|lambda| are dropped) -- the
+// completeOrthogonalDecomposition().pseudoInverse() of mixedBCs.h:45 for the
+// symmetric Q_F^T C0 Q_F.
+inline std::vector<double> sym_pinv(std::vector<double> A, int n)
+{
+    std::vector<double> V(n * n, 0.0);
+    for (int i = 0; i < n; ++i)
+        V[i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q)
+                off += A[p * n + q] * A[p * n + q];
+        if (off < 1e-300)
+            break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p * n + q];
+                if (std::fabs(apq) < 1e-300)
+                    continue;
+                const double theta = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) { // A <- A J
+                    const double akp = A[k * n + p], akq = A[k * n + q];
+                    A[k * n + p] = c * akp - s * akq;
+                    A[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) { // A <- J^T A
+                    const double apk = A[p * n + k], aqk = A[q * n + k];
+                    A[p * n + k] = c * apk - s * aqk;
+                    A[q * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = V[k * n + p], vkq = V[k * n + q];
+                    V[k * n + p] = c * vkp - s * vkq;
+                    V[k * n + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    double lmax = 0.0;
+    for (int i = 0; i < n; ++i)
+        lmax = std::max(lmax, std::fabs(A[i * n + i]));
+    const double thr = n * 2.220446049250313e-16 * lmax;
+    std::vector<double> P(n * n, 0.0);
+    for (int k = 0; k < n; ++k) {
+        const double l = A[k * n + k];
+        if (std::fabs(l) <= thr)
+            continue;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j)
+                P[i * n + j] += V[i * n + k] * V[j * n + k] / l;
+    }
+    return P;
 }
 
 } // namespace fe

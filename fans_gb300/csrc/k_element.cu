@@ -21,6 +21,7 @@ namespace fansgpu {
 namespace {
 
 constexpr int kElThreads = 128;
+constexpr int kPrm       = 8; // law parameters per phase
 
 __device__ __forceinline__ void elem_nodes(int nx, int ny, int nz, long long e, long long idx[8])
 {
@@ -83,6 +84,57 @@ __device__ __forceinline__ void j2_sigma(const double *prm, const double (&e)[6]
 // butterfly reduce-scatter, after which lane gp holds NCOL/NGP of the sums.
 // The loop runs whole warps (the trip count is rounded up to 32) so that every
 // shuffle sees all lanes; lanes past the end compute on zeros and store nothing.
+// PseudoPlasticLinearHardening / NonLinearHardening::get_sigma (PseudoPlastic.h:
+// 92-115, 138-160), history-free.  prm (8 per phase): linear {K, G, sigma_y, h,
+// eps_crit, E_s, flag_elastic, flag_plastic}; nonlinear {K, G, sigma_y, n, eps_0,
+// eps_crit, flag_elastic, flag_plastic}.  Returns the Gauss point's plastic flag.
+__device__ __forceinline__ double pseudo_sigma(int law, const double *prm, const double (&e)[6], double (&sig)[6])
+{
+    const double K = prm[0], G = prm[1], sy = prm[2];
+    const double treps = e[0] + e[1] + e[2];
+    double       dev[6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        dev[i] = e[i] - (1.0 / 3.0) * treps;
+#pragma unroll
+    for (int i = 3; i < 6; ++i)
+        dev[i] = e[i];
+    double n2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        n2 += dev[i] * dev[i];
+    const double nrm  = sqrt(n2);
+    const double buf1 = K * treps;
+    double       buf2, flag;
+    if (law == FANSGPU_LAW_PSEUDO_LINEAR) {
+        const double h = prm[3], eps_crit = prm[4], E_s = prm[5];
+        if (nrm <= eps_crit) {
+            buf2 = 2.0 * G;
+            flag = prm[6];
+        } else {
+            buf2 = (sqrt(2.0 / 3.0) * sy + (2.0 / 3.0) * E_s * h * (nrm - eps_crit)) / nrm;
+            flag = prm[7];
+        }
+    } else {
+        const double n = prm[3], eps0 = prm[4], eps_crit = prm[5];
+        const double eq = sqrt(2.0 / 3.0) * nrm;
+        if (eq <= eps_crit) {
+            buf2 = 2.0 * G;
+            flag = prm[6];
+        } else {
+            buf2 = sqrt(2.0 / 3.0) * sy * pow(eq / eps0, n) / nrm;
+            flag = prm[7];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        sig[i] = buf1 + buf2 * dev[i];
+#pragma unroll
+    for (int i = 3; i < 6; ++i)
+        sig[i] = buf2 * dev[i];
+    return flag;
+}
+
 template <int C, int NGP, int MODE>
 __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
 {
@@ -134,13 +186,17 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
                 e[i] = acc + a.g0[i];
             }
         }
-        if (valid && C == 3 && a.law[ph] == FANSGPU_LAW_J2_LINEAR) {
+        const int law = valid ? a.law[ph] : -1;
+        double    flag = 0.0; // elements outside a PseudoPlastic model keep flag 0 (PseudoPlastic.h:37-40)
+        if (C == 3 && (law == FANSGPU_LAW_PSEUDO_LINEAR || law == FANSGPU_LAW_PSEUDO_NONLINEAR)) {
+            flag = pseudo_sigma(law, a.prm + ph * kPrm, e, sig);
+        } else if (C == 3 && law == FANSGPU_LAW_J2_LINEAR) {
             double          ep_in[6], ep_out[6], q_out;
             const long long base = (long long)gp * N + el;
 #pragma unroll
             for (int i = 0; i < 6; ++i)
                 ep_in[i] = a.ep_t[(long long)i * NGP * N + base];
-            j2_sigma(a.prm + ph * 4, e, ep_in, a.q_t[base], sig, ep_out, q_out);
+            j2_sigma(a.prm + ph * kPrm, e, ep_in, a.q_t[base], sig, ep_out, q_out);
             if (a.ep) {
 #pragma unroll
                 for (int i = 0; i < 6; ++i)
@@ -157,6 +213,12 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
                     acc += Cm[i * NSTR + k] * e[k];
                 sig[i] = acc;
             }
+        }
+        if (valid && a.scale) {
+            const double sc = a.scale[el];
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i)
+                sig[i] *= sc;
         }
         if constexpr (MODE == ELEM_RESIDUAL) {
             double v[NCOL];
@@ -198,12 +260,16 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
                 for (int i = 0; i < NSTR; ++i)
                     a.stress_gp[(el * NGP + gp) * NSTR + i] = sig[i];
 #pragma unroll
-            for (int m = NGP / 2; m >= 1; m /= 2)
+            for (int m = NGP / 2; m >= 1; m /= 2) {
 #pragma unroll
                 for (int i = 0; i < NSTR; ++i) {
                     e[i] += __shfl_xor_sync(0xffffffffu, e[i], m);
                     sig[i] += __shfl_xor_sync(0xffffffffu, sig[i], m);
                 }
+                flag += __shfl_xor_sync(0xffffffffu, flag, m);
+            }
+            if (valid && gp == 0 && a.flag)
+                a.flag[el] = flag / NGP;
             if (valid && gp == 0) {
 #pragma unroll
                 for (int i = 0; i < NSTR; ++i) {
@@ -342,7 +408,91 @@ __global__ void k_ivar_gp(const double *__restrict__ ep_t, const double *__restr
     }
 }
 
+// one thread per element; the Gauss-point strains of the n solutions in registers
+template <int C, int NGP, int NMAX>
+__global__ void __launch_bounds__(128) k_sensitivity(SensArgs a)
+{
+    constexpr int NSTR = C == 1 ? 3 : 6, NCOL = 8 * C;
+    __shared__ double Bs[NGP * NSTR * NCOL];
+    for (int i = threadIdx.x; i < NGP * NSTR * NCOL; i += blockDim.x)
+        Bs[i] = a.B[i];
+    __syncthreads();
+    const int       nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const long long N  = (long long)nx * ny * nz;
+    for (long long el = blockIdx.x * (long long)blockDim.x + threadIdx.x; el < N; el += (long long)gridDim.x * blockDim.x) {
+        long long idx[8];
+        elem_nodes(nx, ny, nz, el, idx);
+        const double *Cm  = a.Cph + a.ms[el] * NSTR * NSTR;
+        double        acc = 0.0;
+        for (int gp = 0; gp < NGP; ++gp) {
+            const double *Bg = Bs + gp * NSTR * NCOL;
+            double        eps[NMAX][NSTR];
+            for (int k = 0; k < a.n; ++k) {
+                const double *u = a.u + (long long)k * C * N;
+                double        ue[NCOL];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const double u0 = u[c * N + idx[0]];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        ue[q * C + c] = u[c * N + idx[q]] - u0;
+                }
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i) {
+                    double s = a.g0[k * NSTR + i];
+#pragma unroll
+                    for (int q = 0; q < NCOL; ++q)
+                        s += Bg[i * NCOL + q] * ue[q];
+                    eps[k][i] = s;
+                }
+            }
+            for (int j = 0; j < a.n; ++j) {
+                double ce[NSTR];
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i) {
+                    double s = 0.0;
+#pragma unroll
+                    for (int k = 0; k < NSTR; ++k)
+                        s += Cm[i * NSTR + k] * eps[j][k];
+                    ce[i] = s;
+                }
+                for (int i = 0; i < a.n; ++i) {
+                    double s = 0.0;
+#pragma unroll
+                    for (int k = 0; k < NSTR; ++k)
+                        s += eps[i][k] * ce[k];
+                    acc += a.W[i * a.n + j] * s;
+                }
+            }
+        }
+        a.grad[el] = acc / (NGP * (double)N);
+    }
+}
+
+__global__ void k_set_alpha(CgScalars *scal)
+{
+    scal->alpha = scal->delta / scal->dAd;
+}
+
 } // namespace
+
+cudaError_t launch_sensitivity(const SensArgs &a, cudaStream_t st)
+{
+    const int nb = grid_blocks_for(a.g.N());
+    if (a.n < 1 || a.n > 6)
+        return cudaErrorInvalidValue;
+    if (a.C == 1)
+        a.ngp == 8 ? k_sensitivity<1, 8, 6><<<nb, 128, 0, st>>>(a) : k_sensitivity<1, 1, 6><<<nb, 128, 0, st>>>(a);
+    else
+        a.ngp == 8 ? k_sensitivity<3, 8, 6><<<nb, 128, 0, st>>>(a) : k_sensitivity<3, 1, 6><<<nb, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_alpha(CgScalars *scal, cudaStream_t st)
+{
+    k_set_alpha<<<1, 1, 0, st>>>(scal);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_ivar_gp(const double *ep_t, const double *q_t, int ngp, long long N, double *ep_out, double *q_out,
                            cudaStream_t st)

@@ -649,6 +649,86 @@ cudaError_t launch_residual_df(const StencilArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// Per-phase sums of the element strain (centre gradient + g0) and element
+// counts: out[ph*NSTR + i], out[NPHM*NSTR + ph].  With linear laws the stress
+// sums follow on the host as C_ph times the strain sums (matmodel.h:203-225 by
+// linearity), so the averages need no per-element stress.
+template <int C, int NSTR, int NPHM>
+__global__ void __launch_bounds__(256) k_strain_sums(StrainStressArgs a)
+{
+    constexpr int NV = NPHM * (NSTR + 1);
+    static_assert(NV <= kMaxRed, "reduction partial slots");
+    __shared__ double red_smem[32 * NV];
+    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const long long N = (long long)nx * ny * nz;
+    double acc[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        acc[i] = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N; e += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(e % nz), y = (int)((e / nz) % ny), x = (int)(e / ((long long)nz * ny));
+        const int ph = a.ms[e];
+        const int x1 = x + 1 == nx ? 0 : x + 1, y1 = y + 1 == ny ? 0 : y + 1, z1 = z + 1 == nz ? 0 : z + 1;
+        const long long i0 = ((long long)x * ny + y) * nz, i1 = ((long long)x1 * ny + y) * nz;
+        const long long i2 = ((long long)x * ny + y1) * nz, i3 = ((long long)x1 * ny + y1) * nz;
+        double g[C][3];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const double *u = a.u + c * N;
+            const double u0 = u[i0 + z], u1 = u[i1 + z], u2 = u[i2 + z], u3 = u[i3 + z];
+            const double u4 = u[i0 + z1], u5 = u[i1 + z1], u6 = u[i2 + z1], u7 = u[i3 + z1];
+            g[c][0] = ((u1 - u0) + (u3 - u2) + (u5 - u4) + (u7 - u6)) * a.inv4l[0];
+            g[c][1] = ((u2 - u0) + (u3 - u1) + (u6 - u4) + (u7 - u5)) * a.inv4l[1];
+            g[c][2] = ((u4 - u0) + (u5 - u1) + (u6 - u2) + (u7 - u3)) * a.inv4l[2];
+        }
+        double eps[NSTR];
+        if (C == 1) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                eps[i] = g[0][i];
+        } else {
+            const double sh = 7.071067811865476e-01;
+            eps[0] = g[0][0];
+            eps[1] = g[C > 1 ? 1 : 0][1];
+            eps[2] = g[C > 2 ? 2 : 0][2];
+            eps[3] = sh * (g[0][1] + g[C > 1 ? 1 : 0][0]);
+            eps[4] = sh * (g[0][2] + g[C > 2 ? 2 : 0][0]);
+            eps[5] = sh * (g[C > 1 ? 1 : 0][2] + g[C > 2 ? 2 : 0][1]);
+        }
+#pragma unroll
+        for (int k = 0; k < NPHM; ++k)
+            if (ph == k) {
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i)
+                    acc[k * NSTR + i] += eps[i] + a.g0[i];
+                acc[NPHM * NSTR + k] += 1.0;
+            }
+    }
+    int ops[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        ops[i] = RED_SUM;
+    block_reduce<NV>(acc, ops, red_smem);
+    if (grid_partial_commit<NV>(acc, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+        grid_final<NV>(acc, ops, a.red.partials, gridDim.x, red_smem);
+        if (threadIdx.x == 0)
+            for (int i = 0; i < NV; ++i)
+                a.out_red[i] = acc[i];
+    }
+}
+
+cudaError_t launch_strain_sums(const StrainStressArgs &a, cudaStream_t st)
+{
+    const int nb = grid_blocks_for(a.g.N());
+    if (a.nph > 2)
+        return cudaErrorInvalidValue;
+    if (a.C == 1)
+        k_strain_sums<1, 3, 2><<<nb, 256, 0, st>>>(a);
+    else
+        k_strain_sums<3, 6, 2><<<nb, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_strain_stress(const StrainStressArgs &a, cudaStream_t st)
 {
     const int nb = grid_blocks_for(a.g.N());

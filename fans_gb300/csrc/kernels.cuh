@@ -71,6 +71,18 @@ struct StrainStressArgs {
     int            red_site;
 };
 cudaError_t launch_strain_stress(const StrainStressArgs &a, cudaStream_t st);
+// Per-phase strain sums and counts for at most 2 phases: out_red[ph*nstr + i],
+// then the two counts at out_red[2*nstr + ph].
+cudaError_t launch_strain_sums(const StrainStressArgs &a, cudaStream_t st);
+
+// ---------------------------------------------- tensor-core CG operator ---
+// FP32 fused d = s + beta d_old, K d and <d, K d> with the element matvecs on
+// tcgen05 (3xTF32); needs ny % 8 == 0, nz % 32 == 0 and at most 2 phases.
+bool        stencil_tc_supported(const Grid3 &g, int C, int nph);
+size_t      stencil_tc_weights(int C, int nph); // floats of the packed W (hi + lo)
+void        stencil_tc_pack_weights(int C, int nph, const float *K32, float *out);
+cudaError_t launch_stencil_tc(const StencilArgs &a, const float *W, int nph, cudaStream_t st);
+long long   stencil_tc_blocks(const Grid3 &g);
 
 // -------------------------------------------------------- element kernels ---
 enum ElemMode { ELEM_RESIDUAL = 0, ELEM_AVERAGES = 1 };
@@ -83,7 +95,7 @@ struct ElementArgs {
     const double  *g0;    // nstr
     const int     *law;   // per phase
     const double  *Cph;   // per phase nstr x nstr (linear laws)
-    const double  *prm;   // per phase {K, G, sigma_y, h} (J2)
+    const double  *prm;   // per phase, 8 law parameters (J2, PseudoPlastic)
     const double  *ep_t, *q_t; // committed internal variables [6][ngp][N], [ngp][N]
     double        *ep, *q;     // trial internal variables (written)
     double         ve;
@@ -92,11 +104,28 @@ struct ElementArgs {
     int            phase_filter;
     double        *strain, *stress; // [N][nstr] or null
     double        *strain_gp, *stress_gp; // [N][ngp][nstr] or null
+    double        *flag;                  // [N] element mean of the Gauss-point plastic flags, or null
+    const double  *scale;                 // [N] per-voxel stiffness scale (sigma *= scale[e]), or null
     double        *out_red;         // [0,nstr) sum eps, [nstr,2nstr) sum sig, [2nstr] count
     GridRed        red;
     int            red_site;
 };
 cudaError_t launch_element(const ElementArgs &a, cudaStream_t st);
+// Sensitivity of sum_ij W_ij C_ij to the per-voxel stiffness scale, C_ij the
+// energy-form effective stiffness of n stored solutions u_k (load g0_k):
+// grad[e] = (1/N) mean_gp sum_ij W_ij eps_i^T C_ph(e) eps_j  (linear laws).
+struct SensArgs {
+    Grid3          g;
+    int            C, nstr, ngp, n;
+    const double  *u;     // n stored solutions, each SoA [C][N]
+    const double  *g0;    // n x nstr
+    const double  *W;     // n x n
+    const uint8_t *ms;
+    const double  *B, *Cph;
+    double        *grad;  // [N]
+};
+cudaError_t launch_sensitivity(const SensArgs &a, cudaStream_t st);
+cudaError_t launch_set_alpha(CgScalars *scal, cudaStream_t st); // alpha = delta / dAd
 cudaError_t launch_gather(const double *rows, double *r, const Grid3 &g, int C, cudaStream_t st);
 cudaError_t launch_dot(const double *a, const double *b, long long n, double *out, GridRed red, int site,
                        cudaStream_t st);

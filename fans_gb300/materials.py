@@ -26,6 +26,18 @@ def _iso_elastic(props, i):
     return [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i])]
 
 
+def _pseudo_lin(props, i):
+    # plastic_flag values: index in the group and group size (PseudoPlastic.h:103-108)
+    return [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i]), float(props["yield_stress"][i]),
+            float(props["hardening_parameter"][i]), float(i), float(len(props["bulk_modulus"]))]
+
+
+def _pseudo_nl(props, i):
+    return [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i]), float(props["yield_stress"][i]),
+            float(props["hardening_exponent"][i]), float(props["eps_0"][i]), float(i),
+            float(len(props["bulk_modulus"]))]
+
+
 def _j2(props, i):
     return [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i]), float(props["yield_stress"][i]),
             float(props["isotropic_hardening_parameter"][i])]
@@ -55,6 +67,8 @@ MODELS = {
     "LinearElasticIsotropic": (C.LAW_ELASTIC_ISO, "mechanical", _iso_elastic),
     "LinearElasticTriclinic": (C.LAW_ELASTIC_TRI, "mechanical", _tri(_TRI_E, 6)),
     "J2PlasticityNew_LinearIsotropicHardening": (C.LAW_J2_LINEAR, "mechanical", _j2),
+    "PseudoPlasticLinearHardening": (C.LAW_PSEUDO_LINEAR, "mechanical", _pseudo_lin),
+    "PseudoPlasticNonLinearHardening": (C.LAW_PSEUDO_NONLINEAR, "mechanical", _pseudo_nl),
 }
 
 
@@ -77,7 +91,8 @@ def group_reference_stiffness(law, params):
         M = np.zeros((6, 6))
         M[:3, :3] = lr
         return M + 2 * mr * np.eye(6)
-    if law == C.LAW_J2_LINEAR:  # J2PlasticityNew.h:111-121 (mean K, G)
+    if law in (C.LAW_J2_LINEAR, C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR):
+        # J2PlasticityNew.h:111-121, PseudoPlastic.h:41-51 (mean K, G)
         Kb, Gb = np.mean([p[0] for p in params]), np.mean([p[1] for p in params])
         M = np.zeros((6, 6))
         M[:3, :3] = Kb - 2.0 * Gb / 3.0
@@ -127,7 +142,7 @@ class MaterialManager:
                 self.law[ph] = law
                 self.params[ph] = prm
                 gparams.append(prm)
-            if law == C.LAW_J2_LINEAR:
+            if law in (C.LAW_J2_LINEAR, C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR):
                 self.all_linear = False
             self.groups.append((name, law, list(mg["phases"]), gparams))
             refs.append(group_reference_stiffness(law, gparams))

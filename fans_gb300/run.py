@@ -116,6 +116,12 @@ def postprocess(solver, reader: Reader, results: ResultsFile, load_idx: int, tim
             results.writeSlab("isotropic_hardening_variable_gp", load_idx, time_idx,
                               ctx.get_field(C.FIELD_HARDENING_GP), (ctx.n_gp,))
 
+    # PseudoPlastic::postprocess (PseudoPlastic.h:55-63): element mean of the plastic flags, float32
+    if want("plastic_flag") and any(law in (C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR)
+                                    for law in solver.matmanager.law):
+        results.writeSlab("plastic_flag", load_idx, time_idx,
+                          ctx.get_field(C.FIELD_PLASTIC_FLAG).astype(np.float32), (1,))
+
     if want("homogenized_tangent"):
         T = solver.get_homogenized_tangent(1e-6)
         log("# Homogenized tangent: \n" + np.array2string(T, precision=12) + "\n")
@@ -130,15 +136,16 @@ def run_solver(reader: Reader, results: ResultsFile, precision="fp64", log=print
         reader.ReadMS()
     out = []
     for li, lc in enumerate(reader.load_cases):
-        if lc.mixed:
-            raise NotImplementedError("mixed stress/strain boundary conditions are not in this build")
         mm = MaterialManager(reader.inputJson, reader.problemType)
         solver = create_solver(reader, mm, precision)
         try:
             log(f"# Load case {li + 1}/{len(reader.load_cases)}: {lc.n_steps} time steps")
             for ti in range(lc.n_steps):
                 log(f"#   Time step {ti + 1}/{lc.n_steps} (load case {li + 1}/{len(reader.load_cases)})")
-                solver.set_gradient(lc.g0_path[ti])
+                if lc.mixed:  # main.cpp:29-34
+                    solver.enableMixedBC(lc.mbc, ti)
+                else:
+                    solver.set_gradient(lc.g0_path[ti])
                 st = solver.solve()
                 avg = postprocess(solver, reader, results, li, ti, log)
                 out.append(dict(load=li, step=ti, iterations=st["iterations"], stress=avg["stress_average"].copy(),

@@ -120,7 +120,7 @@ class Context:
             shape = (self.howmany,)
         elif which == C.FIELD_PLASTIC_STRAIN:
             shape = (6,)
-        elif which == C.FIELD_HARDENING:
+        elif which in (C.FIELD_HARDENING, C.FIELD_PLASTIC_FLAG):
             shape = (1,)
         elif which in (C.FIELD_STRAIN_GP, C.FIELD_STRESS_GP):
             shape = (self.n_gp, self.n_str)
@@ -174,6 +174,42 @@ class Context:
         self._chk(self.lib.fansgpu_kernel_times(self.ctx, _ptr(ms), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                                 n))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(C.KERNEL_NAMES)}
+
+    def enable_mixed_bc(self, idx_e, strain_e, idx_f, stress_f, step):
+        """MixedBCController::activate (mixedBCs.h:180-226) for one time step."""
+        ie = np.ascontiguousarray(idx_e, dtype=np.int32)
+        jf = np.ascontiguousarray(idx_f, dtype=np.int32)
+        se = np.ascontiguousarray(strain_e, dtype=float)
+        sf = np.ascontiguousarray(stress_f, dtype=float)
+        i32 = ctypes.POINTER(ctypes.c_int32)
+        self._chk(self.lib.fansgpu_enable_mixed_bc(self.ctx, len(ie), ie.ctypes.data_as(i32), _ptr(se), len(jf),
+                                                   jf.ctypes.data_as(i32), _ptr(sf), int(step)))
+
+    def disable_mixed_bc(self):
+        self._chk(self.lib.fansgpu_disable_mixed_bc(self.ctx))
+
+    def gradient(self):
+        g = np.zeros(self.n_str)
+        self._chk(self.lib.fansgpu_get_gradient(self.ctx, _ptr(g)))
+        return g
+
+    def set_voxel_scale(self, scale):
+        """Per-voxel stiffness scale s(x) ([x][y][z]); None clears it."""
+        if scale is None:
+            self._chk(self.lib.fansgpu_set_voxel_field(self.ctx, C.VOXEL_STIFFNESS_SCALE, None))
+            return
+        a = np.ascontiguousarray(scale, dtype=float)
+        assert a.shape == self.n
+        self._chk(self.lib.fansgpu_set_voxel_field(self.ctx, C.VOXEL_STIFFNESS_SCALE, _ptr(a)))
+
+    def store_solution(self, slot):
+        self._chk(self.lib.fansgpu_store_solution(self.ctx, int(slot)))
+
+    def stiffness_gradient(self, W):
+        W = np.ascontiguousarray(W, dtype=float)
+        out = np.zeros(self.n)
+        self._chk(self.lib.fansgpu_stiffness_gradient(self.ctx, W.shape[0], _ptr(W), _ptr(out)))
+        return out
 
     def commit_state(self):
         self._chk(self.lib.fansgpu_commit_state(self.ctx))
@@ -261,6 +297,13 @@ class Solver:
 
     def extrapolateDisplacement(self):
         self.ctx.extrapolate_displacement()
+
+    def enableMixedBC(self, mbc, step):
+        """Solver::enableMixedBC (solver.h:71-74) with a reader.MixedBC."""
+        self.ctx.enable_mixed_bc(mbc.idx_E, mbc.F_E_path[step], mbc.idx_F, mbc.P_F_path[step], step)
+
+    def disableMixedBC(self):
+        self.ctx.disable_mixed_bc()
 
     def close(self):
         self.ctx.close()

@@ -47,12 +47,19 @@ extern "C" {
  *   ELASTIC_ISO  {bulk_modulus, shear_modulus}                    LinearElastic.h:7-75
  *   J2_LINEAR    {bulk, shear, yield_stress, isotropic_hardening} J2PlasticityNew.h:7-152
  *   THERMAL_TRI  {K (3x3 row-major)}                              LinearThermal.h:52-118
- *   ELASTIC_TRI  {C (6x6 row-major, Mandel)}                      LinearElastic.h:77-159 */
+ *   ELASTIC_TRI  {C (6x6 row-major, Mandel)}                      LinearElastic.h:77-159
+ *   PSEUDO_LINEAR    {bulk, shear, yield_stress, hardening_parameter
+ *                     [, index in its material group, phases in the group]}  PseudoPlastic.h:80-122
+ *   PSEUDO_NONLINEAR {bulk, shear, yield_stress, hardening_exponent, eps_0
+ *                     [, index in its material group, phases in the group]}  PseudoPlastic.h:124-167
+ *   (the optional pair sets the plastic_flag values, mat_index / n_mat + mat_index) */
 #define FANSGPU_LAW_THERMAL_ISO 0
 #define FANSGPU_LAW_ELASTIC_ISO 1
 #define FANSGPU_LAW_J2_LINEAR 2
 #define FANSGPU_LAW_THERMAL_TRI 3
 #define FANSGPU_LAW_ELASTIC_TRI 4
+#define FANSGPU_LAW_PSEUDO_LINEAR 5
+#define FANSGPU_LAW_PSEUDO_NONLINEAR 6
 
 /* precision of the solve */
 #define FANSGPU_FP64 0  /* all FP64: parity path against the FP64 reference */
@@ -81,6 +88,7 @@ extern "C" {
 #define FANSGPU_FIELD_STRESS_GP 8          /* stress at every Gauss point, [x][y][z][n_gp][n_str] (get_field only) */
 #define FANSGPU_FIELD_PLASTIC_STRAIN_GP 9  /* J2: committed eps_p, [x][y][z][n_gp][6] (get_field only) */
 #define FANSGPU_FIELD_HARDENING_GP 10      /* J2: committed q, [x][y][z][n_gp] (get_field only) */
+#define FANSGPU_FIELD_PLASTIC_FLAG 11      /* PseudoPlastic: Gauss-point mean of the plastic flag, [x][y][z] */
 
 typedef struct fansgpu_ctx fansgpu_ctx;
 
@@ -143,6 +151,40 @@ int fansgpu_set_reference(fansgpu_ctx *ctx, const double *kapparef);
 /* MaterialManager::set_gradient / Matmodel::setGradient (MaterialManager.h:216-221,
  * matmodel.h:228-236): macroscopic gradient g0 (n_str). */
 int fansgpu_set_gradient(fansgpu_ctx *ctx, const double *g0);
+
+/* MixedBCController (mixedBCs.h:149-227, solver.h:71-85): activate mixed
+ * stress/strain control for time step `step` of a mixed load case.  idx_e are
+ * the strain-controlled Mandel components with this step's values strain_e,
+ * idx_f the stress-controlled ones with target stresses stress_f; together they
+ * cover each component once.  Step 0 starts from g0 = 0; later steps
+ * extrapolate the stress-controlled components linearly.  While active, the CG
+ * solve takes the line-search branch (solverCG.h:96) and updates g0 before
+ * every residual (solverCG.h:131, :152; solverFP.h:47).  Needs set_reference. */
+int fansgpu_enable_mixed_bc(fansgpu_ctx *ctx, int32_t n_e, const int32_t *idx_e, const double *strain_e, int32_t n_f,
+                            const int32_t *idx_f, const double *stress_f, int32_t step);
+/* Per-voxel material field (new on the GPU path; FANS has one law per phase):
+ * FANSGPU_VOXEL_STIFFNESS_SCALE multiplies the stress of voxel element e by
+ * values[e] > 0 ([x][y][z] doubles), i.e. K_e = s_e K_phase for linear laws --
+ * E(x) = s(x) E_phase at fixed Poisson ratio.  NULL clears it.  With a scale
+ * set, solves run the FP64 path with the element kernel as operator. */
+#define FANSGPU_VOXEL_STIFFNESS_SCALE 0
+int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *values);
+
+/* Adjoint of the homogenized stiffness w.r.t. the per-voxel scale.  After
+ * solves with g0 = e_k, fansgpu_store_solution(ctx, k) keeps v_u and g0 (slots
+ * 0..5).  fansgpu_stiffness_gradient returns grad[e] = d(sum_ij W_ij C_ij)/d s_e
+ * for the energy-form C_ij = (1/N) sum_e s_e mean_gp eps_i^T C_ph eps_j of the
+ * stored solutions (equal to <sigma_j>_i at equilibrium; no adjoint solve is
+ * needed because the displacement fields are stationary).  W is n x n
+ * row-major; grad holds n_x*n_y*n_z doubles [x][y][z].  Linear laws only. */
+int fansgpu_store_solution(fansgpu_ctx *ctx, int32_t slot);
+int fansgpu_stiffness_gradient(fansgpu_ctx *ctx, int32_t n, const double *W, double *grad);
+
+/* Solver::disableMixedBC (solver.h:75-78). */
+int fansgpu_disable_mixed_bc(fansgpu_ctx *ctx);
+/* The current macroscale gradient g0 (n_str values; under mixed BCs the
+ * controller's current strain). */
+int fansgpu_get_gradient(fansgpu_ctx *ctx, double *g0);
 
 /* Reader error_parameters / n_it / linesearch_parameters (reader.cpp:94-105). */
 int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *tol);

@@ -44,7 +44,8 @@
 #define FO_API __attribute__((visibility("default")))
 
 enum { FO_HEX8 = 0, FO_HEX8R = 1, FO_BBAR = 2 };
-enum { FO_LAW_THERMAL_ISO = 0, FO_LAW_ELASTIC_ISO = 1, FO_LAW_J2 = 2, FO_LAW_THERMAL_TRI = 3, FO_LAW_ELASTIC_TRI = 4 };
+enum { FO_LAW_THERMAL_ISO = 0, FO_LAW_ELASTIC_ISO = 1, FO_LAW_J2 = 2, FO_LAW_THERMAL_TRI = 3, FO_LAW_ELASTIC_TRI = 4,
+       FO_LAW_PSEUDO_LIN = 5, FO_LAW_PSEUDO_NL = 6 };
 enum { FO_L1 = 0, FO_L2 = 1, FO_LINF = 2 };
 enum { FO_ABS = 0, FO_REL = 1 };
 
@@ -596,6 +597,34 @@ static void law_sigma(const fo_problem *P, int phase, size_t elem, int gp, const
                 acc += pr[i * n + k] * eps[k];
             sig[i] = acc;
         }
+        break;
+    }
+    case FO_LAW_PSEUDO_LIN:
+    case FO_LAW_PSEUDO_NL: {
+        /* PseudoPlasticLinearHardening::get_sigma (PseudoPlastic.h:92-115), param = {K, G, sigma_y, h};
+         * PseudoPlasticNonLinearHardening::get_sigma (PseudoPlastic.h:138-160), param = {K, G, sigma_y, n, eps_0} */
+        const double Kb = pr[0], G = pr[1], sy = pr[2];
+        double treps = eps[0] + eps[1] + eps[2], dev[6], nrm = 0.0, buf2;
+        for (int i = 0; i < 3; ++i)
+            dev[i] = eps[i] - (1.0 / 3.0) * treps;
+        for (int i = 3; i < 6; ++i)
+            dev[i] = eps[i];
+        for (int i = 0; i < 6; ++i)
+            nrm += dev[i] * dev[i];
+        nrm = sqrt(nrm);
+        const double buf1 = Kb * treps;
+        if (P->law[phase] == FO_LAW_PSEUDO_LIN) {
+            const double h = pr[3], ec = sqrt(2. / 3.) * sy / (2. * G), Es = (3. * G) / (3. * G + h);
+            buf2 = nrm <= ec ? 2.0 * G : (sqrt(2. / 3.) * sy + (2. / 3.) * Es * h * (nrm - ec)) / nrm;
+        } else {
+            const double n = pr[3], e0 = pr[4], ec = e0 * pow(sy / (3.0 * G * e0), 1.0 / (1.0 - n));
+            const double eq = sqrt(2.0 / 3.0) * nrm;
+            buf2 = eq <= ec ? 2.0 * G : sqrt(2.0 / 3.0) * sy * pow(eq / e0, n) / nrm;
+        }
+        for (int i = 0; i < 3; ++i)
+            sig[i] = buf1 + buf2 * dev[i];
+        for (int i = 3; i < 6; ++i)
+            sig[i] = buf2 * dev[i];
         break;
     }
     case FO_LAW_J2: {

@@ -28,6 +28,8 @@ LIB_PATH = os.path.join(HERE, "libfans_oracle.so")
 HEX8, HEX8R, BBAR = 0, 1, 2
 FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
 LAW_THERMAL_ISO, LAW_ELASTIC_ISO, LAW_J2, LAW_THERMAL_TRI, LAW_ELASTIC_TRI = 0, 1, 2, 3, 4
+LAW_PSEUDO_LIN, LAW_PSEUDO_NL = 5, 6
+NONLINEAR_LAWS = (LAW_J2, LAW_PSEUDO_LIN, LAW_PSEUDO_NL)
 L1, L2, LINF = 0, 1, 2
 ABS, REL = 0, 1
 MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}
@@ -109,7 +111,7 @@ def iso_elastic_C(K, G):
 def law_C(law, params):
     if law == LAW_THERMAL_ISO:
         return params[0] * np.eye(3)
-    if law in (LAW_ELASTIC_ISO, LAW_J2):
+    if law in (LAW_ELASTIC_ISO,) + NONLINEAR_LAWS:
         return iso_elastic_C(params[0], params[1])
     if law == LAW_THERMAL_TRI:
         return np.asarray(params[:9], dtype=float).reshape(3, 3)
@@ -137,7 +139,7 @@ def model_reference_stiffness(law, phase_params):
         C[:3, :3] = lr
         C += 2 * mr * np.eye(6)
         return C
-    if law == LAW_J2:
+    if law in NONLINEAR_LAWS:  # J2PlasticityNew.h:111-121, PseudoPlastic.h:41-51
         Kb = np.mean([p[0] for p in pp])
         Gb = np.mean([p[1] for p in pp])
         C = np.zeros((6, 6))
@@ -176,7 +178,7 @@ class OracleProblem:
                 self.law[ph] = law
                 pr = np.asarray(pr, dtype=float).ravel()
                 self.param[ph, : pr.size] = pr
-            if law == LAW_J2:
+            if law in NONLINEAR_LAWS:
                 self.linear = False
             refs.append(model_reference_stiffness(law, params))
         # MaterialManager::compute_reference_stiffness (MaterialManager.h:177-205)
@@ -251,8 +253,117 @@ class OracleProblem:
     def homogenized_stress(self):
         return self.strain_stress()["stress_average"]
 
+    # -- mixed stress/strain boundary conditions (mixedBCs.h:149-227) ----------
+    mixed_active = False
+
+    def enable_mixed_bc(self, idx_E, strain_E, idx_F, stress_F, step):
+        """MixedBCController::activate (mixedBCs.h:180-226) with MixedBC::finalize
+        (mixedBCs.h:30-48): M = pinv(Q_F^T C0 Q_F); step 0 starts from g0 = 0, later
+        steps extrapolate the stress-controlled components; then one update."""
+        self.idx_E, self.idx_F = list(idx_E), list(idx_F)
+        self.mbc_PF = np.asarray(stress_F, dtype=float)
+        C0 = np.asarray(self.kapparef, dtype=float)
+        self.mbc_M = np.linalg.pinv(C0[np.ix_(self.idx_F, self.idx_F)]) if self.idx_F else np.zeros((0, 0))
+        g0 = np.asarray(self.g0, dtype=float).copy()
+        if step == 0:
+            g0 = np.zeros(self.nstr)
+            self.g0_prev = g0.copy()
+        else:
+            delta = g0 - self.g0_prev
+            self.g0_prev = g0.copy()
+            g0[self.idx_F] += delta[self.idx_F]
+        g0[self.idx_E] = np.asarray(strain_E, dtype=float)
+        self.g0 = g0
+        self.mixed_active = True
+        self._mixed_update()
+
+    def disable_mixed_bc(self):
+        self.mixed_active = False
+
+    def _mixed_update(self):
+        """MixedBCController::update (mixedBCs.h:160-177)."""
+        if not self.mixed_active or not self.idx_F:
+            return
+        Pbar = self.strain_stress()["stress_average"]
+        g0 = self.g0.copy()
+        g0[self.idx_F] += self.mbc_M @ (self.mbc_PF - Pbar[self.idx_F])
+        self.g0 = g0
+
+    def _solve_mixed(self, method, measure, type, tol, n_it, ls_max_iter, ls_tol):
+        """SolverCG::internalSolve with mixed BCs active: the line-search branch
+        (solverCG.h:96-105, LineSearchSecant :120-160) with an update before every
+        residual (:131, :152); SolverFP likewise (solverFP.h:44-48).  Vector algebra
+        in numpy; residual, convolution and averages from the C oracle."""
+        m = MEASURES[measure]
+
+        def norm(r):
+            return np.abs(r).sum() if m == 0 else (np.sqrt((r * r).sum()) if m == 1 else np.abs(r).max())
+
+        err_all = []
+
+        def err(it, r):
+            e = norm(r)
+            err_all.append(e)
+            if type == "absolute":
+                return e
+            return 100.0 if it == 0 else e / err_all[0]
+
+        u = self.u
+        r = self.residual(u)
+        it = 0
+        err_rel = err(0, r)
+        if method == "fp":
+            while it < n_it and err_rel > tol:
+                u -= self.convolve(r)
+                self._mixed_update()
+                r = self.residual(u)
+                it += 1
+                err_rel = err(it, r)
+        else:
+            s = np.zeros_like(u)
+            d = np.zeros_like(u)
+            delta, alpha_warm = 1.0, 0.1
+            while it < n_it and err_rel > tol:
+                deltamid = float((r * s).sum())
+                s = -self.convolve(r)
+                delta0, delta = delta, float((r * s).sum())
+                d = s + max(0.0, (delta - deltamid) / delta0) * d
+                e_ls, k, a_prev, a_cur = 10.0, 0, 0.0, alpha_warm
+                rpd = float((r * d).sum())
+                u += d * a_cur
+                self._mixed_update()
+                rnew = self.residual(u)
+                r1pd = float((rnew * d).sum())
+                while k < ls_max_iter and e_ls > ls_tol:
+                    denom = r1pd - rpd
+                    if abs(denom) < 1e-14 * (abs(r1pd) + abs(rpd)):
+                        break
+                    a_next = a_cur - r1pd * (a_cur - a_prev) / denom
+                    if a_next <= 0.0:
+                        a_next = 0.5 * (a_prev + a_cur)
+                    e_ls = abs(a_next - a_cur)
+                    u += d * (a_next - a_cur)
+                    a_prev, rpd, a_cur = a_cur, r1pd, a_next
+                    k += 1
+                    self._mixed_update()
+                    rnew = self.residual(u)
+                    r1pd = float((rnew * d).sum())
+                alpha_warm = 0.1 if (k == ls_max_iter and e_ls > ls_tol) else a_cur
+                r = rnew
+                it += 1
+                err_rel = err(it, r)
+        self.r = r
+        self.err_all = np.array(err_all)
+        self.iterations = it
+        if not self.linear:
+            self.ep_t[...] = self.ep
+            self.q_t[...] = self.q
+        return it
+
     def solve(self, method="cg", measure="L2", type="relative", tol=1e-10, n_it=100, ls_max_iter=5, ls_tol=1e-2):
         """Solver::solve (solver.h:283-300): internalSolve then commit internal variables."""
+        if self.mixed_active:
+            return self._solve_mixed(method, measure, type, tol, n_it, ls_max_iter, ls_tol)
         r = np.zeros_like(self.u)
         err = np.zeros(n_it + 1)
         m, t = MEASURES[measure], TYPES[type]

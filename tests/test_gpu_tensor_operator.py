@@ -1,0 +1,67 @@
+"""The tensor-core CG operator (tcgen05 kind::tf32, 3xTF32 split) against the
+CUDA-core FP32 operator and the FP64 oracle.
+
+Mixed-precision solves are run twice on the same context settings, once with
+the tensor-core operator (default where the grid allows it: n_y % 8 == 0,
+n_z % 32 == 0, at most two phases) and once with FANSGPU_STENCIL=simt, which
+selects the CUDA-core operator at context creation.  Both are FP32-accurate
+operators inside the same reliable-update CG, so they take the same number of
+iterations (within 1) and give the same solution to the accuracy the FP64
+refreshes pin (1e-9 relative on the stress average); both meet the oracle's
+C_eff to 1e-6, the bar of the mixed-precision parity test."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import ELASTIC, THERMAL, gpu_context, oracle_problem, random_ms, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(P, g0, simt):
+    old = os.environ.get("FANSGPU_STENCIL")
+    os.environ["FANSGPU_STENCIL"] = "simt" if simt else "tc"
+    try:
+        ctx = gpu_context(P, precision="mixed")
+    finally:
+        if old is None:
+            del os.environ["FANSGPU_STENCIL"]
+        else:
+            os.environ["FANSGPU_STENCIL"] = old
+    ctx.set_tolerance("L2", "relative", 1e-8, 500)
+    ctx.set_gradient(g0)
+    ctx.set_timing(True)
+    st = ctx.solve()
+    out = dict(st=st, stress=ctx.homogenized_stress(), u=ctx.get_field(0), times=ctx.kernel_times())
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("c,groups,shape", [(3, ELASTIC, (32, 32, 32)), (3, ELASTIC, (16, 8, 64)),
+                                            (1, THERMAL, (32, 16, 32)), (3, ELASTIC, (20, 24, 32))])
+def test_tensor_operator_matches_cuda_core_operator(c, groups, shape):
+    ms = random_ms(shape, vf=0.3, seed=21)
+    P = oracle_problem(ms, c, groups, "HEX8")
+    g0 = np.linspace(1.0, 0.4, P.nstr)
+    a = _solve(P, g0, simt=False)
+    b = _solve(P, g0, simt=True)
+    assert a["st"]["converged"] and b["st"]["converged"]
+    assert abs(a["st"]["iterations"] - b["st"]["iterations"]) <= 1
+    assert rel(a["stress"], b["stress"]) < 1e-9
+    assert rel(a["u"], b["u"]) < 1e-6
+    P.set_gradient(g0)
+    P.solve(measure="L2", type="relative", tol=1e-8, n_it=500)
+    assert rel(a["stress"], P.homogenized_stress()) < 1e-7
+
+
+def test_tensor_operator_single_phase_and_hex8r():
+    ms = np.zeros((16, 16, 32), dtype=np.uint16)
+    ms[4:9, 3:12, 10:20] = 1
+    for fe in ("HEX8R", "BBAR"):
+        P = oracle_problem(ms, 3, ELASTIC, fe)
+        g0 = np.array([0.3, -0.1, 0.2, 0.05, 0.0, 0.1])
+        a = _solve(P, g0, simt=False)
+        b = _solve(P, g0, simt=True)
+        assert abs(a["st"]["iterations"] - b["st"]["iterations"]) <= 1
+        assert rel(a["stress"], b["stress"]) < 1e-9

@@ -144,3 +144,10 @@ def test_cli_usage_and_bad_input(tmp_path, capsys):
     bad.write_text("{}")
     assert main([str(bad), str(tmp_path / "o.h5")]) == 10
     assert "ERROR trying to read input file" in capsys.readouterr().err
+
+
+def test_pyfans_cmat_packing_is_the_upper_triangle_row_by_row():
+    from fans_gb300.pyfans import CMAT_ENTRIES
+
+    assert len(CMAT_ENTRIES) == 21 and len(set(CMAT_ENTRIES)) == 21
+    assert CMAT_ENTRIES == [(r, c) for r in range(6) for c in range(r, 6)]
