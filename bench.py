@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU path")
     ap.add_argument("--cpu-iters", type=int, default=2)
+    ap.add_argument("--workload", default="headline", choices=["headline", "batch64"],
+                    help="batch64: 64 independent micro problems, sequential vs fansgpu_solve_batch (own JSON line)")
     return ap.parse_args()
 
 
@@ -271,10 +273,82 @@ def run_reference(args):
     return 0
 
 
+def run_batch64(args):
+    """The batched workload: 64 instances (edges 32..96, thermal 3 RHS / elastic 6
+    RHS, mixed precision, rel. L2 tol).  Times all 288 solves one after another and
+    as six fansgpu_solve_batch calls (one per load-case index), contexts created
+    and Green's tables built beforehand."""
+    import torch
+
+    from fans_gb300 import Context, solve_batch
+    from fans_gb300.microstructure import batch_workload
+
+    torch.cuda.set_device(0)
+    work = batch_workload(64)
+    ctxs = []
+    for w in work:
+        n = w["n"]
+        if w["thermal"]:
+            c = Context((n, n, n), (1.0, 1.0, 1.0), 1, "HEX8", "mixed", "cg")
+            c.set_microstructure(w["ms"])
+            c.set_phase_material(0, 0, [1.0])
+            c.set_phase_material(1, 0, [10.0])
+            c.set_reference(5.5 * np.eye(3))
+        else:
+            c = Context((n, n, n), (1.0, 1.0, 1.0), 3, "HEX8", "mixed", "cg")
+            c.set_microstructure(w["ms"])
+            for ph in range(2):
+                c.set_phase_material(ph, 1, MAT[ph])
+            c.set_reference(kapparef())
+        c.set_tolerance("L2", "relative", args.tol, 2000)
+        ctxs.append(c)
+
+    def prepare(c, l):
+        c.reset()
+        g = np.zeros(c.n_str)
+        g[l] = 1.0
+        c.set_gradient(g)
+
+    for c in ctxs:  # warm-up: tables, Green's operator, graphs
+        prepare(c, 0)
+        c.solve()
+    stress_seq, t0 = [], time.perf_counter()
+    for c in ctxs:
+        for l in range(c.n_str):
+            prepare(c, l)
+            c.solve()
+            stress_seq.append(c.homogenized_stress())
+    seq_ms = (time.perf_counter() - t0) * 1e3
+    stress_bat, t0 = {}, time.perf_counter()
+    for l in range(6):
+        group = [c for c in ctxs if l < c.n_str]
+        for c in group:
+            prepare(c, l)
+        sts = solve_batch(group)
+        assert all(st["converged"] for st in sts)
+        for c in group:
+            stress_bat[(id(c), l)] = c.homogenized_stress()
+    bat_ms = (time.perf_counter() - t0) * 1e3
+    diff = max(float(np.abs(stress_bat[(id(c), l)] - s_).max())
+               for (c, l), s_ in zip([(c, l) for c in ctxs for l in range(c.n_str)], stress_seq))
+    voxel_rhs = sum(w["n"] ** 3 * (3 if w["thermal"] else 6) for w in work)
+    print(json.dumps({"workload": "batch64: 64 micro problems (edges 32-96; thermal 3 RHS / elastic 6 RHS), "
+                                  f"mixed precision, rel L2 {args.tol}",
+                      "solves": sum(c.n_str for c in ctxs), "voxel_rhs": voxel_rhs,
+                      "sequential_ms": round(seq_ms, 1), "batched_ms": round(bat_ms, 1),
+                      "speedup": round(seq_ms / bat_ms, 2), "max_stress_diff_batched_vs_sequential": diff,
+                      "graphs": os.environ.get("FANSGPU_GRAPHS", "1") != "0"}))
+    for c in ctxs:
+        c.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch64":
+        return run_batch64(args)
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -3,6 +3,6 @@ elements, hand-written sm_103a CUDA behind the C ABI in include/fans_gb300.h."""
 from . import _lib
 from ._lib import FansGpuError
 from .materials import MaterialManager
-from .solver import Context, Solver, SolverCG, SolverFP, create_solver
+from .solver import Context, Solver, SolverCG, SolverFP, create_solver, solve_batch
 
-__all__ = ["Context", "Solver", "SolverCG", "SolverFP", "create_solver", "MaterialManager", "FansGpuError", "_lib"]
+__all__ = ["solve_batch", "Context", "Solver", "SolverCG", "SolverFP", "create_solver", "MaterialManager", "FansGpuError", "_lib"]

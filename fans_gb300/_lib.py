@@ -40,7 +40,7 @@ EXPORTS = [
     "fansgpu_green_table", "fansgpu_version", "fansgpu_reset", "fansgpu_get_stream", "fansgpu_set_timing",
     "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc", "fansgpu_set_refresh",
     "fansgpu_enable_mixed_bc", "fansgpu_disable_mixed_bc", "fansgpu_get_gradient", "fansgpu_set_voxel_field",
-    "fansgpu_store_solution", "fansgpu_stiffness_gradient",
+    "fansgpu_store_solution", "fansgpu_stiffness_gradient", "fansgpu_solve_batch",
 ]
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
                 "residual64", "norm", "green_table", "strain_stress"]
@@ -125,6 +125,7 @@ def _declare(L):
     L.fansgpu_set_voxel_field.argtypes = [vp, ip, dp]
     L.fansgpu_store_solution.argtypes = [vp, ip]
     L.fansgpu_stiffness_gradient.argtypes = [vp, ip, dp, dp]
+    L.fansgpu_solve_batch.argtypes = [ctypes.POINTER(vp), ip, ctypes.POINTER(Stats), i32p]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

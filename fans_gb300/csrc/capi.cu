@@ -14,6 +14,8 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <thread>
+#include <atomic>
 
 using namespace fansgpu;
 
@@ -100,6 +102,11 @@ struct fansgpu_ctx {
     // tensor-core CG operator (mixed path): packed per-phase stiffness, hi/lo tf32 split
     float *Wtc    = nullptr;
     bool   use_tc = false;
+
+    // CUDA graphs of one mixed CG iteration (one per d ping-pong parity)
+    bool            use_graphs   = true;
+    bool            graphs_valid = false;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     bool   tc_allowed = true; // FANSGPU_STENCIL=simt at create time selects the CUDA-core operator
 };
 
@@ -386,6 +393,7 @@ int setup(fansgpu_ctx *ctx)
         ctx->K64h = K64;
         ctx->K32h = K32;
         ctx->use_tc = false;
+        ctx->graphs_valid = false;
         if (ctx->tc_allowed && ctx->desc.precision == FANSGPU_MIXED && stencil_tc_supported(ctx->g, C, ctx->nph)) {
             std::vector<float> w(stencil_tc_weights(C, ctx->nph));
             stencil_tc_pack_weights(C, ctx->nph, K32.data(), w.data());
@@ -674,6 +682,44 @@ int solve_cg64(fansgpu_ctx *ctx)
     return 0;
 }
 
+// One inner iteration of the mixed CG on the context stream: s = -G*r with
+// delta/beta, d = s + beta d_old with K d and alpha, then the FP32 update.
+cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
+{
+    const long long n = ctx->n;
+    ConvArgs        ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+    cudaError_t     e = run_conv<float>(ctx, ctx->cp32, ca);
+    if (e != cudaSuccess)
+        return e;
+    StencilArgs sa{};
+    sa.g        = ctx->g;
+    sa.C        = ctx->C;
+    sa.x        = ctx->s32;
+    sa.d_old    = ctx->d32[cd];
+    sa.d_new    = ctx->d32[cd ^ 1];
+    sa.y        = ctx->Kd32;
+    sa.ms       = ctx->d_ms;
+    sa.Kph      = ctx->K32;
+    sa.Kph_host = ctx->K32h.data();
+    sa.nph      = ctx->nph;
+    sa.fuse_d   = 1;
+    sa.reduce   = 1;
+    sa.scal     = ctx->scal;
+    sa.red      = ctx->red;
+    sa.red_site = SITE_STENCIL;
+    int e0      = tk_mark(ctx);
+    e           = ctx->use_tc ? launch_stencil_tc(sa, ctx->Wtc, ctx->nph, ctx->st) : launch_stencil<float>(sa, ctx->st);
+    if (e != cudaSuccess)
+        return e;
+    tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
+    UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->e32, ctx->d32[cd ^ 1], ctx->s32, ctx->tol.measure, 1, ctx->scal,
+                  ctx->red, SITE_UPDATE};
+    int e2 = tk_mark(ctx);
+    e      = launch_cg_update<float, float>(ua, ctx->st);
+    tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
+    return e;
+}
+
 // Mixed precision: FANS's flexible CG run on FP32 fields (stencil, FFT
 // preconditioner, recursive residual) with FP64 dot products, an FP64
 // solution and reliable updates -- the true residual R(u) recomputed in FP64
@@ -703,36 +749,35 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     double err_rel    = err_value(ctx, ctx->scal_h->err);
     double last_true  = ctx->scal_h->err;
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
-        ConvArgs ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
-        FANS_CUDA_CHECK(run_conv<float>(ctx, ctx->cp32, ca));
-        StencilArgs sa{};
-        sa.g        = ctx->g;
-        sa.C        = ctx->C;
-        sa.x        = ctx->s32;
-        sa.d_old    = ctx->d32[ctx->cur_d];
-        sa.d_new    = ctx->d32[ctx->cur_d ^ 1];
-        sa.y        = ctx->Kd32;
-        sa.ms       = ctx->d_ms;
-        sa.Kph      = ctx->K32;
-        sa.Kph_host = ctx->K32h.data();
-        sa.nph      = ctx->nph;
-        sa.fuse_d   = 1;
-        sa.reduce   = 1;
-        sa.scal     = ctx->scal;
-        sa.red      = ctx->red;
-        sa.red_site = SITE_STENCIL;
-        int e0 = tk_mark(ctx);
-        if (ctx->use_tc)
-            FANS_CUDA_CHECK(launch_stencil_tc(sa, ctx->Wtc, ctx->nph, ctx->st));
-        else
-            FANS_CUDA_CHECK(launch_stencil<float>(sa, ctx->st));
-        tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
+        if (ctx->use_graphs && !ctx->timing && ctx->iter > 0) { // the first iteration runs uncaptured
+            // one CUDA graph per d ping-pong parity holds the iteration's 7 launches
+            if (!ctx->graphs_valid) {
+                for (int k = 0; k < 2; ++k) {
+                    if (ctx->graph_exec[k])
+                        cudaGraphExecDestroy(ctx->graph_exec[k]);
+                    ctx->graph_exec[k] = nullptr;
+                    cudaGraph_t g      = nullptr;
+                    FANS_CUDA_CHECK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+                    const cudaError_t ce = enqueue_mixed_iteration(ctx, k);
+                    const cudaError_t ee = cudaStreamEndCapture(ctx->st, &g);
+                    if (ce != cudaSuccess || ee != cudaSuccess) {
+                        if (g)
+                            cudaGraphDestroy(g);
+                        return fail(ctx, FANSGPU_ECUDA, "iteration graph capture: %s",
+                                    cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+                    }
+                    const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec[k], g, 0);
+                    cudaGraphDestroy(g);
+                    if (ie != cudaSuccess)
+                        return fail(ctx, FANSGPU_ECUDA, "iteration graph instantiate: %s", cudaGetErrorString(ie));
+                }
+                ctx->graphs_valid = true;
+            }
+            FANS_CUDA_CHECK(cudaGraphLaunch(ctx->graph_exec[ctx->cur_d], ctx->st));
+        } else {
+            FANS_CUDA_CHECK(enqueue_mixed_iteration(ctx, ctx->cur_d));
+        }
         ctx->cur_d ^= 1;
-        UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->e32, ctx->d32[ctx->cur_d], ctx->s32, ctx->tol.measure, 1, ctx->scal,
-                      ctx->red, SITE_UPDATE};
-        int e2 = tk_mark(ctx);
-        FANS_CUDA_CHECK((launch_cg_update<float, float>(ua, ctx->st)));
-        tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
         if ((rc = sync_scalars(ctx)))
             return rc;
         ctx->iter++;
@@ -1075,6 +1120,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     ctx->desc        = *desc;
     if (const char *ev = std::getenv("FANSGPU_STENCIL"))
         ctx->tc_allowed = std::strcmp(ev, "simt") != 0;
+    if (const char *ev = std::getenv("FANSGPU_GRAPHS"))
+        ctx->use_graphs = std::strcmp(ev, "0") != 0;
     ctx->g           = Grid3{n[0], n[1], n[2]};
     ctx->C           = desc->howmany;
     ctx->nstr        = nstr_of(ctx->C);
@@ -1201,6 +1248,9 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
         cudaEventDestroy(ctx->ev1);
     for (auto e : ctx->tpool)
         cudaEventDestroy(e);
+    for (auto g : ctx->graph_exec)
+        if (g)
+            cudaGraphExecDestroy(g);
     if (ctx->st)
         cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1547,7 +1597,8 @@ int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *t)
         return fail(ctx, FANSGPU_EINVAL, "n_it >= 0 and tolerance >= 0 required");
     if (t->ls_max_iter < 1 || !(t->ls_tol > 0))
         return fail(ctx, FANSGPU_EINVAL, "linesearch_parameters: max_iter >= 1 and tol > 0 required");
-    ctx->tol = *t;
+    ctx->tol          = *t;
+    ctx->graphs_valid = false; // the update kernel's error measure is a captured argument
     return 0;
 }
 
@@ -1590,6 +1641,35 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
         stats->solve_ms    = ms;
     }
     return conv ? 0 : FANSGPU_ENOTCONV;
+}
+
+int fansgpu_solve_batch(fansgpu_ctx *const *ctxs, int32_t n, fansgpu_stats *stats, int32_t *rcs)
+{
+    if (!ctxs || n < 0)
+        return fail(nullptr, FANSGPU_EINVAL, "fansgpu_solve_batch: bad arguments");
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j)
+            if (!ctxs[i] || ctxs[i] == ctxs[j])
+                return fail(nullptr, FANSGPU_EINVAL, "fansgpu_solve_batch: null or repeated context");
+    std::vector<int>         rc(n, 0);
+    std::vector<std::thread> pool;
+    const int                nt = std::min<int>(n, std::max(1u, std::thread::hardware_concurrency()) * 2);
+    std::atomic<int>         next{0};
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&]() {
+            for (int i = next++; i < n; i = next++)
+                rc[i] = fansgpu_solve(ctxs[i], stats ? &stats[i] : nullptr);
+        });
+    for (auto &th : pool)
+        th.join();
+    int worst = 0;
+    for (int i = 0; i < n; ++i) {
+        if (rcs)
+            rcs[i] = rc[i];
+        if (rc[i] != 0 && rc[i] != FANSGPU_ENOTCONV)
+            worst = rc[i];
+    }
+    return worst;
 }
 
 int fansgpu_homogenized_stress(fansgpu_ctx *ctx, double *out)
@@ -1847,7 +1927,7 @@ int fansgpu_apply_operator(fansgpu_ctx *ctx, const double *x, double *y)
     const long long N = ctx->N;
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, x, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
     FANS_CUDA_CHECK((launch_aos_to_soa<double, double>(ctx->staging, ctx->Kd, N, ctx->C, ctx->st)));
-    if ((rc = run_stencil<double>(ctx, ctx->Kd, ctx->s, false)))
+    if ((rc = ctx->vscale ? run_operator_elem(ctx, ctx->Kd, ctx->s) : run_stencil<double>(ctx, ctx->Kd, ctx->s, false)))
         return rc;
     FANS_CUDA_CHECK((launch_soa_to_aos<double, double>(ctx->s, ctx->staging, N, ctx->C, ctx->st)));
     FANS_CUDA_CHECK(cudaMemcpyAsync(y, ctx->staging, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));

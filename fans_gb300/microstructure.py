@@ -85,3 +85,24 @@ def laminate(n, axis=0, frac=0.5):
     sl[axis] = slice(int(round(m * frac)), m)
     ms[tuple(sl)] = 1
     return ms
+
+
+BATCH_EDGES = (32, 48, 64, 80, 96)
+
+
+def batch_workload(count=64, seed_base=100):
+    """The batched-micro-problem workload: instance k uses seed seed_base + k for
+    its edge (uniform over BATCH_EDGES) and its spheres; even k is thermal
+    (r = 4, vf 0.20, conductivities 1 and 10, three unit gradients), odd k
+    elastic (r = 6, vf 0.30, six unit strains).  The sphere count follows the
+    volume fraction; random sequential addition stops at its attempt cap when a
+    small box cannot hold them all."""
+    out = []
+    for k in range(count):
+        rng = np.random.default_rng(seed_base + k)
+        n = int(BATCH_EDGES[int(rng.integers(0, len(BATCH_EDGES)))])
+        thermal = k % 2 == 0
+        ms, centres = spheres(n, 4 if thermal else 6, 0.20 if thermal else 0.30, seed_base + k,
+                              max_attempts=200_000)
+        out.append({"k": k, "n": n, "thermal": thermal, "ms": ms, "spheres": len(centres)})
+    return out

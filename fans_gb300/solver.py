@@ -238,6 +238,21 @@ class Context:
         return out
 
 
+def solve_batch(contexts):
+    """fansgpu_solve_batch: solve several independent contexts concurrently.
+    Returns one stats dict per context (as Context.solve) plus its status code."""
+    lib = C.load()
+    n = len(contexts)
+    arr = (ctypes.c_void_p * n)(*[c.ctx for c in contexts])
+    st = (C.Stats * n)()
+    rcs = (ctypes.c_int32 * n)()
+    rc = lib.fansgpu_solve_batch(arr, n, st, rcs)
+    if rc not in (C.OK, C.ENOTCONV):
+        raise C.FansGpuError(rc, lib.fansgpu_last_error(None).decode())
+    return [{"iterations": s.iterations, "converged": bool(s.converged), "err0": s.err0, "err": s.err,
+             "refinements": s.refinements, "solve_ms": s.solve_ms, "rc": int(r)} for s, r in zip(st, rcs)]
+
+
 class Solver:
     """Solver<howmany, n_str> (solver.h:11-103) on the GPU.
 

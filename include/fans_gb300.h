@@ -195,6 +195,14 @@ int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *tol);
  * n_it was reached (the state is still valid, as in the reference). */
 int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats);
 
+/* Independent solves of several contexts at once (batched micro problems, e.g.
+ * one per macroscopic integration point): each context's fansgpu_solve runs on
+ * its own host thread and CUDA stream, so small problems overlap on the GPU.
+ * stats and rc (either may be NULL) receive per-context results; returns 0 or
+ * the last hard error (ENOTCONV is reported per context only).  Contexts must
+ * be distinct and not used by other threads meanwhile. */
+int fansgpu_solve_batch(fansgpu_ctx *const *ctxs, int32_t n, fansgpu_stats *stats, int32_t *rc);
+
 /* Solver::get_homogenized_stress (solver.h:708-737): volume average of the
  * element-averaged stress/flux (n_str doubles). */
 int fansgpu_homogenized_stress(fansgpu_ctx *ctx, double *out);
