@@ -16,6 +16,10 @@ EINVAL, ENOMEM, ECUDA, ENOTCONV, ENAN, EUNSUPPORTED, ESTATE = -1, -2, -3, -4, -5
 HEX8, HEX8R, BBAR = 0, 1, 2
 LAW_THERMAL_ISO, LAW_ELASTIC_ISO, LAW_J2_LINEAR, LAW_THERMAL_TRI, LAW_ELASTIC_TRI = 0, 1, 2, 3, 4
 LAW_PSEUDO_LINEAR, LAW_PSEUDO_NONLINEAR = 5, 6
+LAW_J2VISCO_LINEAR, LAW_J2VISCO_NONLINEAR = 7, 8
+LAW_SVK, LAW_NEOHOOKEAN = 9, 10
+SMALL_STRAIN, LARGE_STRAIN = 0, 1
+STRAIN_TYPES = {"small": SMALL_STRAIN, "large": LARGE_STRAIN}
 FP64, MIXED = 0, 1
 CG, FP = 0, 1
 L1, L2, LINF = 0, 1, 2
@@ -24,6 +28,7 @@ FIELD_U, FIELD_R, FIELD_STRAIN, FIELD_STRESS, FIELD_U_PREV = 0, 1, 2, 3, 4
 FIELD_PLASTIC_STRAIN, FIELD_HARDENING = 5, 6
 FIELD_STRAIN_GP, FIELD_STRESS_GP, FIELD_PLASTIC_STRAIN_GP, FIELD_HARDENING_GP = 7, 8, 9, 10
 FIELD_PLASTIC_FLAG = 11
+FIELD_KINEMATIC, FIELD_KINEMATIC_GP = 12, 13
 VOXEL_STIFFNESS_SCALE = 0
 
 FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
@@ -48,7 +53,8 @@ KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv",
 
 class Desc(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32 * 3), ("L", ctypes.c_double * 3), ("howmany", ctypes.c_int32),
-                ("fe_type", ctypes.c_int32), ("precision", ctypes.c_int32), ("method", ctypes.c_int32)]
+                ("fe_type", ctypes.c_int32), ("precision", ctypes.c_int32), ("method", ctypes.c_int32),
+                ("strain_type", ctypes.c_int32)]
 
 
 class Tol(ctypes.Structure):

@@ -85,6 +85,7 @@ struct fansgpu_ctx {
     // nonlinear laws (J2PlasticityNew): internal variables SoA eps_p [6][ngp][N], q [ngp][N],
     // committed (_t) and trial copies; element-row scratch [8C][N] for the residual gather
     double *ep_t = nullptr, *q_t = nullptr, *ep = nullptr, *q = nullptr, *rows = nullptr;
+    double *pb_t = nullptr, *pb = nullptr; // J2ViscoPlastic kinematic hardening [6][ngp][N]
     int    *law_d = nullptr;
     double *prm_d = nullptr;
     double  alpha_warm = 0.1;
@@ -284,7 +285,11 @@ int alloc_nonlinear(fansgpu_ctx *ctx)
     int             rc;
     if ((rc = ensure_rows(ctx)))
         return rc;
-    if (!ctx->ep_t) {
+    bool ivars = false; // laws with internal variables (J2PlasticityNew, J2ViscoPlastic)
+    for (int ph = 0; ph < ctx->nph; ++ph)
+        ivars |= ctx->law[ph] == FANSGPU_LAW_J2_LINEAR || ctx->law[ph] == FANSGPU_LAW_J2VISCO_LINEAR ||
+                 ctx->law[ph] == FANSGPU_LAW_J2VISCO_NONLINEAR;
+    if (ivars && !ctx->ep_t) {
         if ((rc = dalloc(ctx, &ctx->ep_t, nep)) || (rc = dalloc(ctx, &ctx->ep, nep)) ||
             (rc = dalloc(ctx, &ctx->q_t, nq)) || (rc = dalloc(ctx, &ctx->q, nq)))
             return rc;
@@ -292,6 +297,15 @@ int alloc_nonlinear(fansgpu_ctx *ctx)
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep, 0, sizeof(double) * nep, ctx->st));
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q_t, 0, sizeof(double) * nq, ctx->st));
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q, 0, sizeof(double) * nq, ctx->st));
+    }
+    bool visco = false;
+    for (int ph = 0; ph < ctx->nph; ++ph)
+        visco |= ctx->law[ph] == FANSGPU_LAW_J2VISCO_LINEAR || ctx->law[ph] == FANSGPU_LAW_J2VISCO_NONLINEAR;
+    if (visco && !ctx->pb_t) {
+        if ((rc = dalloc(ctx, &ctx->pb_t, nep)) || (rc = dalloc(ctx, &ctx->pb, nep)))
+            return rc;
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->pb_t, 0, sizeof(double) * nep, ctx->st));
+        FANS_CUDA_CHECK(cudaMemsetAsync(ctx->pb, 0, sizeof(double) * nep, ctx->st));
     }
     return 0;
 }
@@ -327,6 +341,10 @@ int upload_law_tables(fansgpu_ctx *ctx)
             const double ec = e0 * std::pow(sy / (3.0 * G * e0), 1.0 / (1.0 - n));
             const double v[8] = {p[0], G, sy, n, e0, ec, mi, nm + mi};
             std::copy(v, v + 8, o);
+        } else if (lw[ph] == FANSGPU_LAW_J2VISCO_LINEAR || lw[ph] == FANSGPU_LAW_J2VISCO_NONLINEAR) {
+            // {K, G, sigma_y, K_iso, H_kin, eta/dt, sigma_inf, delta} (J2Plasticity.h:12-20, :190-199)
+            const double v[8] = {p[0], p[1], p[2], p[3], p[4], p[5] / p[6], opt(7, 0.0), opt(8, 0.0)};
+            std::copy(v, v + 8, o);
         } else {
             for (size_t i = 0; i < std::min<size_t>(kPrm, p.size()); ++i)
                 o[i] = p[i];
@@ -346,8 +364,12 @@ int setup(fansgpu_ctx *ctx)
     const int C = ctx->C, nstr = ctx->nstr, NC = 8 * C;
     if (ctx->tables_dirty) {
         const int nph = std::max(ctx->ms_max + 1, (int)ctx->law.size());
-        if (nph > 16)
-            return fail(ctx, FANSGPU_EUNSUPPORTED, "%d phases: at most 16 phases per context in this build", nph);
+        // per-phase element stiffness tables live in shared memory on the FP64 and
+        // double-float paths: 255 phases fit for thermal problems, 32 for mechanics
+        const int max_ph = C == 1 ? 255 : 32;
+        if (nph > max_ph)
+            return fail(ctx, FANSGPU_EUNSUPPORTED, "%d phases: at most %d phases per context for howmany=%d", nph,
+                        max_ph, C);
         ctx->law.resize(nph, -1);
         ctx->prm.resize(nph);
         ctx->assigned.resize(nph, 0);
@@ -374,7 +396,9 @@ int setup(fansgpu_ctx *ctx)
         std::vector<float>  K32(ctx->nph * NC * NC);
         for (int ph = 0; ph < ctx->nph; ++ph) {
             if (ctx->law[ph] == FANSGPU_LAW_J2_LINEAR || ctx->law[ph] == FANSGPU_LAW_PSEUDO_LINEAR ||
-                ctx->law[ph] == FANSGPU_LAW_PSEUDO_NONLINEAR)
+                ctx->law[ph] == FANSGPU_LAW_PSEUDO_NONLINEAR || ctx->law[ph] == FANSGPU_LAW_J2VISCO_LINEAR ||
+                ctx->law[ph] == FANSGPU_LAW_J2VISCO_NONLINEAR || ctx->law[ph] == FANSGPU_LAW_SVK ||
+                ctx->law[ph] == FANSGPU_LAW_NEOHOOKEAN)
                 ctx->all_linear = false;
             if (!fe::law_C(ctx->law[ph], ctx->prm[ph], nstr, &Cph[ph * nstr * nstr]))
                 return fail(ctx, FANSGPU_EINVAL, "phase %d: law %d does not fit problem with n_str=%d", ph,
@@ -551,6 +575,8 @@ ElementArgs element_args(fansgpu_ctx *ctx, const double *u, int mode)
     a.q_t   = ctx->q_t;
     a.ep    = ctx->ep;
     a.q     = ctx->q;
+    a.pb_t  = ctx->pb_t;
+    a.pb    = ctx->pb;
     a.ve    = ctx->ve;
     a.rows  = ctx->rows;
     a.red   = ctx->red;
@@ -618,7 +644,7 @@ int solve_cg64(fansgpu_ctx *ctx)
     if ((rc = init_scalars(ctx)))
         return rc;
     // r = R(u) (compute_residual<2>, solverCG.h:76)
-    if ((rc = run_stencil<double>(ctx, ctx->u, ctx->r, true)))
+    if ((rc = run_residual64(ctx, ctx->u, ctx->r)))
         return rc;
     { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
@@ -867,7 +893,7 @@ int mixed_update(fansgpu_ctx *ctx)
     if (!ctx->mixed_active || ctx->idxF.empty())
         return 0;
     int    rc;
-    double red[16];
+    double red[32];
     if ((rc = setup(ctx)) || (rc = strain_stress(ctx, -1, nullptr, nullptr, red, nullptr, nullptr, nullptr)))
         return rc;
     const int nf = (int)ctx->idxF.size();
@@ -986,6 +1012,8 @@ int commit_ivars(fansgpu_ctx *ctx)
     const long long nep = 6LL * ctx->ngp * ctx->N, nq = (long long)ctx->ngp * ctx->N;
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->ep_t, ctx->ep, sizeof(double) * nep, cudaMemcpyDeviceToDevice, ctx->st));
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->q_t, ctx->q, sizeof(double) * nq, cudaMemcpyDeviceToDevice, ctx->st));
+    if (ctx->pb_t)
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->pb_t, ctx->pb, sizeof(double) * nep, cudaMemcpyDeviceToDevice, ctx->st));
     return 0;
 }
 
@@ -1112,6 +1140,10 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         return fail(nullptr, FANSGPU_EINVAL, "method must be cg or fp");
     if (desc->precision == FANSGPU_MIXED && desc->method != FANSGPU_CG)
         return fail(nullptr, FANSGPU_EUNSUPPORTED, "mixed precision is implemented for the CG method");
+    if (desc->strain_type != FANSGPU_SMALL_STRAIN && desc->strain_type != FANSGPU_LARGE_STRAIN)
+        return fail(nullptr, FANSGPU_EINVAL, "strain_type must be either 'small' or 'large'");
+    if (desc->strain_type == FANSGPU_LARGE_STRAIN && desc->howmany != 3)
+        return fail(nullptr, FANSGPU_EINVAL, "large strain needs a mechanical problem (howmany = 3)");
     for (int i = 0; i < 3; ++i)
         if (!(desc->L[i] > 0))
             return fail(nullptr, FANSGPU_EINVAL, "L must be positive");
@@ -1124,13 +1156,13 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         ctx->use_graphs = std::strcmp(ev, "0") != 0;
     ctx->g           = Grid3{n[0], n[1], n[2]};
     ctx->C           = desc->howmany;
-    ctx->nstr        = nstr_of(ctx->C);
+    ctx->nstr        = desc->strain_type == FANSGPU_LARGE_STRAIN ? 9 : nstr_of(ctx->C);
     ctx->N           = ctx->g.N();
     ctx->n           = ctx->N * ctx->C;
     for (int i = 0; i < 3; ++i)
         ctx->le[i] = desc->L[i] / (double)n[i]; // reader.cpp:293-296
     ctx->ve  = ctx->le[0] * ctx->le[1] * ctx->le[2];
-    ctx->ngp = fe::gauss_B(desc->fe_type, ctx->C, ctx->le, ctx->B);
+    ctx->ngp = fe::gauss_B(desc->fe_type, ctx->C, ctx->le, ctx->B, ctx->nstr);
     const int NC = 8 * ctx->C, ns = ctx->nstr;
     ctx->Bbar.assign(ns * NC, 0.0);
     for (int gp = 0; gp < ctx->ngp; ++gp)
@@ -1235,7 +1267,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d,
-                    ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc,
+                    ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc, ctx->pb_t, ctx->pb,
                     ctx->vscale, ctx->zero_g0, ctx->stored_u};
     for (void *p : ptrs)
         if (p)
@@ -1292,6 +1324,10 @@ int fansgpu_reset(fansgpu_ctx *ctx)
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep, 0, sizeof(double) * nep, ctx->st));
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q_t, 0, sizeof(double) * nq, ctx->st));
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->q, 0, sizeof(double) * nq, ctx->st));
+        if (ctx->pb_t) {
+            FANS_CUDA_CHECK(cudaMemsetAsync(ctx->pb_t, 0, sizeof(double) * nep, ctx->st));
+            FANS_CUDA_CHECK(cudaMemsetAsync(ctx->pb, 0, sizeof(double) * nep, ctx->st));
+        }
     }
     ctx->err_all.clear();
     ctx->iter   = 0;
@@ -1355,12 +1391,16 @@ int fansgpu_set_phase_material(fansgpu_ctx *ctx, int32_t phase, int32_t law, con
         return FANSGPU_EINVAL;
     if (phase < 0 || phase > 255)
         return fail(ctx, FANSGPU_EINVAL, "MaterialManager: Invalid or duplicate phase %d", phase);
-    if (law < 0 || law > 6 || !params || n_params < 1)
+    if (law < 0 || law > 10 || !params || n_params < 1)
         return fail(ctx, FANSGPU_EINVAL, "invalid material law %d / parameters", law);
     const bool thermal = (law == FANSGPU_LAW_THERMAL_ISO || law == FANSGPU_LAW_THERMAL_TRI);
     if (thermal != (ctx->C == 1))
         return fail(ctx, FANSGPU_EINVAL, "law %d is not valid for a %s problem", law, ctx->C == 1 ? "thermal" : "mechanical");
-    const int need[7] = {1, 2, 4, 9, 36, 4, 5}, most[7] = {1, 2, 4, 9, 36, 6, 7};
+    const bool large_law = law == FANSGPU_LAW_SVK || law == FANSGPU_LAW_NEOHOOKEAN;
+    if (large_law != (ctx->nstr == 9))
+        return fail(ctx, FANSGPU_EINVAL, "law %d is not valid for a %s-strain problem", law,
+                    ctx->nstr == 9 ? "large" : "small");
+    const int need[11] = {1, 2, 4, 9, 36, 4, 5, 7, 9, 2, 2}, most[11] = {1, 2, 4, 9, 36, 6, 7, 7, 9, 2, 2};
     if (n_params < need[law])
         return fail(ctx, FANSGPU_EINVAL, "law %d needs %d parameters, got %d", law, need[law], n_params);
     n_params = std::min(n_params, most[law]);
@@ -1469,6 +1509,8 @@ int fansgpu_enable_mixed_bc(fansgpu_ctx *ctx, int32_t n_e, const int32_t *idx_e,
     // MixedBCController::activate (mixedBCs.h:180-226)
     if (step == 0) {
         ctx->g0.assign(ns, 0.0);
+        if (ns == 9) // large strain starts from F = I (mixedBCs.h:196-202)
+            ctx->g0[0] = ctx->g0[4] = ctx->g0[8] = 1.0;
         ctx->g0_prev = ctx->g0;
     } else {
         if (ctx->g0_prev.size() != (size_t)ns)
@@ -1666,8 +1708,10 @@ int fansgpu_solve_batch(fansgpu_ctx *const *ctxs, int32_t n, fansgpu_stats *stat
     for (int i = 0; i < n; ++i) {
         if (rcs)
             rcs[i] = rc[i];
-        if (rc[i] != 0 && rc[i] != FANSGPU_ENOTCONV)
-            worst = rc[i];
+        if (rc[i] != 0 && rc[i] != FANSGPU_ENOTCONV) {
+            worst          = rc[i];
+            g_create_error = "context " + std::to_string(i) + ": " + ctxs[i]->err_msg;
+        }
     }
     return worst;
 }
@@ -1679,7 +1723,7 @@ int fansgpu_homogenized_stress(fansgpu_ctx *ctx, double *out)
     int rc = setup(ctx);
     if (rc)
         return rc;
-    double red[16];
+    double red[32];
     if ((rc = strain_stress(ctx, -1, nullptr, nullptr, red)))
         return rc;
     for (int i = 0; i < ctx->nstr; ++i)
@@ -1782,7 +1826,7 @@ int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host)
         int rc = setup(ctx);
         if (rc)
             return rc;
-        double red[16];
+        double red[32];
         if ((rc = strain_stress(ctx, -1, which == FANSGPU_FIELD_STRAIN ? ctx->staging : nullptr,
                                 which == FANSGPU_FIELD_STRESS ? ctx->staging : nullptr, red)))
             return rc;
@@ -1805,11 +1849,32 @@ int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host)
         FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
         return 0;
     }
+    if (which == FANSGPU_FIELD_KINEMATIC || which == FANSGPU_FIELD_KINEMATIC_GP) {
+        int rc = setup(ctx);
+        if (rc)
+            return rc;
+        if (!ctx->pb_t)
+            return fail(ctx, FANSGPU_EINVAL, "field %d: no J2ViscoPlastic material", which);
+        const bool gpf = which == FANSGPU_FIELD_KINEMATIC_GP;
+        double    *tmp = nullptr;
+        if (gpf && (rc = dalloc(ctx, &tmp, N * ctx->ngp * 6)))
+            return rc;
+        cudaError_t e = gpf ? launch_ivar_gp(ctx->pb_t, nullptr, ctx->ngp, N, tmp, nullptr, ctx->st)
+                            : launch_ivar_mean(ctx->pb_t, nullptr, ctx->ngp, N, ctx->staging, nullptr, ctx->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(host, gpf ? tmp : ctx->staging, sizeof(double) * N * (gpf ? ctx->ngp : 1) * 6,
+                                cudaMemcpyDeviceToHost, ctx->st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->st);
+        if (tmp)
+            cudaFree(tmp);
+        return e == cudaSuccess ? 0 : fail(ctx, FANSGPU_ECUDA, "kinematic field: %s", cudaGetErrorString(e));
+    }
     if (which == FANSGPU_FIELD_PLASTIC_FLAG) {
         int rc = setup(ctx);
         if (rc)
             return rc;
-        double red[16];
+        double red[32];
         if ((rc = strain_stress(ctx, -1, nullptr, nullptr, red, nullptr, nullptr, ctx->staging)))
             return rc;
         FANS_CUDA_CHECK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->st));
@@ -1828,7 +1893,7 @@ int fansgpu_get_field(fansgpu_ctx *ctx, int32_t which, double *host)
         double         *tmp = nullptr; // postprocess only: a temporary of n_gp x the staging size
         if ((rc = dalloc(ctx, &tmp, cnt)))
             return rc;
-        double red[16];
+        double red[32];
         if (!ivar) {
             rc = strain_stress(ctx, -1, nullptr, nullptr, red, which == FANSGPU_FIELD_STRAIN_GP ? tmp : nullptr,
                                which == FANSGPU_FIELD_STRESS_GP ? tmp : nullptr);

@@ -55,7 +55,35 @@ struct GridRed {
     double      *partials; // [max_blocks][kMaxRed]
     unsigned int *counter;  // one counter per reduction site
 };
-constexpr int kMaxRed = 16;
+constexpr int kMaxRed = 20; // large-strain averages reduce 2*9+1 values
+
+// The device's opt-in maximum of dynamic shared memory per block.  Kernels get
+// this as their MaxDynamicSharedMemorySize permission (a per-kernel, process-wide
+// attribute): one value for every launch, so host threads driving different
+// contexts never race on it.  Occupancy follows each launch's actual size.
+inline int smem_optin_max()
+{
+    static const int v = [] {
+        int dev = 0, b = 48 * 1024;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&b, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return b;
+    }();
+    return v;
+}
+
+// Lets `fn` take as much dynamic shared memory as the device allows next to
+// its static shared memory.  The value is fixed per kernel, so contexts that
+// run on several host threads never race one another to different limits.
+template <typename F>
+inline cudaError_t allow_max_dyn_smem(F *fn)
+{
+    cudaFuncAttributes fa;
+    cudaError_t        e = cudaFuncGetAttributes(&fa, (const void *)fn);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smem_optin_max() - (int)fa.sharedSizeBytes);
+}
 
 // Block-wide reduction of NV values (sum or max per value), result valid in
 // thread 0.  Uses warp shuffles then one pass through shared memory.

@@ -25,11 +25,21 @@ inline void basic_B(double x, double y, double z, const double le[3], double out
 }
 
 // Model B: thermal 3 x 8 (matmodel.h:267-270), small-strain Mandel 6 x 24
-// with shear rows scaled by sqrt(1/2) (matmodel.h:284-304).
-inline void model_B(int C, double x, double y, double z, const double le[3], double *out)
+// with shear rows scaled by sqrt(1/2) (matmodel.h:284-304), or (nstr = 9) the
+// large-strain deformation-gradient B_F: row 3i + J, column 3q + i holds
+// dN_q/dX_J (LargeStrainMechModel.h:209-225).
+inline void model_B(int C, double x, double y, double z, const double le[3], double *out, int nstr = 0)
 {
     double b[3][8];
     basic_B(x, y, z, le, b);
+    if (nstr == 9) {
+        std::memset(out, 0, sizeof(double) * 9 * 24);
+        for (int i = 0; i < 3; ++i)
+            for (int J = 0; J < 3; ++J)
+                for (int q = 0; q < 8; ++q)
+                    out[(3 * i + J) * 24 + 3 * q + i] = b[J][q];
+        return;
+    }
     if (C == 1) {
         for (int i = 0; i < 3; ++i)
             for (int q = 0; q < 8; ++q)
@@ -54,22 +64,22 @@ inline void model_B(int C, double x, double y, double z, const double le[3], dou
 // Gauss-point B matrices (Construct_B, matmodel.h:104-155): HEX8 and BBAR use
 // the 2x2x2 rule at 0.5 +- sqrt(3)/6, HEX8R the centre; BBAR replaces the
 // volumetric part of the normal rows with its centre value (small strain only).
-inline int gauss_B(int fe_type, int C, const double le[3], std::vector<double> &B)
+inline int gauss_B(int fe_type, int C, const double le[3], std::vector<double> &B, int nstr_in = 0)
 {
-    const int nstr = C == 1 ? 3 : 6, ncol = 8 * C;
+    const int nstr = nstr_in ? nstr_in : (C == 1 ? 3 : 6), ncol = 8 * C;
     if (fe_type == 1) {
         B.assign(nstr * ncol, 0.0);
-        model_B(C, 0.5, 0.5, 0.5, le, B.data());
+        model_B(C, 0.5, 0.5, 0.5, le, B.data(), nstr);
         return 1;
     }
     const double p = 0.5 + std::sqrt(3.) / 6., m = 0.5 - std::sqrt(3.) / 6.;
     const double xi[8][3] = {{m, m, m}, {p, m, m}, {m, p, m}, {p, p, m}, {m, m, p}, {p, m, p}, {m, p, p}, {p, p, p}};
     B.assign(8 * nstr * ncol, 0.0);
     for (int g = 0; g < 8; ++g)
-        model_B(C, xi[g][0], xi[g][1], xi[g][2], le, B.data() + g * nstr * ncol);
+        model_B(C, xi[g][0], xi[g][1], xi[g][2], le, B.data() + g * nstr * ncol, nstr);
     if (fe_type == 2 && nstr > 3) {
         std::vector<double> Bv(nstr * ncol);
-        model_B(C, 0.5, 0.5, 0.5, le, Bv.data());
+        model_B(C, 0.5, 0.5, 0.5, le, Bv.data(), nstr);
         for (int g = 0; g < 8; ++g) {
             double *Bg = B.data() + g * nstr * ncol;
             for (int col = 0; col < ncol; ++col) {
@@ -86,7 +96,7 @@ inline int gauss_B(int fe_type, int C, const double le[3], std::vector<double> &
 // Constitutive matrix of a linear law (nstr x nstr, row-major).
 // law 0 thermal iso: kappa I (LinearThermal.h:186);
 // law 1 elastic iso: lambda on the normal 3x3 block + 2 mu I (LinearElastic.h:28-35);
-// laws 2, 5, 6 (J2, PseudoPlastic; their elastic part, for the reference/tangent): as law 1;
+// laws 2, 5-8 (J2, PseudoPlastic, J2ViscoPlastic; their elastic part, for the reference/tangent): as law 1;
 // law 3/4 triclinic: the given matrix (LinearThermal.h:250-254, LinearElastic.h:114-129).
 inline bool law_C(int law, const std::vector<double> &prm, int nstr, double *C)
 {
@@ -96,13 +106,28 @@ inline bool law_C(int law, const std::vector<double> &prm, int nstr, double *C)
             C[i * 3 + i] = prm[0];
         return true;
     }
-    if ((law == 1 || law == 2 || law == 5 || law == 6) && nstr == 6) {
+    if ((law == 1 || law == 2 || law == 5 || law == 6 || law == 7 || law == 8) && nstr == 6) {
         const double lam = prm[0] - (2.0 / 3.0) * prm[1];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)
                 C[i * 6 + j] = lam;
         for (int i = 0; i < 6; ++i)
             C[i * 6 + i] += 2.0 * prm[1];
+        return true;
+    }
+    if ((law == 9 || law == 10) && nstr == 9) {
+        // dP/dF at F = I of SaintVenantKirchhoff / CompressibleNeoHookean as
+        // LargeStrainMechModel::compute_spatial_tangent builds it (LargeStrainMechModel.h:96-170,
+        // S = 0): lambda d_iJ d_kL + mu (d_ik d_JL + d_iL d_Jk), halved where k != L
+        // because that loop takes each symmetric pair (P, Q) once.  Row 3i + J, column 3k + L.
+        const double mu = prm[1], lam = prm[0] - (2.0 / 3.0) * mu;
+        for (int i = 0; i < 3; ++i)
+            for (int J = 0; J < 3; ++J)
+                for (int k = 0; k < 3; ++k)
+                    for (int L = 0; L < 3; ++L)
+                        C[(3 * i + J) * 9 + 3 * k + L] =
+                            (k == L ? 1.0 : 0.5) *
+                            (lam * (i == J) * (k == L) + mu * ((i == k) * (J == L) + (i == L) * (J == k)));
         return true;
     }
     if ((law == 3 && nstr == 3) || (law == 4 && nstr == 6)) {
@@ -119,7 +144,7 @@ inline bool law_C(int law, const std::vector<double> &prm, int nstr, double *C)
 inline void element_stiffness(int C, int ngp, const std::vector<double> &B, const double *Cm, double ve,
                               std::vector<double> &K)
 {
-    const int nstr = C == 1 ? 3 : 6, ncol = 8 * C;
+    const int ncol = 8 * C, nstr = (int)(B.size() / ((size_t)ngp * ncol));
     K.assign(ncol * ncol, 0.0);
     std::vector<double> CB(nstr * ncol);
     for (int g = 0; g < ngp; ++g) {
@@ -145,8 +170,8 @@ inline void element_stiffness(int C, int ngp, const std::vector<double> &B, cons
 inline void element_force(int C, int ngp, const std::vector<double> &B, const double *Cm, const double *g0, double ve,
                           double *f)
 {
-    const int nstr = C == 1 ? 3 : 6, ncol = 8 * C;
-    double    sig[6];
+    const int ncol = 8 * C, nstr = (int)(B.size() / ((size_t)ngp * ncol));
+    double    sig[9];
     for (int i = 0; i < nstr; ++i) {
         double acc = 0.0;
         for (int k = 0; k < nstr; ++k)

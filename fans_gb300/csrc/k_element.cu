@@ -78,6 +78,55 @@ __device__ __forceinline__ void j2_sigma(const double *prm, const double (&e)[6]
     q_out = q_in + c23 * dgamma;
 }
 
+// LargeStrainMechModel::get_sigma (LargeStrainMechModel.h:190-196) for
+// SaintVenantKirchhoff (S = lambda tr(E) I + 2 mu E, E = (F^T F - I)/2,
+// SaintVenantKirchhoff.h:36-41) and CompressibleNeoHookean (S = lambda log(J)
+// C^-1 + mu (I - C^-1), CompressibleNeoHookean.h:36-49): P = F S, F and P stored
+// row-major (F_iJ at 3i + J).  prm: {K, G}, lambda = K - 2G/3, mu = G.  A
+// non-positive det F (where the reference throws) yields NaN, which the solver
+// reports as a non-finite residual.
+__device__ __forceinline__ void large_strain_sigma(int law, const double *prm, const double (&F)[9], double (&P)[9])
+{
+    const double mu = prm[1], lam = prm[0] - (2.0 / 3.0) * mu;
+    double       Cg[9]; // right Cauchy-Green C = F^T F
+#pragma unroll
+    for (int I = 0; I < 3; ++I)
+#pragma unroll
+        for (int J = 0; J < 3; ++J)
+            Cg[3 * I + J] = F[I] * F[J] + F[3 + I] * F[3 + J] + F[6 + I] * F[6 + J];
+    double S[9];
+    if (law == FANSGPU_LAW_SVK) {
+        const double trE = 0.5 * (Cg[0] + Cg[4] + Cg[8] - 3.0);
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            S[k] = mu * (Cg[k] - ((k % 4) == 0 ? 1.0 : 0.0)) + ((k % 4) == 0 ? lam * trE : 0.0);
+    } else {
+        const double J = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+                         F[2] * (F[3] * F[7] - F[4] * F[6]);
+        // C^-1 = adj(C) / det(C), det(C) = J^2
+        double Ci[9];
+        Ci[0] = Cg[4] * Cg[8] - Cg[5] * Cg[7];
+        Ci[1] = Cg[2] * Cg[7] - Cg[1] * Cg[8];
+        Ci[2] = Cg[1] * Cg[5] - Cg[2] * Cg[4];
+        Ci[3] = Cg[5] * Cg[6] - Cg[3] * Cg[8];
+        Ci[4] = Cg[0] * Cg[8] - Cg[2] * Cg[6];
+        Ci[5] = Cg[2] * Cg[3] - Cg[0] * Cg[5];
+        Ci[6] = Cg[3] * Cg[7] - Cg[4] * Cg[6];
+        Ci[7] = Cg[1] * Cg[6] - Cg[0] * Cg[7];
+        Ci[8] = Cg[0] * Cg[4] - Cg[1] * Cg[3];
+        const double inv_det = 1.0 / (J * J);
+        const double c1      = J > 0.0 ? lam * log(J) - mu : __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            S[k] = c1 * Ci[k] * inv_det + ((k % 4) == 0 ? mu : 0.0);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int J = 0; J < 3; ++J)
+            P[3 * i + J] = F[3 * i] * S[J] + F[3 * i + 1] * S[3 + J] + F[3 * i + 2] * S[6 + J];
+}
+
 // One thread per (element, Gauss point): the NGP threads of an element are
 // adjacent lanes of one warp.  Each computes eps, sigma (and the J2 update) of
 // its Gauss point; the element row B^T sigma is summed over the group by a
@@ -135,10 +184,68 @@ __device__ __forceinline__ double pseudo_sigma(int law, const double *prm, const
     return flag;
 }
 
-template <int C, int NGP, int MODE>
+// J2Plasticity::get_sigma with J2ViscoPlastic hardening (J2Plasticity.h:62-108,
+// :158-225), one Gauss point.  prm: {K, G, sigma_y, K_iso, H_kin, eta/dt,
+// sigma_inf, delta}.  The trial psi and psi_bar accumulate over evaluations
+// (psi += c23 gamma, psi_bar -= gamma n), as in the reference; eps_p is rebuilt
+// from its committed value.  Returns gamma; writes sigma and the direction n.
+__device__ __forceinline__ double j2visco_sigma(bool nonlin, const double *prm, const double (&e)[6],
+                                                const double (&ep_in)[6], double psit, const double (&pbt)[6],
+                                                double (&sig)[6], double (&nv)[6])
+{
+    const double K = prm[0], G = prm[1], sy = prm[2], Ki = prm[3], H = prm[4], eta_dt = prm[5];
+    const double c23 = sqrt(2.0 / 3.0);
+    double       ee[6], st[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        ee[i] = e[i] - ep_in[i];
+    const double treps = ee[0] + ee[1] + ee[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        st[i] = (K - 2.0 * G / 3.0) * treps + 2 * G * ee[i];
+#pragma unroll
+    for (int i = 3; i < 6; ++i)
+        st[i] = 2 * G * ee[i];
+    const double mean = (st[0] + st[1] + st[2]) / 3.0;
+    double       qtr  = -Ki * psit;
+    if (nonlin)
+        qtr -= (prm[6] - sy) * (1 - exp(-prm[7] * psit));
+    double dmq[6], n2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        dmq[i] = (i < 3 ? st[i] - mean : st[i]) + (2.0 / 3.0) * H * pbt[i];
+        n2 += dmq[i] * dmq[i];
+    }
+    const double nrm = sqrt(n2);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        nv[i] = nrm < 1e-12 ? 0.0 : dmq[i] / nrm;
+    const double f   = nrm - c23 * (sy - qtr);
+    const double den = 2 * G + (2.0 / 3.0) * (Ki + H) + eta_dt;
+    double       gam = 0.0;
+    if (f >= 0) {
+        if (!nonlin) {
+            gam = f / den;
+        } else { // Newton iteration of J2Plasticity.h:203-214 (its (2 / 3) factor is integer zero)
+            const double sdiff = c23 * (prm[6] - sy), del = prm[7];
+            double       inc   = 1.0;
+            for (int it = 0; inc > 1e-10 && it < 10; ++it) {
+                const double g = f - gam * den - sdiff * (-exp(-del * (psit + c23 * gam)) + exp(-del * psit));
+                inc            = g / den; // -g / dg with dg = -den
+                gam += inc;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        sig[i] = st[i] - gam * 2 * G * nv[i];
+    return gam;
+}
+
+template <int C, int NGP, int MODE, bool LARGE = false>
 __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
 {
-    constexpr int NSTR = C == 1 ? 3 : 6, NCOL = 8 * C;
+    constexpr int NSTR = LARGE ? 9 : (C == 1 ? 3 : 6), NCOL = 8 * C, NE = NSTR > 6 ? NSTR : 6;
     static_assert(32 % NGP == 0 && NCOL % NGP == 0, "group layout");
     __shared__ double Bs[NGP * NSTR * NCOL];
     for (int i = threadIdx.x; i < NGP * NSTR * NCOL; i += blockDim.x)
@@ -159,7 +266,7 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
         const long long el    = t / NGP;
         const bool      valid = el < N;
         const int       ph    = valid ? a.ms[el] : 0;
-        double          e[6], sig[6];
+        double          e[NE], sig[NE];
         {
             double ue[NCOL];
             if (valid) {
@@ -188,8 +295,28 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
         }
         const int law = valid ? a.law[ph] : -1;
         double    flag = 0.0; // elements outside a PseudoPlastic model keep flag 0 (PseudoPlastic.h:37-40)
-        if (C == 3 && (law == FANSGPU_LAW_PSEUDO_LINEAR || law == FANSGPU_LAW_PSEUDO_NONLINEAR)) {
+        if constexpr (LARGE) {
+            large_strain_sigma(law, a.prm + ph * kPrm, e, sig);
+        } else if (C == 3 && (law == FANSGPU_LAW_PSEUDO_LINEAR || law == FANSGPU_LAW_PSEUDO_NONLINEAR)) {
             flag = pseudo_sigma(law, a.prm + ph * kPrm, e, sig);
+        } else if (C == 3 && (law == FANSGPU_LAW_J2VISCO_LINEAR || law == FANSGPU_LAW_J2VISCO_NONLINEAR)) {
+            double          ep_in[6], pbt[6], nv[6];
+            const long long base = (long long)gp * N + el;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                ep_in[i] = a.ep_t[(long long)i * NGP * N + base];
+                pbt[i]   = a.pb_t[(long long)i * NGP * N + base];
+            }
+            const double gam = j2visco_sigma(law == FANSGPU_LAW_J2VISCO_NONLINEAR, a.prm + ph * kPrm, e, ep_in,
+                                             a.q_t[base], pbt, sig, nv);
+            if (a.ep) {
+#pragma unroll
+                for (int i = 0; i < 6; ++i) {
+                    a.ep[(long long)i * NGP * N + base] = ep_in[i] + gam * nv[i];
+                    a.pb[(long long)i * NGP * N + base] -= gam * nv[i];
+                }
+                a.q[base] += gam * sqrt(2.0 / 3.0);
+            }
         } else if (C == 3 && law == FANSGPU_LAW_J2_LINEAR) {
             double          ep_in[6], ep_out[6], q_out;
             const long long base = (long long)gp * N + el;
@@ -517,11 +644,17 @@ cudaError_t launch_element(const ElementArgs &a, cudaStream_t st)
 #define FANSGPU_EL(C_, G_)                                                                                   \
     (res ? (k_element<C_, G_, ELEM_RESIDUAL><<<nb, kElThreads, 0, st>>>(a), 0)                                 \
          : (k_element<C_, G_, ELEM_AVERAGES><<<nb, kElThreads, 0, st>>>(a), 0))
-    if (a.C == 1)
+#define FANSGPU_EL_LARGE(G_)                                                                                 \
+    (res ? (k_element<3, G_, ELEM_RESIDUAL, true><<<nb, kElThreads, 0, st>>>(a), 0)                            \
+         : (k_element<3, G_, ELEM_AVERAGES, true><<<nb, kElThreads, 0, st>>>(a), 0))
+    if (a.nstr == 9)
+        a.ngp == 8 ? FANSGPU_EL_LARGE(8) : FANSGPU_EL_LARGE(1);
+    else if (a.C == 1)
         a.ngp == 8 ? FANSGPU_EL(1, 8) : FANSGPU_EL(1, 1);
     else
         a.ngp == 8 ? FANSGPU_EL(3, 8) : FANSGPU_EL(3, 1);
 #undef FANSGPU_EL
+#undef FANSGPU_EL_LARGE
     return cudaGetLastError();
 }
 

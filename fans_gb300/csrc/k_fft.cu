@@ -222,7 +222,7 @@ int z_rows_per_cta(const ConvPlan<T> &p)
 template <typename T>
 cudaError_t set_smem(const void *fn, size_t bytes)
 {
-    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return allow_max_dyn_smem(fn);
 }
 
 // ------------------------------------------------------------ Green's table --
@@ -279,6 +279,52 @@ __device__ void sym_pinv3(int n, const double *Ain, double tol, double *P)
         }
 }
 
+// Inverse of a symmetric positive-definite n x n block (n <= 3) by LDL^T when
+// every pivot exceeds 1e-4 of the largest diagonal entry and 1e-8 in absolute
+// value: the block is then well conditioned and its eigenvalues lie far above
+// the pseudo-inverse's absolute cut of 1e-14, so its inverse equals that
+// pseudo-inverse to round-off.  Returns false (caller takes the Jacobi path)
+// otherwise -- singular blocks (hourglass frequencies of HEX8R, round-off-sized
+// blocks) always do.
+__device__ bool spd_inv3(int n, const double *A, double *P)
+{
+    double dmax = 0.0;
+    for (int i = 0; i < n; ++i)
+        dmax = fmax(dmax, fabs(A[i * n + i]));
+    double L[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, D[3];
+    for (int j = 0; j < n; ++j) {
+        double d = A[j * n + j];
+        for (int k = 0; k < j; ++k)
+            d -= L[j][k] * L[j][k] * D[k];
+        if (!(d > 1e-4 * dmax) || !(d > 1e-8)) // well conditioned and far above the 1e-14 cut
+            return false;
+        D[j] = d;
+        for (int i = j + 1; i < n; ++i) {
+            double s = A[i * n + j];
+            for (int k = 0; k < j; ++k)
+                s -= L[i][k] * L[j][k] * D[k];
+            L[i][j] = s / d;
+        }
+    }
+    // inverse of the unit lower-triangular L, then P = L^-T D^-1 L^-1
+    double Li[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 1; i < n; ++i)
+        for (int j = 0; j < i; ++j) {
+            double s = 0.0;
+            for (int k = j; k < i; ++k)
+                s -= L[i][k] * Li[k][j];
+            Li[i][j] = s;
+        }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            double s = 0.0;
+            for (int k = (i > j ? i : j); k < n; ++k)
+                s += Li[k][i] * Li[k][j] / D[k];
+            P[i * n + j] = s;
+        }
+    return true;
+}
+
 template <int C>
 __global__ void __launch_bounds__(256) k_green(GreenArgs a)
 {
@@ -322,7 +368,8 @@ __global__ void __launch_bounds__(256) k_green(GreenArgs a)
                     blk[i * C + j] = acc;
                     blk[j * C + i] = acc;
                 }
-            sym_pinv3(C, blk, 1e-14, pinv);
+            if (!spd_inv3(C, blk, pinv))
+                sym_pinv3(C, blk, 1e-14, pinv);
             int t = 0;
 #pragma unroll
             for (int i = 0; i < C; ++i)

@@ -292,13 +292,13 @@ cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
     dim3          g((p.nzh + KC - 1) / KC, p.g.ny);
     if (p.C == 1) {
         const size_t sm = sizeof(cplx<T>) * (size_t)N1 * N2 * KC;
-        cudaError_t  e  = cudaFuncSetAttribute(k_x_green_reg<T, N1, N2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 1>);
         if (e != cudaSuccess)
             return e;
         k_x_green_reg<T, N1, N2, 1><<<g, KC * N1, sm, st>>>(p);
     } else {
         const size_t sm = sizeof(cplx<T>) * (size_t)3 * N1 * N2 * KC;
-        cudaError_t  e  = cudaFuncSetAttribute(k_x_green_reg<T, N1, N2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 3>);
         if (e != cudaSuccess)
             return e;
         k_x_green_reg<T, N1, N2, 3><<<g, 3 * KC * N1, sm, st>>>(p);

@@ -304,7 +304,7 @@ cudaError_t launch_stencil_pk(const StencilArgs &a, cudaStream_t st)
         }
     dim3         grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + TZ - 1) / TZ);
     const size_t sm = sizeof(T) * (size_t)C * HX * HY * HZ + EX * EY * EZ;
-    cudaError_t  e  = cudaFuncSetAttribute(k_stencil_pk<T, C, NPH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t  e  = allow_max_dyn_smem(k_stencil_pk<T, C, NPH>);
     if (e != cudaSuccess)
         return e;
     k_stencil_pk<T, C, NPH><<<grid, kStencilThreads, sm, st>>>(a, P);
@@ -334,7 +334,7 @@ cudaError_t launch_stencil_c(const StencilArgs &a, cudaStream_t st)
     }
     dim3   grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + TZ - 1) / TZ);
     size_t sm = stencil_smem<T, C>(a);
-    cudaError_t e = cudaFuncSetAttribute(k_stencil<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = allow_max_dyn_smem(k_stencil<T, C>);
     if (e != cudaSuccess)
         return e;
     k_stencil<T, C><<<grid, kStencilThreads, sm, st>>>(a);
@@ -345,13 +345,10 @@ cudaError_t launch_stencil_c(const StencilArgs &a, cudaStream_t st)
 template <int C, int NSTR>
 __global__ void __launch_bounds__(256) k_strain_stress(StrainStressArgs a)
 {
-    __shared__ double Cs[16 * NSTR * NSTR];
+    const double     *Cs = a.Cph; // per-phase constitutive matrices (read through L1)
     __shared__ double red_smem[32 * (2 * NSTR + 1)];
-    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
-    const long long N = (long long)nx * ny * nz;
-    for (int i = threadIdx.x; i < a.nph * NSTR * NSTR; i += blockDim.x)
-        Cs[i] = a.Cph[i];
-    __syncthreads();
+    const int         nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const long long   N  = (long long)nx * ny * nz;
     double se[NSTR], ss[NSTR], cnt = 0.0;
 #pragma unroll
     for (int i = 0; i < NSTR; ++i)
@@ -638,11 +635,11 @@ cudaError_t launch_residual_df(const StencilArgs &a, cudaStream_t st)
     const size_t sm = sizeof(float) * (2 * (size_t)a.C * HX * HY * HZ + 2 * (size_t)a.nph * NC * NC) + EX * EY * EZ;
     cudaError_t  e;
     if (a.C == 1) {
-        if ((e = cudaFuncSetAttribute(k_residual_df<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
+        if ((e = allow_max_dyn_smem(k_residual_df<1>)))
             return e;
         k_residual_df<1><<<grid, kStencilThreads, sm, st>>>(a);
     } else {
-        if ((e = cudaFuncSetAttribute(k_residual_df<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
+        if ((e = allow_max_dyn_smem(k_residual_df<3>)))
             return e;
         k_residual_df<3><<<grid, kStencilThreads, sm, st>>>(a);
     }

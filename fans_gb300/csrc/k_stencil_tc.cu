@@ -6,7 +6,8 @@
 // U[e] = u_e - u_e,node0 (the 8C element displacements relative to the element's
 // first node, solver.h:252) and W the per-phase element stiffnesses.  The GEMM
 // runs as tcgen05.mma kind::tf32 (M = 128 elements, N = 8C x phases, K = 8C)
-// with both operands split hi + lo (3xTF32: lo*hi + hi*lo + hi*hi), which keeps
+// with both operands split hi + lo (hi = the top 11 significant bits, lo = the exact
+// FP32 remainder; 3xTF32: lo*hi + hi*lo + hi*hi), which keeps
 // the product at FP32 accuracy; D accumulates in tensor memory.  Each thread
 // then keeps its element's phase columns and the node gather sums the 8
 // element rows around every node in a fixed order (deterministic).
@@ -84,12 +85,13 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr)
     return d;
 }
 
-__device__ __forceinline__ float to_tf32(float x)
-{
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
+// tf32 part of x by truncation to the 10 explicit mantissa bits the MMA reads;
+// x - hi is exact in FP32 and carries the rest (one LOP3 instead of a rounding
+// conversion).
+__device__ __forceinline__ float to_tf32(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+// x in [-n, 2n): periodic index without a division
+__device__ __forceinline__ int wrap(int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 {
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     // node plane X: thread's share of (s, d_old) into registers
     float sv[NPF], dv[NPF];
     auto load_plane = [&](int X) {
-        const long long gx = (long long)pmod(X, nx) * plane;
+        const long long gx = (long long)wrap(X, nx) * plane;
 #pragma unroll
         for (int k = 0; k < NPF; ++k)
             if (valid_mask & (1u << k)) {
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     // d = s + beta d_old of the registered plane X into node slot ds (+ d_new for owned nodes)
     auto store_plane = [&](int X, int ds) {
         const bool      owned_x = X >= xs && X < xe;
-        const long long gx      = (long long)pmod(X, nx) * plane;
+        const long long gx      = (long long)wrap(X, nx) * plane;
 #pragma unroll
         for (int k = 0; k < NPF; ++k)
             if (valid_mask & (1u << k)) {
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     auto output_plane = [&](int Xo, int so, int ds) {
         if (!out_ok)
             return;
-        const long long gi = (long long)pmod(Xo, nx) * plane + oyz;
+        const long long gi = (long long)wrap(Xo, nx) * plane + oyz;
         float dl = 0.f;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     const uint32_t tmem = *tmem_slot;
     store_plane(xs - 1, 0);
     load_plane(xs);
-    int ph_cur = a.ms[(long long)pmod(xs - 1, nx) * plane + el_yz];
+    int ph_cur = a.ms[(long long)wrap(xs - 1, nx) * plane + el_yz];
 
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Cfg::NW >> 3) << 17) | (8u << 24);
     bool ok = true;
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
         store_plane(X + 1, (j + 1) % 3);
         if (X + 2 <= xe)
             load_plane(X + 2);
-        const int ph_next = X + 1 < xe ? (int)a.ms[(long long)pmod(X + 1, nx) * plane + el_yz] : 0;
+        const int ph_next = X + 1 < xe ? (int)a.ms[(long long)wrap(X + 1, nx) * plane + el_yz] : 0;
         __syncthreads(); // S2: node plane X+1 ready
 
         // element row of plane X, split hi/lo, in the core-matrix layout
@@ -407,9 +409,8 @@ void stencil_tc_pack_weights(int C, int nph, const float *K32, float *out)
             const float x = K32[((size_t)(n / ncol) * ncol + n % ncol) * ncol + k];
             uint32_t    u;
             std::memcpy(&u, &x, 4);
-            // round to nearest, ties away from zero, at tf32 precision (10 explicit mantissa bits)
-            const uint32_t e = u & 0x7F800000u;
-            uint32_t       h = e == 0x7F800000u ? u : ((u + 0x1000u) & 0xFFFFE000u);
+            // top 11 significant bits (10 explicit mantissa bits), as the kernel splits its operand
+            const uint32_t h = u & 0xFFFFE000u;
             float          hi;
             std::memcpy(&hi, &h, 4);
             const float  lo  = x - hi;
@@ -425,7 +426,7 @@ cudaError_t launch_stencil_tc(const StencilArgs &a, const float *W, int nph, cud
 #define FANSGPU_TC(C_, P_)                                                                                       \
     do {                                                                                                       \
         constexpr int sm = TcCfg<C_, P_>::SMEM;                                                                \
-        cudaError_t   e  = cudaFuncSetAttribute(k_stencil_tc<C_, P_>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm); \
+        cudaError_t   e  = allow_max_dyn_smem(k_stencil_tc<C_, P_>); \
         if (e != cudaSuccess)                                                                                  \
             return e;                                                                                          \
         k_stencil_tc<C_, P_><<<grid, TPB, sm, st>>>(a, W);                                                     \

@@ -98,6 +98,8 @@ struct ElementArgs {
     const double  *prm;   // per phase, 8 law parameters (J2, PseudoPlastic)
     const double  *ep_t, *q_t; // committed internal variables [6][ngp][N], [ngp][N]
     double        *ep, *q;     // trial internal variables (written)
+    const double  *pb_t;       // committed kinematic hardening psi_bar [6][ngp][N] (J2ViscoPlastic)
+    double        *pb;         // trial psi_bar
     double         ve;
     double        *rows;  // RESIDUAL: [8C][N] element rows
     // AVERAGES:

@@ -213,6 +213,8 @@ class H5File:
     @staticmethod
     def _dtype(d):
         cls, ver = d[0] & 0x0F, d[0] >> 4
+        if cls == 9 and (d[1] & 0x0F) == 1:
+            return "vlen_str"  # variable-length string: (length, global heap address, index) per element
         bits = d[1] | (d[2] << 8) | (d[3] << 16)
         size = int.from_bytes(d[4:8], "little")
         order = ">" if bits & 1 else "<"
@@ -236,6 +238,22 @@ class H5File:
         dims = struct.unpack_from(f"<{nd}Q", d, p)
         return tuple(int(x) for x in dims)
 
+    def _global_heap_object(self, addr, index):
+        """Object `index` of the global heap collection at `addr` (GCOL)."""
+        a = self._addr(addr)
+        if self.buf[a:a + 4] != b"GCOL":
+            raise H5Error("bad global heap collection signature")
+        size = self._u(a + 8, 8)
+        p, end = a + 16, a + size
+        while p + 16 <= end:
+            idx, osz = self._u(p, 2), self._u(p + 8, 8)
+            if idx == 0:
+                break
+            if idx == index:
+                return self.buf[p + 16:p + 16 + osz]
+            p += 16 + _pad8(osz)
+        raise H5Error(f"global heap object {index} not found")
+
     def _read_attr(self, d):
         ver = d[0]
         nlen, tlen, slen = struct.unpack_from("<HHH", d, 2)
@@ -256,6 +274,15 @@ class H5File:
             shape = self._dataspace(d[p:p + slen])
             p += slen
         count = int(np.prod(shape)) if shape else 1
+        if isinstance(dt, str):  # variable-length strings
+            vals = []
+            for k in range(count):
+                q = p + 16 * k
+                ln = int.from_bytes(d[q:q + 4], "little")
+                addr = int.from_bytes(d[q + 4:q + 12], "little")
+                idx = int.from_bytes(d[q + 12:q + 16], "little")
+                vals.append(self._global_heap_object(addr, idx)[:ln].decode("utf-8") if ln else "")
+            return name, vals[0] if not shape else vals
         arr = np.frombuffer(d, dtype=dt, count=count, offset=p).copy()
         return name, arr.reshape(shape) if shape else arr[0]
 
@@ -426,6 +453,10 @@ def _msg(t, data, flags=0):
     return struct.pack("<HHB3x", t, len(data), flags) + data
 
 
+class VlenStr(str):
+    """A string attribute written as an HDF5 variable-length string (as h5py does)."""
+
+
 class _Stored:
     """A dataset whose raw data is already in the file."""
 
@@ -451,6 +482,7 @@ class H5Writer:
         self.f = open(path, "wb")
         self.f.write(b"\0" * 96)  # superblock + root symbol-table entry, written at close
         self.pos = 96
+        self._gheap = []  # (index, bytes) of variable-length string attributes
 
     def __enter__(self):
         return self
@@ -498,6 +530,21 @@ class H5Writer:
     def close(self):
         if self.f is None:
             return
+        # variable-length strings live in one global heap collection; its address is
+        # needed by the attribute messages, so it is placed first
+        vl = []
+        self._collect_vlen(self.root, vl)
+        self._gheap_addr = UNDEF
+        if vl:
+            body = b""
+            for i, txt in enumerate(vl, start=1):
+                raw = txt.encode("utf-8")
+                body += struct.pack("<HHIQ", i, 1, 0, len(raw)) + raw + b"\0" * (_pad8(len(raw)) - len(raw))
+                self._gheap.append((i, txt))
+            size = max(4096, 16 + len(body) + 16)
+            free = size - 16 - len(body)
+            body += struct.pack("<HHIQ", 0, 0, 0, free) + b"\0" * (free - 16)
+            self._gheap_addr = self._append(b"GCOL" + bytes([1, 0, 0, 0]) + struct.pack("<Q", size) + body)
         root_addr = self._write_group(self.root)
         eof = self.pos
         sb = bytearray()
@@ -511,9 +558,39 @@ class H5Writer:
         self.f.close()
         self.f = None
 
+    def _collect_vlen(self, node, out):
+        items = node.children.values() if isinstance(node, _Node) else []
+        for v in (node.attrs.values() if isinstance(node, _Node) else []):
+            if isinstance(v, VlenStr):
+                out.append(str(v))
+        for ch in items:
+            if isinstance(ch, _Node):
+                self._collect_vlen(ch, out)
+            else:
+                out.extend(str(v) for v in ch.attrs.values() if isinstance(v, VlenStr))
+
+    def _vlen_index(self, txt):
+        for i, t in self._gheap:
+            if t == txt:
+                return i
+        raise H5Error("variable-length string not in the global heap")
+
     def _attr_msgs(self, attrs):
         out = b""
         for k, v in attrs.items():
+            if isinstance(v, VlenStr):
+                name = k.encode() + b"\0"
+                raw = str(v).encode("utf-8")
+                base = struct.pack("<BBBBI", 0x10, 0, 0, 0, 1) + struct.pack("<HH", 0, 8)  # unsigned 8-bit char
+                dt = struct.pack("<BBBBI", 0x19, 0x01, 0x01, 0, 16) + base  # vlen string, UTF-8
+                sp = _space_msg(())
+                body = struct.pack("<BBHHH", 1, 0, len(name), len(dt), len(sp))
+                body += name + b"\0" * (_pad8(len(name)) - len(name))
+                body += dt + b"\0" * (_pad8(len(dt)) - len(dt))
+                body += sp + b"\0" * (_pad8(len(sp)) - len(sp))
+                body += struct.pack("<IQI", len(raw), self._gheap_addr, self._vlen_index(str(v)))
+                out += _msg(0x0C, body)
+                continue
             if isinstance(v, str):
                 v = np.frombuffer(v.encode() + b"\0", dtype=f"S{len(v.encode()) + 1}")[0]
             arr = np.asarray(v)

@@ -9,6 +9,8 @@ model's get_reference_stiffness().
 """
 from __future__ import annotations
 
+import json
+
 import numpy as np
 
 from . import _lib as C
@@ -36,6 +38,22 @@ def _pseudo_nl(props, i):
     return [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i]), float(props["yield_stress"][i]),
             float(props["hardening_exponent"][i]), float(props["eps_0"][i]), float(i),
             float(len(props["bulk_modulus"]))]
+
+
+def _j2visco(nonlinear):
+    def build(props, i):  # J2Plasticity.h:12-20, :190-199
+        p = [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i]), float(props["yield_stress"][i]),
+             float(props["isotropic_hardening_parameter"][i]), float(props["kinematic_hardening_parameter"][i]),
+             float(props["viscosity"][i]), float(props["time_step"])]
+        if nonlinear:
+            p += [float(props["saturation_stress"][i]), float(props["saturation_exponent"][i])]
+        return p
+
+    return build
+
+
+def _large(props, i):  # SaintVenantKirchhoff.h:17-31, CompressibleNeoHookean.h:19-33
+    return [float(props["bulk_modulus"][i]), float(props["shear_modulus"][i])]
 
 
 def _j2(props, i):
@@ -69,7 +87,36 @@ MODELS = {
     "J2PlasticityNew_LinearIsotropicHardening": (C.LAW_J2_LINEAR, "mechanical", _j2),
     "PseudoPlasticLinearHardening": (C.LAW_PSEUDO_LINEAR, "mechanical", _pseudo_lin),
     "PseudoPlasticNonLinearHardening": (C.LAW_PSEUDO_NONLINEAR, "mechanical", _pseudo_nl),
+    "J2ViscoPlastic_LinearIsotropicHardening": (C.LAW_J2VISCO_LINEAR, "mechanical", _j2visco(False)),
+    "J2ViscoPlastic_NonLinearIsotropicHardening": (C.LAW_J2VISCO_NONLINEAR, "mechanical", _j2visco(True)),
+    "SaintVenantKirchhoff": (C.LAW_SVK, "mechanical_large", _large),
+    "CompressibleNeoHookean": (C.LAW_NEOHOOKEAN, "mechanical_large", _large),
 }
+
+
+NONLINEAR_LAWS = (C.LAW_J2_LINEAR, C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR, C.LAW_J2VISCO_LINEAR,
+                  C.LAW_J2VISCO_NONLINEAR, C.LAW_SVK, C.LAW_NEOHOOKEAN)
+LARGE_STRAIN_LAWS = (C.LAW_SVK, C.LAW_NEOHOOKEAN)
+
+
+def large_strain_tangent(K, G):
+    """dP/dF at F = I (row 3i + J, column 3k + L) as
+    LargeStrainMechModel::compute_spatial_tangent (LargeStrainMechModel.h:96-170)
+    assembles it from the Mandel tangent lambda 1 1^T + 2 mu I that both
+    SaintVenantKirchhoff and CompressibleNeoHookean have at F = I (S = 0).  That
+    loop visits each symmetric pair (P, Q) once with dE_PQ/dF_kL =
+    (F_kP d_QL + F_kQ d_PL)/2, so entries with k != L carry half of
+    lambda d_iJ d_kL + mu (d_ik d_JL + d_iL d_Jk)."""
+    lam, mu = K - 2.0 / 3.0 * G, G
+    A = np.zeros((9, 9))
+    d = np.eye(3)
+    for i in range(3):
+        for J in range(3):
+            for k in range(3):
+                for L in range(3):
+                    v = lam * d[i, J] * d[k, L] + mu * (d[i, k] * d[J, L] + d[i, L] * d[J, k])
+                    A[3 * i + J, 3 * k + L] = v if k == L else 0.5 * v
+    return A
 
 
 def iso_elastic_C(K, G):
@@ -91,8 +138,10 @@ def group_reference_stiffness(law, params):
         M = np.zeros((6, 6))
         M[:3, :3] = lr
         return M + 2 * mr * np.eye(6)
-    if law in (C.LAW_J2_LINEAR, C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR):
-        # J2PlasticityNew.h:111-121, PseudoPlastic.h:41-51 (mean K, G)
+    if law in LARGE_STRAIN_LAWS:  # SaintVenantKirchhoff.h:61-80, CompressibleNeoHookean.h:108-121
+        return np.mean([large_strain_tangent(p[0], p[1]) for p in params], axis=0)
+    if law in NONLINEAR_LAWS:
+        # J2PlasticityNew.h:111-121, PseudoPlastic.h:41-51, J2Plasticity.h:113-124 (mean K, G)
         Kb, Gb = np.mean([p[0] for p in params]), np.mean([p[1] for p in params])
         M = np.zeros((6, 6))
         M[:3, :3] = Kb - 2.0 * Gb / 3.0
@@ -102,10 +151,45 @@ def group_reference_stiffness(law, params):
     return np.mean([np.asarray(p).reshape(n, n) for p in params], axis=0)
 
 
-class MaterialManager:
-    """Phase id -> (law, parameters) table plus the reference stiffness."""
+def gb_diffusion_tensors(props, gb_info):
+    """GBDiffusion phase conductivities (GBDiffusion.h:45-118): crystals (tags below
+    num_crystals) D_bulk I, grain boundaries D_par (I - n n^T) + D_perp n n^T with the
+    normalised GB normal of the tag.  `gb_info` holds num_crystals, num_GB and the
+    GBVoxelInfo JSON of the microstructure dataset's attributes."""
+    nc, ngb = int(gb_info["num_crystals"]), int(gb_info["num_GB"])
+    n_mat = nc + ngb
+    info = gb_info["GBVoxelInfo"]
+    info = json.loads(info) if isinstance(info, (str, bytes)) else info
+    normals = np.zeros((n_mat, 3))
+    for v in info.values():
+        normals[int(v["GB_tag"])] = np.asarray(v["GB_normal"], dtype=float)
+    if props["GB_unformity"]:
+        Db, Dpa, Dpe = np.zeros(n_mat), np.zeros(n_mat), np.zeros(n_mat)
+        Db[:nc] = float(props["D_bulk"])
+        Dpa[nc:] = float(props["D_par"])
+        Dpe[nc:] = float(props["D_perp"])
+    else:
+        Db, Dpa, Dpe = (np.asarray(props[k][:n_mat], dtype=float) for k in ("D_bulk", "D_par", "D_perp"))
+    out = []
+    for i in range(n_mat):
+        if i < nc:
+            K = Db[i] * np.eye(3)
+        else:
+            n = normals[i] / np.linalg.norm(normals[i])
+            K = Dpa[i] * (np.eye(3) - np.outer(n, n)) + Dpe[i] * np.outer(n, n)
+        out.append(list(K.ravel()))
+    return out, normals
 
-    def __init__(self, input_json: dict, problem_type: str | None = None):
+
+class MaterialManager:
+    """Phase id -> (law, parameters) table plus the reference stiffness.
+
+    `gb_info` supplies the microstructure attributes a GBDiffusion group needs
+    (num_crystals, num_GB, GBVoxelInfo); the driver reads them from the HDF5
+    dataset as GBDiffusion.h:50-60 does."""
+
+    def __init__(self, input_json: dict, problem_type: str | None = None, gb_info: dict | None = None,
+                 strain_type: str = "small"):
         if "matmodel" in input_json and "material_properties" in input_json:
             props = input_json["material_properties"]
             n = next(len(v) for v in props.values() if isinstance(v, list))
@@ -124,13 +208,35 @@ class MaterialManager:
         self.groups = []
         self.all_linear = True
         refs = []
+        self.gb_normals = None
         for mg in mats:
             name = mg["matmodel"]
+            if name == "GBDiffusion":
+                if problem_type is not None and problem_type != "thermal":
+                    raise ValueError(f"{name} is not a valid matmodel for {problem_type} problem")
+                if gb_info is None:
+                    raise RuntimeError("Error in GBDiffusion initialization: microstructure attributes missing")
+                tensors, self.gb_normals = gb_diffusion_tensors(mg["material_properties"], gb_info)
+                gparams = []
+                for i, ph in enumerate(mg["phases"]):
+                    if ph < 0 or ph >= n_phases or self.law[ph] is not None:
+                        raise RuntimeError(f"MaterialManager: Invalid or duplicate phase {ph}")
+                    self.law[ph] = C.LAW_THERMAL_TRI
+                    self.params[ph] = tensors[i]
+                    gparams.append(tensors[i])
+                self.groups.append((name, C.LAW_THERMAL_TRI, list(mg["phases"]), gparams))
+                refs.append(np.mean([np.asarray(p).reshape(3, 3) for p in tensors], axis=0))  # kappa_average
+                continue
             if name not in MODELS:
                 raise ValueError(f"{name} is not a valid matmodel")
             law, kind, builder = MODELS[name]
-            if problem_type is not None and kind != problem_type:
-                raise ValueError(f"{name} is not a valid matmodel for {problem_type} problem")
+            want = problem_type
+            if problem_type == "mechanical" and strain_type == "large":
+                want = "mechanical_large"
+            if problem_type is not None and kind != want:  # setup.h:22-73
+                what = {"thermal": "matmodel for thermal problem", "mechanical": "small strain material model",
+                        "mechanical_large": "large strain material model"}[want]
+                raise ValueError(f"{name} is not a valid {what}")
             gparams = []
             for i, ph in enumerate(mg["phases"]):
                 if ph < 0 or ph >= n_phases or self.law[ph] is not None:
@@ -142,7 +248,7 @@ class MaterialManager:
                 self.law[ph] = law
                 self.params[ph] = prm
                 gparams.append(prm)
-            if law in (C.LAW_J2_LINEAR, C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR):
+            if law in NONLINEAR_LAWS:
                 self.all_linear = False
             self.groups.append((name, law, list(mg["phases"]), gparams))
             refs.append(group_reference_stiffness(law, gparams))

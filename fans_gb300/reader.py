@@ -191,6 +191,22 @@ class Reader:
         self.set_microstructure(ms)
         return self
 
+    def gb_info(self):
+        """num_crystals, num_GB and GBVoxelInfo of the microstructure dataset (the
+        attributes GBDiffusion reads, GBDiffusion.h:50-60), or None."""
+        if getattr(self, "_gb_info", None) is not None:
+            return self._gb_info
+        path = self.ms_filename
+        if not os.path.isabs(path) and os.path.exists(os.path.join(self.base_dir, path)):
+            path = os.path.join(self.base_dir, path)
+        if not os.path.exists(path):
+            return None
+        attrs = h5.H5File(path).attrs(self.ms_datasetname)
+        if "num_crystals" not in attrs:
+            return None
+        self._gb_info = {k: attrs[k] for k in ("num_crystals", "num_GB", "GBVoxelInfo")}
+        return self._gb_info
+
     def set_microstructure(self, ms):
         """Install an [x][y][z] phase array directly (the ReadMS result)."""
         ms = np.ascontiguousarray(ms).astype(np.uint16)  # H5T_NATIVE_USHORT (reader.cpp:259)

@@ -70,7 +70,11 @@ def postprocess(solver, reader: Reader, results: ResultsFile, load_idx: int, tim
     z = np.arange(nz) * dz - reader.L[2] / 2.0
     X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
     u_total = v_u.copy()
-    if howmany == 3:
+    if n_str == 9:  # large strain: u = (F - I) X (solver.h:622-640)
+        Fm = np.reshape(strain_average, (3, 3)) - np.eye(3)
+        for i in range(3):
+            u_total[..., i] += Fm[i, 0] * X + Fm[i, 1] * Y + Fm[i, 2] * Z
+    elif howmany == 3:
         rs2 = 0.7071067811865475
         g11, g22, g33 = strain_average[0], strain_average[1], strain_average[2]
         g12, g13, g23 = strain_average[3] * rs2, strain_average[4] * rs2, strain_average[5] * rs2
@@ -102,8 +106,10 @@ def postprocess(solver, reader: Reader, results: ResultsFile, load_idx: int, tim
     if want("stress_gp"):
         results.writeSlab("stress_gp", load_idx, time_idx, ctx.get_field(C.FIELD_STRESS_GP), (ctx.n_gp, n_str))
 
-    # MaterialManager::postprocess -> J2PlasticityNew::postprocess (J2PlasticityNew.h:160-200)
-    if not solver.matmanager.all_linear:
+    # MaterialManager::postprocess -> J2PlasticityNew::postprocess (J2PlasticityNew.h:160-200) and
+    # J2Plasticity::postprocess (J2Plasticity.h:248-322)
+    ivar_laws = (C.LAW_J2_LINEAR, C.LAW_J2VISCO_LINEAR, C.LAW_J2VISCO_NONLINEAR)
+    if any(law in ivar_laws for law in solver.matmanager.law):
         if want("plastic_strain"):
             results.writeSlab("plastic_strain", load_idx, time_idx, ctx.get_field(C.FIELD_PLASTIC_STRAIN), (6,))
         if want("plastic_strain_gp"):
@@ -115,12 +121,25 @@ def postprocess(solver, reader: Reader, results: ResultsFile, load_idx: int, tim
         if want("isotropic_hardening_variable_gp"):
             results.writeSlab("isotropic_hardening_variable_gp", load_idx, time_idx,
                               ctx.get_field(C.FIELD_HARDENING_GP), (ctx.n_gp,))
+        visco = any(law in (C.LAW_J2VISCO_LINEAR, C.LAW_J2VISCO_NONLINEAR) for law in solver.matmanager.law)
+        if visco and want("kinematic_hardening_variable"):  # J2Plasticity.h:283-288
+            results.writeSlab("kinematic_hardening_variable", load_idx, time_idx, ctx.get_field(C.FIELD_KINEMATIC),
+                              (6,))
+        if visco and want("kinematic_hardening_variable_gp"):
+            results.writeSlab("kinematic_hardening_variable_gp", load_idx, time_idx,
+                              ctx.get_field(C.FIELD_KINEMATIC_GP), (ctx.n_gp, 6))
 
     # PseudoPlastic::postprocess (PseudoPlastic.h:55-63): element mean of the plastic flags, float32
     if want("plastic_flag") and any(law in (C.LAW_PSEUDO_LINEAR, C.LAW_PSEUDO_NONLINEAR)
                                     for law in solver.matmanager.law):
         results.writeSlab("plastic_flag", load_idx, time_idx,
                           ctx.get_field(C.FIELD_PLASTIC_FLAG).astype(np.float32), (1,))
+
+    # GBDiffusion::postprocess (GBDiffusion.h:171-187): the GB normal of each GB voxel
+    if want("GBnormals") and solver.matmanager.gb_normals is not None:
+        nc = int(reader.gb_info()["num_crystals"])
+        normals = np.where((reader.ms >= nc)[..., None], solver.matmanager.gb_normals[reader.ms], 0.0)
+        results.writeSlab("GBnormals", load_idx, time_idx, normals, (3,))
 
     if want("homogenized_tangent"):
         T = solver.get_homogenized_tangent(1e-6)
@@ -136,7 +155,7 @@ def run_solver(reader: Reader, results: ResultsFile, precision="fp64", log=print
         reader.ReadMS()
     out = []
     for li, lc in enumerate(reader.load_cases):
-        mm = MaterialManager(reader.inputJson, reader.problemType)
+        mm = MaterialManager(reader.inputJson, reader.problemType, reader.gb_info(), reader.strain_type)
         solver = create_solver(reader, mm, precision)
         try:
             log(f"# Load case {li + 1}/{len(reader.load_cases)}: {lc.n_steps} time steps")
@@ -180,9 +199,8 @@ def main(argv=None, log=print):
     except Exception as e:  # reader.cpp:179-182
         sys.stderr.write(f"ERROR trying to read input file '{argv[0]}' for FANS: {e}\n")
         return 10
-    if reader.problemType not in ("thermal", "mechanical") or (reader.problemType == "mechanical" and
-                                                                reader.strain_type != "small"):
-        raise ValueError(f"{reader.problemType} ({reader.strain_type} strain) is not a valid problem type here")
+    if reader.problemType not in ("thermal", "mechanical"):  # main.cpp:64-77
+        raise ValueError(f"Invalid problem type: {reader.problemType}")
     results = ResultsFile(reader, argv[1])
     try:
         run_solver(reader, results, precision, log)

@@ -24,7 +24,8 @@ def _ptr(a):
 class Context:
     """One GPU solver context (fansgpu_create .. fansgpu_destroy)."""
 
-    def __init__(self, n, L=(1.0, 1.0, 1.0), howmany=3, fe_type="HEX8", precision="fp64", method="cg"):
+    def __init__(self, n, L=(1.0, 1.0, 1.0), howmany=3, fe_type="HEX8", precision="fp64", method="cg",
+                 strain_type="small"):
         self.lib = C.load()
         d = C.Desc()
         d.n[:] = [int(v) for v in n]
@@ -33,6 +34,7 @@ class Context:
         d.fe_type = C.FE_TYPES[fe_type] if isinstance(fe_type, str) else int(fe_type)
         d.precision = {"fp64": C.FP64, "mixed": C.MIXED}[precision] if isinstance(precision, str) else int(precision)
         d.method = {"cg": C.CG, "fp": C.FP}[method] if isinstance(method, str) else int(method)
+        d.strain_type = C.STRAIN_TYPES[strain_type] if isinstance(strain_type, str) else int(strain_type)
         ptr = ctypes.c_void_p()
         rc = self.lib.fansgpu_create(ctypes.byref(d), ctypes.byref(ptr))
         if rc != C.OK:
@@ -40,7 +42,8 @@ class Context:
         self.ctx = ptr
         self.n = tuple(int(v) for v in n)
         self.howmany = int(howmany)
-        self.n_str = 3 if howmany == 1 else 6
+        self.large_strain = d.strain_type == C.LARGE_STRAIN
+        self.n_str = 9 if self.large_strain else (3 if howmany == 1 else 6)
         self.n_gp = 1 if d.fe_type == C.FE_TYPES["HEX8R"] else 8
         self.N = self.n[0] * self.n[1] * self.n[2]
 
@@ -118,8 +121,10 @@ class Context:
     def get_field(self, which):
         if which in (C.FIELD_U, C.FIELD_R, C.FIELD_U_PREV):
             shape = (self.howmany,)
-        elif which == C.FIELD_PLASTIC_STRAIN:
+        elif which in (C.FIELD_PLASTIC_STRAIN, C.FIELD_KINEMATIC):
             shape = (6,)
+        elif which == C.FIELD_KINEMATIC_GP:
+            shape = (self.n_gp, 6)
         elif which in (C.FIELD_HARDENING, C.FIELD_PLASTIC_FLAG):
             shape = (1,)
         elif which in (C.FIELD_STRAIN_GP, C.FIELD_STRESS_GP):
@@ -266,8 +271,9 @@ class Solver:
         self.reader = reader
         self.matmanager = matmanager
         self.howmany = 1 if reader.problemType == "thermal" else 3
-        self.n_str = 3 if self.howmany == 1 else 6
-        self.ctx = Context(reader.dims, reader.L, self.howmany, reader.FE_type, precision, self.method)
+        strain_type = getattr(reader, "strain_type", "small") if self.howmany == 3 else "small"
+        self.ctx = Context(reader.dims, reader.L, self.howmany, reader.FE_type, precision, self.method, strain_type)
+        self.n_str = self.ctx.n_str
         self.ctx.set_microstructure(reader.ms)
         matmanager.apply(self.ctx)
         self._push_tolerance()

@@ -52,7 +52,11 @@ extern "C" {
  *                     [, index in its material group, phases in the group]}  PseudoPlastic.h:80-122
  *   PSEUDO_NONLINEAR {bulk, shear, yield_stress, hardening_exponent, eps_0
  *                     [, index in its material group, phases in the group]}  PseudoPlastic.h:124-167
- *   (the optional pair sets the plastic_flag values, mat_index / n_mat + mat_index) */
+ *   (the optional pair sets the plastic_flag values, mat_index / n_mat + mat_index)
+ *   J2VISCO_LINEAR    {bulk, shear, yield_stress, isotropic_hardening, kinematic_hardening,
+ *                      viscosity, time_step}                        J2Plasticity.h:7-185
+ *   J2VISCO_NONLINEAR {... as J2VISCO_LINEAR, saturation_stress, saturation_exponent}
+ *                                                                  J2Plasticity.h:187-245 */
 #define FANSGPU_LAW_THERMAL_ISO 0
 #define FANSGPU_LAW_ELASTIC_ISO 1
 #define FANSGPU_LAW_J2_LINEAR 2
@@ -60,6 +64,10 @@ extern "C" {
 #define FANSGPU_LAW_ELASTIC_TRI 4
 #define FANSGPU_LAW_PSEUDO_LINEAR 5
 #define FANSGPU_LAW_PSEUDO_NONLINEAR 6
+#define FANSGPU_LAW_J2VISCO_LINEAR 7
+#define FANSGPU_LAW_J2VISCO_NONLINEAR 8
+#define FANSGPU_LAW_SVK 9         /* SaintVenantKirchhoff {bulk, shear} (large strain) */
+#define FANSGPU_LAW_NEOHOOKEAN 10 /* CompressibleNeoHookean {bulk, shear} (large strain) */
 
 /* precision of the solve */
 #define FANSGPU_FP64 0  /* all FP64: parity path against the FP64 reference */
@@ -89,6 +97,8 @@ extern "C" {
 #define FANSGPU_FIELD_PLASTIC_STRAIN_GP 9  /* J2: committed eps_p, [x][y][z][n_gp][6] (get_field only) */
 #define FANSGPU_FIELD_HARDENING_GP 10      /* J2: committed q, [x][y][z][n_gp] (get_field only) */
 #define FANSGPU_FIELD_PLASTIC_FLAG 11      /* PseudoPlastic: Gauss-point mean of the plastic flag, [x][y][z] */
+#define FANSGPU_FIELD_KINEMATIC 12         /* J2ViscoPlastic: Gauss-point mean of committed psi_bar, [x][y][z][6] */
+#define FANSGPU_FIELD_KINEMATIC_GP 13      /* J2ViscoPlastic: committed psi_bar, [x][y][z][n_gp][6] */
 
 typedef struct fansgpu_ctx fansgpu_ctx;
 
@@ -97,11 +107,16 @@ typedef struct fansgpu_ctx fansgpu_ctx;
 typedef struct {
     int32_t n[3];      /* voxels n_x, n_y, n_z (each even, 4..1024) */
     double  L[3];      /* microstructure box lengths (reader.cpp:83) */
-    int32_t howmany;   /* 1: thermal <1,3>; 3: small-strain mechanics <3,6> (main.cpp:67-75) */
-    int32_t fe_type;   /* FANSGPU_HEX8 / HEX8R / BBAR */
-    int32_t precision; /* FANSGPU_FP64 / FANSGPU_MIXED */
-    int32_t method;    /* FANSGPU_CG / FANSGPU_FP */
+    int32_t howmany;     /* 1: thermal <1,3>; 3: mechanics (main.cpp:67-75) */
+    int32_t fe_type;     /* FANSGPU_HEX8 / HEX8R / BBAR */
+    int32_t precision;   /* FANSGPU_FP64 / FANSGPU_MIXED */
+    int32_t method;      /* FANSGPU_CG / FANSGPU_FP */
+    int32_t strain_type; /* FANSGPU_SMALL_STRAIN <3,6> (0, default) or FANSGPU_LARGE_STRAIN <3,9> */
 } fansgpu_desc;
+
+#define FANSGPU_SMALL_STRAIN 0
+#define FANSGPU_LARGE_STRAIN 1 /* n_str = 9: g0 and strains are the deformation gradient F (row-major),
+                                  stresses the first Piola-Kirchhoff stress P (LargeStrainMechModel.h) */
 
 /* error_parameters, n_it and linesearch_parameters (reader.cpp:94-105). */
 typedef struct {

@@ -45,7 +45,17 @@
 
 enum { FO_HEX8 = 0, FO_HEX8R = 1, FO_BBAR = 2 };
 enum { FO_LAW_THERMAL_ISO = 0, FO_LAW_ELASTIC_ISO = 1, FO_LAW_J2 = 2, FO_LAW_THERMAL_TRI = 3, FO_LAW_ELASTIC_TRI = 4,
-       FO_LAW_PSEUDO_LIN = 5, FO_LAW_PSEUDO_NL = 6 };
+       FO_LAW_PSEUDO_LIN = 5, FO_LAW_PSEUDO_NL = 6, FO_LAW_J2VISCO_LIN = 7, FO_LAW_J2VISCO_NL = 8 };
+
+/* Kinematic-hardening internal variable psi_bar of J2ViscoPlastic [N][ngp][6]
+ * (committed and trial), bound before calls that evaluate the laws. */
+static const double *g_pb_t = 0;
+static double       *g_pb   = 0;
+FO_API void fo_bind_kinematic(const double *pb_t, double *pb)
+{
+    g_pb_t = pb_t;
+    g_pb   = pb;
+}
 enum { FO_L1 = 0, FO_L2 = 1, FO_LINF = 2 };
 enum { FO_ABS = 0, FO_REL = 1 };
 
@@ -625,6 +635,68 @@ static void law_sigma(const fo_problem *P, int phase, size_t elem, int gp, const
             sig[i] = buf1 + buf2 * dev[i];
         for (int i = 3; i < 6; ++i)
             sig[i] = buf2 * dev[i];
+        break;
+    }
+    case FO_LAW_J2VISCO_LIN:
+    case FO_LAW_J2VISCO_NL: {
+        /* J2Plasticity::get_sigma (J2Plasticity.h:62-108) with compute_q_trial / compute_gamma of
+         * J2ViscoPlastic_{Linear,NonLinear}IsotropicHardening (:158-225); param = {K, G, sigma_y,
+         * K_iso, H_kin, eta, dt, sigma_inf, delta}.  As the reference does, the trial psi and psi_bar
+         * accumulate over every evaluation (psi += ..., psi_bar -= ...); the plastic strain is
+         * recomputed from its committed value. */
+        const double Kb = pr[0], G = pr[1], sy = pr[2], Ki = pr[3], H = pr[4], eta = pr[5], dt = pr[6];
+        const double c23 = sqrt(2.0 / 3.0);
+        const size_t gi  = elem * P->ngp + gp;
+        const double *ep_in = P->ep_t + gi * 6, *pbt = g_pb_t + gi * 6;
+        double ee[6], st[6], dev[6], dmq[6], nv[6], nrm = 0.0;
+        for (int i = 0; i < 6; ++i)
+            ee[i] = eps[i] - ep_in[i];
+        const double treps = ee[0] + ee[1] + ee[2];
+        for (int i = 0; i < 3; ++i)
+            st[i] = (Kb - 2.0 * G / 3.0) * treps + 2 * G * ee[i];
+        for (int i = 3; i < 6; ++i)
+            st[i] = 2 * G * ee[i];
+        const double mean = (st[0] + st[1] + st[2]) / 3.0;
+        for (int i = 0; i < 6; ++i)
+            dev[i] = i < 3 ? st[i] - mean : st[i];
+        const double psit = P->q_t[gi];
+        double qtr = -Ki * psit;
+        if (P->law[phase] == FO_LAW_J2VISCO_NL)
+            qtr -= (pr[7] - sy) * (1 - exp(-pr[8] * psit));
+        for (int i = 0; i < 6; ++i) {
+            dmq[i] = dev[i] + (2.0 / 3.0) * H * pbt[i]; /* dev - qbar, qbar = -(2/3) H psi_bar_t */
+            nrm += dmq[i] * dmq[i];
+        }
+        nrm = sqrt(nrm);
+        for (int i = 0; i < 6; ++i)
+            nv[i] = nrm < 1e-12 ? 0.0 : dmq[i] / nrm;
+        const double f = nrm - c23 * (sy - qtr);
+        const double den = 2 * G + (2.0 / 3.0) * (Ki + H) + eta / dt;
+        double gam = 0.0;
+        if (f >= 0) {
+            if (P->law[phase] == FO_LAW_J2VISCO_LIN) {
+                gam = f / den;
+            } else { /* Newton iteration of J2Plasticity.h:203-214; its (2 / 3) is integer 0 */
+                const double sdiff = c23 * (pr[7] - sy), del = pr[8];
+                double inc = 1.0;
+                int it = 0;
+                while (inc > 1e-10 && it < 10) {
+                    const double g  = f - gam * den - sdiff * (-exp(-del * (psit + c23 * gam)) + exp(-del * psit));
+                    const double dg = -den - 0.0 * (pr[7] - sy) * del * exp(-del * (psit + c23 * gam));
+                    inc = -g / dg;
+                    gam += inc;
+                    it++;
+                }
+            }
+        }
+        for (int i = 0; i < 6; ++i)
+            sig[i] = st[i] - gam * 2 * G * nv[i];
+        double *ep_out = P->ep + gi * 6, *pb = g_pb + gi * 6;
+        for (int i = 0; i < 6; ++i) {
+            ep_out[i] = ep_in[i] + gam * nv[i];
+            pb[i] -= gam * nv[i];
+        }
+        P->q[gi] += gam * c23;
         break;
     }
     case FO_LAW_J2: {

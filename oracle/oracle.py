@@ -29,7 +29,8 @@ HEX8, HEX8R, BBAR = 0, 1, 2
 FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
 LAW_THERMAL_ISO, LAW_ELASTIC_ISO, LAW_J2, LAW_THERMAL_TRI, LAW_ELASTIC_TRI = 0, 1, 2, 3, 4
 LAW_PSEUDO_LIN, LAW_PSEUDO_NL = 5, 6
-NONLINEAR_LAWS = (LAW_J2, LAW_PSEUDO_LIN, LAW_PSEUDO_NL)
+LAW_J2VISCO_LIN, LAW_J2VISCO_NL = 7, 8
+NONLINEAR_LAWS = (LAW_J2, LAW_PSEUDO_LIN, LAW_PSEUDO_NL, LAW_J2VISCO_LIN, LAW_J2VISCO_NL)
 L1, L2, LINF = 0, 1, 2
 ABS, REL = 0, 1
 MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}
@@ -66,6 +67,8 @@ _lp = ctypes.POINTER(ctypes.c_long)
 
 
 def _declare(L):
+    L.fo_bind_kinematic.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    L.fo_bind_kinematic.restype = None
     i, d, sz = ctypes.c_int, ctypes.c_double, ctypes.c_size_t
     L.fo_build_B.argtypes = [i, i, _dp, _dp]
     L.fo_build_B.restype = i
@@ -195,6 +198,9 @@ class OracleProblem:
         self.q_t = np.zeros((nel, self.ngp)) if not self.linear else np.zeros(1)
         self.ep = self.ep_t.copy()
         self.q = self.q_t.copy()
+        # J2ViscoPlastic kinematic hardening psi_bar [N][ngp][6] (committed, trial)
+        self.pb_t = np.zeros((nel, self.ngp, 6)) if not self.linear else np.zeros(6)
+        self.pb = self.pb_t.copy()
         self.g0 = np.zeros(self.nstr)
         self.u = np.zeros((self.nx, self.ny, self.nz, c))
         self.u_prev = np.zeros_like(self.u)
@@ -212,6 +218,7 @@ class OracleProblem:
         return self._G
 
     def _common(self):
+        lib().fo_bind_kinematic(_p(self.pb_t), _p(self.pb))
         return (self.nx, self.ny, self.nz, self.c, self.ngp, self.ve, _p(self.B), _p(self.ms, _u16p), self.nphase,
                 _p(self.law, _ip), _p(self.param), _p(self.g0), _p(self.ep_t), _p(self.q_t), _p(self.ep),
                 _p(self.q))
@@ -358,6 +365,7 @@ class OracleProblem:
         if not self.linear:
             self.ep_t[...] = self.ep
             self.q_t[...] = self.q
+            self.pb_t[...] = self.pb
         return it
 
     def solve(self, method="cg", measure="L2", type="relative", tol=1e-10, n_it=100, ls_max_iter=5, ls_tol=1e-2):
@@ -378,6 +386,7 @@ class OracleProblem:
         if not self.linear:
             self.ep_t[...] = self.ep
             self.q_t[...] = self.q
+            self.pb_t[...] = self.pb
         return it
 
     def extrapolate_displacement(self):

@@ -31,7 +31,7 @@ def gpu_context(P, precision="fp64", method="cg"):
     ctx = Context((P.nx, P.ny, P.nz), tuple(P.L), P.c, fe, precision, method)
     ctx.set_microstructure(P.ms)
     nparams = {O.LAW_THERMAL_ISO: 1, O.LAW_ELASTIC_ISO: 2, O.LAW_J2: 4, O.LAW_THERMAL_TRI: 9, O.LAW_ELASTIC_TRI: 36,
-               O.LAW_PSEUDO_LIN: 4, O.LAW_PSEUDO_NL: 5}
+               O.LAW_PSEUDO_LIN: 4, O.LAW_PSEUDO_NL: 5, O.LAW_J2VISCO_LIN: 7, O.LAW_J2VISCO_NL: 9}
     for ph in range(P.nphase):
         law = int(P.law[ph])
         ctx.set_phase_material(ph, law, P.param[ph, : nparams[law]])

@@ -151,3 +151,35 @@ def test_pyfans_cmat_packing_is_the_upper_triangle_row_by_row():
 
     assert len(CMAT_ENTRIES) == 21 and len(set(CMAT_ENTRIES)) == 21
     assert CMAT_ENTRIES == [(r, c) for r in range(6) for c in range(r, 6)]
+
+
+def test_vlen_string_attribute_round_trip(tmp_path):
+    info = {"g0": {"GB_tag": 5, "GB_normal": [0.0, 0.6, 0.8]}}
+    p = str(tmp_path / "gb.h5")
+    with h5.H5Writer(p) as w:
+        w.dataset("/poly/ms", np.zeros((4, 4, 4), np.uint8),
+                  {"num_crystals": np.int64(5), "num_GB": np.int64(1), "GBVoxelInfo": h5.VlenStr(json.dumps(info))})
+    a = h5.H5File(p).attrs("/poly/ms")
+    assert int(a["num_crystals"]) == 5 and int(a["num_GB"]) == 1
+    assert json.loads(a["GBVoxelInfo"]) == info
+
+
+def test_gb_diffusion_tensors():
+    from fans_gb300.materials import MaterialManager, gb_diffusion_tensors
+
+    info = {"num_crystals": 2, "num_GB": 2,
+            "GBVoxelInfo": json.dumps({"a": {"GB_tag": 2, "GB_normal": [0, 0, 2.0]},
+                                       "b": {"GB_tag": 3, "GB_normal": [1.0, 1.0, 0]}})}
+    props = {"GB_unformity": True, "D_bulk": 1.5, "D_par": 4.0, "D_perp": 0.5}
+    K, normals = gb_diffusion_tensors(props, info)
+    assert np.allclose(np.reshape(K[0], (3, 3)), 1.5 * np.eye(3))
+    assert np.allclose(np.reshape(K[2], (3, 3)), np.diag([4.0, 4.0, 0.5]))  # normal z, normalised
+    n = np.array([1.0, 1.0, 0]) / np.sqrt(2)
+    assert np.allclose(np.reshape(K[3], (3, 3)) @ n, 0.5 * n)
+    mm = MaterialManager({"materials": [{"phases": [0, 1, 2, 3], "matmodel": "GBDiffusion",
+                                         "material_properties": props}]}, "thermal", info)
+    assert mm.law == [3, 3, 3, 3]
+    assert np.allclose(mm.kapparef_mat, np.mean([np.reshape(k, (3, 3)) for k in K], axis=0))
+    with pytest.raises(ValueError):
+        MaterialManager({"materials": [{"phases": [0], "matmodel": "GBDiffusion", "material_properties": props}]},
+                        "mechanical", info)
