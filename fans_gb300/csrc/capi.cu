@@ -654,6 +654,8 @@ int solve_cg64(fansgpu_ctx *ctx)
         return rc;
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
+    if (!std::isfinite(ctx->scal_h->err))
+        return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm (e.g. det F <= 0 in CompressibleNeoHookean)");
     double err_rel = err_value(ctx, ctx->scal_h->err);
     if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
         ctx->u_zero = false; // u is updated from here on
@@ -771,6 +773,8 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         return rc;
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
+    if (!std::isfinite(ctx->scal_h->err))
+        return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm (e.g. det F <= 0 in CompressibleNeoHookean)");
     *refinements      = 0;
     double err_rel    = err_value(ctx, ctx->scal_h->err);
     double last_true  = ctx->scal_h->err;
@@ -860,6 +864,8 @@ int solve_fp64(fansgpu_ctx *ctx)
         return rc;
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
+    if (!std::isfinite(ctx->scal_h->err))
+        return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm (e.g. det F <= 0 in CompressibleNeoHookean)");
     double err_rel = err_value(ctx, ctx->scal_h->err);
     if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
         ctx->u_zero = false; // u is updated from here on
@@ -950,6 +956,8 @@ int solve_cg_nl(fansgpu_ctx *ctx)
         return rc;
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
+    if (!std::isfinite(ctx->scal_h->err))
+        return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm (e.g. det F <= 0 in CompressibleNeoHookean)");
     double err_rel = err_value(ctx, ctx->scal_h->err);
     if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
         ctx->u_zero = false;
@@ -1427,9 +1435,20 @@ int fansgpu_set_reference(fansgpu_ctx *ctx, const double *kref)
     for (int i = 0; i < ns * ns; ++i)
         if (!std::isfinite(kref[i]))
             return fail(ctx, FANSGPU_EINVAL, "reference_material has non-finite entries");
-    // LLT check as MaterialManager.h:189-192 (symmetric positive definite)
+    // LLT check as MaterialManager.h:189-192 (symmetric positive definite).  The
+    // large-strain reference dP/dF at F = I is only semidefinite (rotations carry
+    // no stress, LargeStrainMechModel.h:96-170), so n_str = 9 checks symmetry.
+    if (ns == 9) {
+        double amax = 0.0;
+        for (int i = 0; i < ns * ns; ++i)
+            amax = std::max(amax, std::fabs(kref[i]));
+        for (int i = 0; i < ns; ++i)
+            for (int j = 0; j < i; ++j)
+                if (std::fabs(kref[i * ns + j] - kref[j * ns + i]) > 1e-12 * amax)
+                    return fail(ctx, FANSGPU_EINVAL, "reference_material must be symmetric");
+    }
     std::vector<double> L(ns * ns, 0.0);
-    for (int j = 0; j < ns; ++j) {
+    for (int j = 0; j < ns && ns != 9; ++j) {
         double d = kref[j * ns + j];
         for (int k = 0; k < j; ++k)
             d -= L[j * ns + k] * L[j * ns + k];
@@ -1740,7 +1759,7 @@ int fansgpu_postprocess_averages(fansgpu_ctx *ctx, double *strain_avg, double *s
     if (rc)
         return rc;
     const int ns = ctx->nstr;
-    double    red[16];
+    double    red[32];
     if ((rc = strain_stress(ctx, -1, nullptr, nullptr, red)))
         return rc;
     for (int i = 0; i < ns; ++i) {

@@ -57,10 +57,7 @@ struct GridRed {
 };
 constexpr int kMaxRed = 20; // large-strain averages reduce 2*9+1 values
 
-// The device's opt-in maximum of dynamic shared memory per block.  Kernels get
-// this as their MaxDynamicSharedMemorySize permission (a per-kernel, process-wide
-// attribute): one value for every launch, so host threads driving different
-// contexts never race on it.  Occupancy follows each launch's actual size.
+// The device's opt-in maximum of shared memory per block (static + dynamic).
 inline int smem_optin_max()
 {
     static const int v = [] {
@@ -73,8 +70,10 @@ inline int smem_optin_max()
 }
 
 // Lets `fn` take as much dynamic shared memory as the device allows next to
-// its static shared memory.  The value is fixed per kernel, so contexts that
-// run on several host threads never race one another to different limits.
+// its static shared memory.  MaxDynamicSharedMemorySize is a per-kernel,
+// process-wide attribute: one fixed value per kernel means contexts driven
+// from several host threads never race one another to different limits.
+// Occupancy follows each launch's actual size.
 template <typename F>
 inline cudaError_t allow_max_dyn_smem(F *fn)
 {
@@ -84,6 +83,11 @@ inline cudaError_t allow_max_dyn_smem(F *fn)
     return cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smem_optin_max() - (int)fa.sharedSizeBytes);
 }
+
+// Maxima that keep NaN (fmax returns the other operand), so that a non-finite
+// residual reaches the host through the Linfinity norm as well.
+__device__ __forceinline__ double nan_max(double a, double b) { return (a > b || a != a) ? a : b; }
+__device__ __forceinline__ float  nan_maxf(float a, float b) { return (a > b || a != a) ? a : b; }
 
 // Block-wide reduction of NV values (sum or max per value), result valid in
 // thread 0.  Uses warp shuffles then one pass through shared memory.
@@ -96,7 +100,7 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&ops)[N
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             double t = __shfl_down_sync(0xffffffffu, v[k], o);
-            v[k]     = ops[k] == RED_MAX ? fmax(v[k], t) : v[k] + t;
+            v[k]     = ops[k] == RED_MAX ? nan_max(v[k], t) : v[k] + t;
         }
     }
     __syncthreads();
@@ -112,7 +116,7 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&ops)[N
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 double t2 = __shfl_down_sync(0xffffffffu, t, o);
-                t         = ops[k] == RED_MAX ? fmax(t, t2) : t + t2;
+                t         = ops[k] == RED_MAX ? nan_max(t, t2) : t + t2;
             }
             v[k] = t;
         }
@@ -161,7 +165,7 @@ __device__ __forceinline__ void grid_final(double (&v)[NV], const int (&ops)[NV]
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             double t = __ldcg(&partials[(size_t)b * kMaxRed + k]);
-            v[k]     = ops[k] == RED_MAX ? fmax(v[k], t) : v[k] + t;
+            v[k]     = ops[k] == RED_MAX ? nan_max(v[k], t) : v[k] + t;
         }
     block_reduce<NV>(v, ops, smem);
 }

@@ -6,25 +6,28 @@
 // U[e] = u_e - u_e,node0 (the 8C element displacements relative to the element's
 // first node, solver.h:252) and W the per-phase element stiffnesses.  The GEMM
 // runs as tcgen05.mma kind::tf32 (M = 128 elements, N = 8C x phases, K = 8C)
-// with both operands split hi + lo (hi = the top 11 significant bits, lo = the exact
-// FP32 remainder; 3xTF32: lo*hi + hi*lo + hi*hi), which keeps
-// the product at FP32 accuracy; D accumulates in tensor memory.  Each thread
-// then keeps its element's phase columns and the node gather sums the 8
-// element rows around every node in a fixed order (deterministic).
+// with both operands split hi + lo (hi = the top 11 significant bits, lo = the
+// exact FP32 remainder; 3xTF32: lo*hi + hi*lo + hi*hi), which keeps the product
+// at FP32 accuracy.  A (the element rows) is written by each thread straight
+// into its tensor-memory lane with tcgen05.st; W sits in shared memory; D
+// accumulates in tensor memory.
 //
 // A CTA owns a 3 (y) x 31 (z) column of nodes, whose element plane is exactly
-// one M-tile (4 x 32 = 128 elements, one per thread), and marches along x over
-// XL planes.  Per step it stores node plane X+1 (d = s + beta d_old, prefetched
-// into registers during the previous step; written to d_new for owned nodes),
-// builds the element rows of plane X, issues the 9 MMAs, writes node plane X-1
-// (K d and <d, K d>) while the tensor cores run, then scatters D into per-colour
-// node accumulators.  Warp w holds element row ey = w and lane l element ez = l;
-// an element adds into copy (ey%2, ez%2): elements of one colour share no node,
-// so no two writers meet, and a node's value is the sum of the four copies in
-// colour order -- a fixed summation order, no atomics, and consecutive lanes on
-// consecutive shared-memory words.  Global offsets of a thread's prefetch slots
-// and output node are computed once; per plane only the x offset changes.
-// 56 KB of shared memory and 64 TMEM columns per CTA let four CTAs share an SM.
+// one M-tile (4 x 32 = 128 elements; warp w holds element row ey = w, lane l
+// element ez = l) and marches along x over XL planes.  Per step it stages node
+// plane X+1 (d = s + beta d_old from registers prefetched one step earlier;
+// written to d_new for owned nodes), builds the element rows of plane X into
+// tensor memory, issues the 9 MMAs, writes node plane X-1 (K d and <d, K d>)
+// while the tensor cores run, then reads its element's phase columns of D and
+// sums them into nodes without shared-memory atomics or colour copies:
+//   x: the rows of the element's far-x nodes are carried in registers to the
+//      next plane, where the same thread adds its near-x rows;
+//   z: one warp shuffle adds lane ez-1's far-z rows;
+//   y: the far-y partial goes through a small shared exchange buffer and warp
+//      ey+1 adds it when it writes the node.
+// Every node is therefore a fixed-order sum (deterministic).  About 12 KB of
+// shared memory is used; 56 KB is requested so that at most four CTAs share an
+// SM, which is what their 4 x 128 tensor-memory columns allow.
 #include "kernels.cuh"
 
 #include <cstring>
@@ -40,8 +43,11 @@ constexpr int NEL = EYN * EZN;            // 128 elements = one M-tile
 constexpr int TPB = 128;
 constexpr int NPL = PY * PZ;              // 165 nodes per plane incl. halo
 constexpr int XL  = 32;                   // planes per CTA
+constexpr int TCOLS  = 128;               // tensor memory: D [0, 64), A hi [64, 96), A lo [96, 128)
+constexpr int COL_AH = 64, COL_AL = 96;
+constexpr int SMEM_REQ = 56 * 1024;       // caps residency at 4 CTAs per SM (4 x 128 TMEM columns)
 constexpr unsigned kWaitLimit = 1u << 24; // bounded mbarrier wait
-static_assert(NEL == 128, "one M-tile per element plane");
+static_assert(NEL == 128 && EYN == 4 && EZN == 32, "one M-tile per element plane, one warp per element row");
 
 template <int C, int NPH>
 struct TcCfg {
@@ -52,18 +58,16 @@ struct TcCfg {
     static constexpr int NROW    = NPH * NCOL;            // stacked phase rows
     static constexpr int NW      = (NROW + 15) / 16 * 16; // MMA N
     static constexpr int KSTEPS  = NCOL / 8;              // K = 8 per tf32 MMA
-    static constexpr int A_BYTES = 128 * NCOL * 4;
     static constexpr int W_BYTES = NW * NCOL * 4;
-    static constexpr int TCOLS   = NW <= 32 ? 32 : NW <= 64 ? 64 : 128;
     static constexpr int NPF     = (C * NPL + TPB - 1) / TPB; // prefetched node values per thread and field
     static constexpr int al(int b) { return (b + 127) / 128 * 128; }
-    static constexpr int OFF_A   = 0;                                // [hi, lo][A_BYTES]
-    static constexpr int OFF_W   = al(OFF_A + 2 * A_BYTES);          // [hi, lo][W_BYTES]
-    static constexpr int OFF_ACC = al(OFF_W + 2 * W_BYTES);          // [4 colours][2 slots][C][NPL] float
-    static constexpr int OFF_D   = al(OFF_ACC + 4 * 2 * C * NPL * 4); // [3 slots][C][NPL] float
-    static constexpr int OFF_BAR = al(OFF_D + 3 * C * NPL * 4);
+    static constexpr int OFF_W   = 0;                                  // [hi, lo][W_BYTES]
+    static constexpr int OFF_D   = al(OFF_W + 2 * W_BYTES);            // [3 slots][C][NPL] float
+    static constexpr int OFF_X   = al(OFF_D + 3 * C * NPL * 4);        // [2 parity][4 warps][C][32] float
+    static constexpr int OFF_BAR = al(OFF_X + 2 * EYN * C * 32 * 4);
     static constexpr int SMEM    = OFF_BAR + 16 + 32 * 8;
-    static_assert(SMEM <= 56 * 1024, "four CTAs per SM");
+    static_assert(NW <= COL_AH && NCOL <= COL_AL - COL_AH && NCOL <= TCOLS - COL_AL, "tensor-memory map");
+    static_assert(SMEM <= SMEM_REQ, "shared memory");
 };
 
 __device__ __forceinline__ int pmod(int i, int n)
@@ -93,7 +97,7 @@ __device__ __forceinline__ float to_tf32(float x) { return __uint_as_float(__flo
 // x in [-n, 2n): periodic index without a division
 __device__ __forceinline__ int wrap(int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 {
     uint32_t r[16];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -105,11 +109,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
         v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc)
+// this thread's lane, 8 consecutive 32-bit columns from taddr
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float *v)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+                 "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                 "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                 "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+                 : "memory");
+}
+
+// D (tmem) += A (tmem, 128 lanes x 8 columns) * B^T (smem descriptor); acc = 0 overwrites
+__device__ __forceinline__ void umma_tf32_ts(uint32_t dtmem, uint32_t atmem, uint64_t bd, uint32_t idesc, uint32_t acc)
 {
     asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-                 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(dtmem),
+                 "r"(atmem), "l"(bd), "r"(idesc), "r"(acc));
 }
 
 template <int C, int NPH>
@@ -118,8 +133,8 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     using Cfg = TcCfg<C, NPH>;
     constexpr int NCOL = Cfg::NCOL, NPF = Cfg::NPF;
     extern __shared__ __align__(16) unsigned char smem[];
-    float    *Acc       = reinterpret_cast<float *>(smem + Cfg::OFF_ACC);
     float    *Dp        = reinterpret_cast<float *>(smem + Cfg::OFF_D);
+    float    *Xch       = reinterpret_cast<float *>(smem + Cfg::OFF_X);
     uint64_t *mbar      = reinterpret_cast<uint64_t *>(smem + Cfg::OFF_BAR);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + Cfg::OFF_BAR + 8);
     double   *red_smem  = reinterpret_cast<double *>(smem + Cfg::OFF_BAR + 16);
@@ -135,8 +150,8 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     float       *yout = reinterpret_cast<float *>(a.y);
     const float  beta = (float)a.scal->beta;
 
-    // this thread's element (row ey = warp, column ez = lane), colour copy, and global (y, z)
-    const int       ey = warp, ez = lane, colour = (ey & 1) * 2 + (ez & 1);
+    // this thread's element (row ey = warp, column ez = lane) and global (y, z)
+    const int       ey = warp, ez = lane;
     const long long el_yz = (long long)pmod(y0 - 1 + ey, ny) * nz + pmod(z0 - 1 + ez, nz);
     const long long plane = (long long)ny * nz;
 
@@ -149,7 +164,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "n"(Cfg::TCOLS)
+                     "n"(TCOLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -174,11 +189,10 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
                 owned_mask |= 1u << k;
         }
     }
-    // output node of this thread (tid < 93): plane-local node and global offset without x
-    const int  oty = tid / BZ, otz = tid % BZ;
-    const bool out_ok = tid < BY * BZ && y0 + oty < ny && z0 + otz < nz;
-    const int  onode  = (oty + 1) * PZ + otz + 1;
-    const long long oyz = out_ok ? (long long)(y0 + oty) * nz + z0 + otz : 0;
+    // output node of this thread: node (ey, ez) of the halo plane, owned for ey >= 1, ez >= 1
+    const bool      out_ok = ey >= 1 && ez >= 1 && y0 - 1 + ey < ny && z0 - 1 + ez < nz;
+    const int       onode  = ey * PZ + ez;
+    const long long oyz    = out_ok ? (long long)(y0 - 1 + ey) * nz + (z0 - 1 + ez) : 0;
 
     // node plane X: thread's share of (s, d_old) into registers
     float sv[NPF], dv[NPF];
@@ -204,19 +218,19 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
                     dnew[goff[k] + gx] = v;
             }
     };
-    // node plane Xo from the four colour copies of slot so; d from node slot ds
+    // node plane Xo: this thread's near-y partial plus warp ey-1's far-y partial (exchange
+    // parity xp); d from node slot ds
+    float  pend[C];
     double dot = 0.0;
-    auto output_plane = [&](int Xo, int so, int ds) {
+    auto output_plane = [&](int Xo, int xp, int ds) {
         if (!out_ok)
             return;
         const long long gi = (long long)wrap(Xo, nx) * plane + oyz;
-        float dl = 0.f;
+        const float    *xc = Xch + ((xp * EYN + ey - 1) * C) * 32 + ez;
+        float           dl = 0.f;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            float v = 0.f;
-#pragma unroll
-            for (int w = 0; w < 4; ++w)
-                v += Acc[((w * 2 + so) * C + c) * NPL + onode];
+            const float v = pend[c] + xc[c * 32];
             yout[c * N + gi] = v;
             dl += Dp[(ds * C + c) * NPL + onode] * v;
         }
@@ -228,25 +242,29 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     store_plane(xs - 1, 0);
     load_plane(xs);
     int ph_cur = a.ms[(long long)wrap(xs - 1, nx) * plane + el_yz];
 
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Cfg::NW >> 3) << 17) | (8u << 24);
-    bool ok = true;
-    unsigned char *Ahi = smem + Cfg::OFF_A, *Alo = smem + Cfg::OFF_A + Cfg::A_BYTES;
-    const int rowoff = (tid / 8) * Cfg::SBO + (tid % 8) * 16; // A row m = tid
+    bool  ok = true;
+    float carry[4 * C]; // far-x rows (qa = 1) of this thread's element in plane X-1, [qb + 2 qc][c]
+#pragma unroll
+    for (int i = 0; i < 4 * C; ++i)
+        carry[i] = 0.f;
 
     for (int X = xs - 1; X < xe; ++X) {
         const int j = X - xs + 1; // 0 .. xe-xs
-        __syncthreads(); // S1: previous step's readers of node slot (j+1)%3 and of A are done
+        // node plane X+1 into slot (j+1)%3: its last readers (element plane X-2, output of
+        // node plane X-2) finished before the previous step's completion barrier
         store_plane(X + 1, (j + 1) % 3);
         if (X + 2 <= xe)
             load_plane(X + 2);
         const int ph_next = X + 1 < xe ? (int)a.ms[(long long)wrap(X + 1, nx) * plane + el_yz] : 0;
-        __syncthreads(); // S2: node plane X+1 ready
+        __syncthreads(); // S2: node planes X, X+1 staged; exchange of node plane X-1 visible
 
-        // element row of plane X, split hi/lo, in the core-matrix layout
+        // element row of plane X, split hi/lo, into this thread's tensor-memory lane
         {
             const float *P0 = Dp + (j % 3) * C * NPL, *P1 = Dp + ((j + 1) % 3) * C * NPL;
             float u0[C], v[NCOL];
@@ -261,48 +279,45 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
                 for (int c = 0; c < C; ++c)
                     v[q * C + c] = P[c * NPL + (ey + qb) * PZ + ez + qc] - u0[c];
             }
+            float h[NCOL], l[NCOL];
 #pragma unroll
-            for (int kc = 0; kc < Cfg::KC; ++kc) {
-                float4 h, l;
-                h.x = to_tf32(v[4 * kc + 0]);
-                h.y = to_tf32(v[4 * kc + 1]);
-                h.z = to_tf32(v[4 * kc + 2]);
-                h.w = to_tf32(v[4 * kc + 3]);
-                l.x = v[4 * kc + 0] - h.x;
-                l.y = v[4 * kc + 1] - h.y;
-                l.z = v[4 * kc + 2] - h.z;
-                l.w = v[4 * kc + 3] - h.w;
-                *reinterpret_cast<float4 *>(Ahi + rowoff + kc * Cfg::LBO) = h;
-                *reinterpret_cast<float4 *>(Alo + rowoff + kc * Cfg::LBO) = l;
+            for (int k = 0; k < NCOL; ++k) {
+                h[k] = to_tf32(v[k]);
+                l[k] = v[k] - h[k];
             }
+#pragma unroll
+            for (int k0 = 0; k0 < NCOL; k0 += 8) {
+                tmem_st8(lane_base + (uint32_t)(COL_AH + k0), h + k0);
+                tmem_st8(lane_base + (uint32_t)(COL_AL + k0), l + k0);
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads(); // S3: A of plane X visible to the tensor cores
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads(); // S3: A of plane X in tensor memory
 
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t wbase = smem_u32(smem + Cfg::OFF_W), abase = smem_u32(Ahi);
+            const uint32_t wbase = smem_u32(smem + Cfg::OFF_W);
             // 3xTF32: lo*hi + hi*lo + hi*hi (small terms first)
 #pragma unroll
             for (int s = 0; s < Cfg::KSTEPS; ++s)
-                umma_tf32(tmem, umma_desc<Cfg::SBO, Cfg::LBO>(abase + Cfg::A_BYTES + s * 256),
-                          umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, s > 0 ? 1u : 0u);
+                umma_tf32_ts(tmem, tmem + COL_AL + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc,
+                             s > 0 ? 1u : 0u);
 #pragma unroll
             for (int s = 0; s < Cfg::KSTEPS; ++s)
-                umma_tf32(tmem, umma_desc<Cfg::SBO, Cfg::LBO>(abase + s * 256),
-                          umma_desc<Cfg::SBO, Cfg::LBO>(wbase + Cfg::W_BYTES + s * 256), idesc, 1u);
+                umma_tf32_ts(tmem, tmem + COL_AH + 8 * s,
+                             umma_desc<Cfg::SBO, Cfg::LBO>(wbase + Cfg::W_BYTES + s * 256), idesc, 1u);
 #pragma unroll
             for (int s = 0; s < Cfg::KSTEPS; ++s)
-                umma_tf32(tmem, umma_desc<Cfg::SBO, Cfg::LBO>(abase + s * 256),
-                          umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, 1u);
+                umma_tf32_ts(tmem, tmem + COL_AH + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, 1u);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              smem_u32(mbar))
                          : "memory");
         }
 
-        // node plane X-1 (complete since the previous step) while the MMAs run
+        // node plane X-1 (its exchange was written before S2) while the MMAs run
         if (X - 1 >= xs)
-            output_plane(X - 1, (j + 1) & 1, (j + 2) % 3);
+            output_plane(X - 1, (X - 1) & 1, (j + 2) % 3);
 
         uint32_t done = 1;
         if (tid == 0) { // one poller; the other threads wait at the barrier below
@@ -314,43 +329,49 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
                              : "r"(smem_u32(mbar)), "r"((uint32_t)(j & 1))
                              : "memory");
         }
-        if (!__syncthreads_and(done ? 1 : 0)) { // S4: D ready; output of plane X-1 done
+        if (!__syncthreads_and(done ? 1 : 0)) { // S4: D ready; output of node plane X-1 done
             ok = false;
             break;
         }
 
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // D -> this element's phase rows -> colour copy: node plane X (+=) and X+1 (=)
         {
+            // this element's phase rows: out[q*C + c], local node q = qa + 2 qb + 4 qc
             float out[NCOL];
-            const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+            {
+                float v[Cfg::NW];
 #pragma unroll
-            for (int c0 = 0; c0 < Cfg::NW; c0 += 16) {
-                float v[16];
-                tmem_ld16(lane_base + (uint32_t)c0, v);
+                for (int c0 = 0; c0 < Cfg::NW; c0 += 16)
+                    tmem_ld16(lane_base + (uint32_t)c0, v + c0);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int jj = 0; jj < 16; ++jj) {
-                    const int col = c0 + jj;
-                    if (col < Cfg::NROW) {
-                        const int k = col / NCOL, r = col % NCOL;
-                        if (k == 0 || ph_cur == k)
-                            out[r] = v[jj];
-                    }
-                }
+                for (int r = 0; r < NCOL; ++r)
+                    out[r] = (NPH > 1 && ph_cur == 1) ? v[NCOL + r] : v[r];
             }
-            float *A0 = Acc + (colour * 2 + (j & 1)) * C * NPL, *A1 = Acc + (colour * 2 + ((j + 1) & 1)) * C * NPL;
+            // x: near-x rows plus the far-x rows carried from element plane X-1
+            float P[4 * C];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int qa = q & 1, qb = (q >> 1) & 1, qc = (q >> 2) & 1;
-                const int node = (ey + qb) * PZ + ez + qc;
+            for (int b = 0; b < 4; ++b) { // b = qb + 2 qc
+                const int q0 = 2 * b;     // qa = 0
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
-                    if (qa)
-                        A1[c * NPL + node] = out[q * C + c];
-                    else
-                        A0[c * NPL + node] += out[q * C + c];
+                    P[b * C + c]     = out[q0 * C + c] + carry[b * C + c];
+                    carry[b * C + c] = out[(q0 + 1) * C + c];
                 }
+            }
+            // z: node (ey + qb, ez) gets lane ez-1's far-z rows (qc = 1)
+            float Z[2 * C];
+#pragma unroll
+            for (int qb = 0; qb < 2; ++qb)
+#pragma unroll
+                for (int c = 0; c < C; ++c)
+                    Z[qb * C + c] = P[qb * C + c] + __shfl_up_sync(0xffffffffu, P[(qb + 2) * C + c], 1);
+            // y: far-y partial (node ey+1) to the exchange; near-y partial kept for the output
+            float *xc = Xch + ((X & 1) * EYN + ey) * C * 32 + ez;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                xc[c * 32] = Z[C + c];
+                pend[c]    = Z[c];
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -358,7 +379,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     }
     __syncthreads();
     if (ok)
-        output_plane(xe - 1, (xe - xs) & 1, (xe - xs) % 3);
+        output_plane(xe - 1, (xe - 1) & 1, (xe - xs) % 3);
     else if (tid == 0)
         a.scal->converged = -3; // tensor-core completion wait timed out
 
@@ -379,7 +400,7 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(Cfg::TCOLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TCOLS) : "memory");
 }
 
 } // namespace
@@ -425,7 +446,7 @@ cudaError_t launch_stencil_tc(const StencilArgs &a, const float *W, int nph, cud
     dim3 grid((a.g.nx + XL - 1) / XL, (a.g.ny + BY - 1) / BY, (a.g.nz + BZ - 1) / BZ);
 #define FANSGPU_TC(C_, P_)                                                                                       \
     do {                                                                                                       \
-        constexpr int sm = TcCfg<C_, P_>::SMEM;                                                                \
+        constexpr int sm = SMEM_REQ;                                                                           \
         cudaError_t   e  = allow_max_dyn_smem(k_stencil_tc<C_, P_>); \
         if (e != cudaSuccess)                                                                                  \
             return e;                                                                                          \

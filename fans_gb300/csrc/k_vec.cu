@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(UpdateArgs a)
                 crs += rv * s[i];
             }
         }
-        nrm = mx ? fmax(nrm, (double)cn) : nrm + (double)cn;
+        nrm = mx ? nan_max(nrm, (double)cn) : nrm + (double)cn;
         rs += (double)crs;
     }
     double v[2]   = {nrm, rs};
@@ -101,10 +101,10 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update_f4(UpdateArgs a)
         if (measure == 1)
             cn = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
         else if (mx)
-            cn = fmaxf(fmaxf(fabsf(rv.x), fabsf(rv.y)), fmaxf(fabsf(rv.z), fabsf(rv.w)));
+            cn = nan_maxf(nan_maxf(fabsf(rv.x), fabsf(rv.y)), nan_maxf(fabsf(rv.z), fabsf(rv.w)));
         else
             cn = fabsf(rv.x) + fabsf(rv.y) + fabsf(rv.z) + fabsf(rv.w);
-        nrm = mx ? fmax(nrm, (double)cn) : nrm + (double)cn;
+        nrm = mx ? nan_max(nrm, (double)cn) : nrm + (double)cn;
         rs += (double)(rv.x * sv.x + rv.y * sv.y + rv.z * sv.z + rv.w * sv.w);
     }
     double v[2]   = {nrm, rs};
@@ -144,10 +144,10 @@ __global__ void __launch_bounds__(kVecThreads) k_norm_fast(const T *__restrict__
         if (measure == 1)
             cn = f.x * f.x + f.y * f.y;
         else if (mx)
-            cn = fmaxf(fabsf(f.x), fabsf(f.y));
+            cn = nan_maxf(fabsf(f.x), fabsf(f.y));
         else
             cn = fabsf(f.x) + fabsf(f.y);
-        nrm = mx ? fmax(nrm, (double)cn) : nrm + (double)cn;
+        nrm = mx ? nan_max(nrm, (double)cn) : nrm + (double)cn;
     }
     double v[1]   = {nrm};
     int    ops[1] = {mx ? RED_MAX : RED_SUM};
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kVecThreads) k_norm(const T *__restrict__ r, l
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         T      v = r[i];
         double t = norm_term((double)v, measure);
-        nrm      = mx ? fmax(nrm, t) : nrm + t;
+        nrm      = mx ? nan_max(nrm, t) : nrm + t;
         if (r_out)
             r_out[i] = (TO)v;
     }

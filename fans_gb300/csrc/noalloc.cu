@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kThreads) k_norm_noalloc(const double *__restr
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const double a = fabs(r[i]);
         const double t = measure == FANSGPU_L2 ? a * a : a;
-        acc            = mx ? fmax(acc, t) : acc + t;
+        acc            = mx ? fansgpu::nan_max(acc, t) : acc + t;
     }
     double    v[1]   = {acc};
     const int ops[1] = {mx ? fansgpu::RED_MAX : fansgpu::RED_SUM};
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kThreads) k_norm_noalloc(const double *__restr
     double    s  = 0.0;
     for (int b = b0; b < b1; ++b) {
         const double t = __ldcg(&partials[b]);
-        s              = mx ? fmax(s, t) : s + t;
+        s              = mx ? fansgpu::nan_max(s, t) : s + t;
     }
     v[0] = s;
     fansgpu::block_reduce<1>(v, ops, red);

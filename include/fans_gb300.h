@@ -160,7 +160,9 @@ int fansgpu_set_phase_material(fansgpu_ctx *ctx, int32_t phase, int32_t law, con
 
 /* MaterialManager::compute_reference_stiffness (MaterialManager.h:177-205):
  * kapparef_mat (n_str x n_str, row-major).  Must be set before the first solve;
- * the host mirror computes the reference's default rule. */
+ * the host mirror computes the reference's default rule.  Small strain and
+ * thermal: symmetric positive definite (FANSGPU_EINVAL otherwise); large
+ * strain: symmetric (dP/dF at F = I is semidefinite). */
 int fansgpu_set_reference(fansgpu_ctx *ctx, const double *kapparef);
 
 /* MaterialManager::set_gradient / Matmodel::setGradient (MaterialManager.h:216-221,

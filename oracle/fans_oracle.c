@@ -19,10 +19,18 @@
  *     threshold: for the real symmetric c x c blocks used here the singular
  *     values are |eigenvalues|, computed by cyclic Jacobi rotations.
  *
- * Parity unpinned: the reference itself cannot be built or run here and its
- * tests hold no golden values, so this oracle is anchored by an independent
- * numpy restatement (oracle/numpy_ref.py), known answers (homogeneous media,
- * laminates) and the invariants the reference's own tests check.
+ * Parity pinning: the reference itself cannot be built or run here.  Its test
+ * inputs test/input_files/test_MixedBCs.json and test_MixedBCs_LargeStrain.json
+ * carry macroscopic states the reference computed on test/microstructures/
+ * sphere32.h5 (the loading of their later load cases); this oracle reproduces
+ * them (small-strain mixed BCs with PseudoPlasticLinearHardening + linear
+ * elasticity to 2.4e-9 relative, CompressibleNeoHookean at F33 = 2 to 3e-10
+ * absolute on P33 = 74.757449712464).  Laws those two files do not exercise
+ * (J2 plasticity, J2ViscoPlastic, SaintVenantKirchhoff, thermal, triclinic,
+ * HEX8R/BBAR) are anchored by an independent numpy restatement
+ * (oracle/numpy_ref.py), known answers (homogeneous media, laminates, strain
+ * energy derivatives) and the invariants the reference's own tests check; for
+ * those, parity is unpinned.
  *
  * Layouts follow the reference: nodal fields are [x][y][z][c] (c fastest,
  * solver.h:123-127 without the FFTW z padding), the microstructure is
@@ -45,7 +53,15 @@
 
 enum { FO_HEX8 = 0, FO_HEX8R = 1, FO_BBAR = 2 };
 enum { FO_LAW_THERMAL_ISO = 0, FO_LAW_ELASTIC_ISO = 1, FO_LAW_J2 = 2, FO_LAW_THERMAL_TRI = 3, FO_LAW_ELASTIC_TRI = 4,
-       FO_LAW_PSEUDO_LIN = 5, FO_LAW_PSEUDO_NL = 6, FO_LAW_J2VISCO_LIN = 7, FO_LAW_J2VISCO_NL = 8 };
+       FO_LAW_PSEUDO_LIN = 5, FO_LAW_PSEUDO_NL = 6, FO_LAW_J2VISCO_LIN = 7, FO_LAW_J2VISCO_NL = 8,
+       FO_LAW_SVK = 9, FO_LAW_NEOHOOKEAN = 10 };
+
+/* Strain measure of mechanical problems: 0 small strain <3,6> (Mandel), 1 large
+ * strain <3,9> (deformation gradient, row-major F_iJ at 3i + J; main.cpp:64-77).
+ * Set before building B and before calls that evaluate the laws. */
+static int g_large = 0;
+FO_API void fo_set_large_strain(int on) { g_large = on ? 1 : 0; }
+static int nstr_of(int c) { return c == 1 ? 3 : (g_large ? 9 : 6); }
 
 /* Kinematic-hardening internal variable psi_bar of J2ViscoPlastic [N][ngp][6]
  * (committed and trial), bound before calls that evaluate the laws. */
@@ -103,6 +119,14 @@ static void model_B(int c, double x, double y, double z, const double le[3], dou
 {
     double b[3][8];
     basic_B(x, y, z, le, b);
+    if (c == 3 && g_large) { /* LargeStrainMechModel::Compute_B (LargeStrainMechModel.h:209-225) */
+        memset(out, 0, sizeof(double) * 9 * 24);
+        for (int i = 0; i < 3; ++i)
+            for (int J = 0; J < 3; ++J)
+                for (int q = 0; q < 8; ++q)
+                    out[(3 * i + J) * 24 + 3 * q + i] = b[J][q];
+        return;
+    }
     if (c == 1) {
         for (int i = 0; i < 3; ++i)
             for (int q = 0; q < 8; ++q)
@@ -128,7 +152,7 @@ static void model_B(int c, double x, double y, double z, const double le[3], dou
  * Returns n_gp; B is n_gp blocks of nstr x 8c (row-major). */
 FO_API int fo_build_B(int fe_type, int c, const double le[3], double *B)
 {
-    const int nstr = (c == 1) ? 3 : 6;
+    const int nstr = nstr_of(c);
     const int ncol = 8 * c;
     if (fe_type == FO_HEX8R) {
         model_B(c, 0.5, 0.5, 0.5, le, B);
@@ -139,7 +163,7 @@ FO_API int fo_build_B(int fe_type, int c, const double le[3], double *B)
     const double xi[8][3] = {{xi_m, xi_m, xi_m}, {xi_p, xi_m, xi_m}, {xi_m, xi_p, xi_m}, {xi_p, xi_p, xi_m},
                              {xi_m, xi_m, xi_p}, {xi_p, xi_m, xi_p}, {xi_m, xi_p, xi_p}, {xi_p, xi_p, xi_p}};
     if (fe_type == FO_BBAR && nstr > 3) {
-        double Bvol[6 * 24], Bfull[6 * 24];
+        double Bvol[9 * 24], Bfull[9 * 24];
         model_B(c, 0.5, 0.5, 0.5, le, Bvol);
         for (int p = 0; p < 8; ++p) {
             model_B(c, xi[p][0], xi[p][1], xi[p][2], le, Bfull);
@@ -164,9 +188,9 @@ FO_API int fo_build_B(int fe_type, int c, const double le[3], double *B)
  * LinearElastic.h:37-39, LinearThermal.h:189-191, matmodel.h:243-245. */
 FO_API void fo_element_stiffness(int c, int ngp, const double *B, const double *C, double ve, double *K)
 {
-    const int nstr = (c == 1) ? 3 : 6, ncol = 8 * c;
+    const int nstr = nstr_of(c), ncol = 8 * c;
     memset(K, 0, sizeof(double) * ncol * ncol);
-    double CB[6 * 24];
+    double CB[9 * 24];
     for (int p = 0; p < ngp; ++p) {
         const double *Bp = B + (size_t)p * nstr * ncol;
         for (int i = 0; i < nstr; ++i)
@@ -699,6 +723,69 @@ static void law_sigma(const fo_problem *P, int phase, size_t elem, int gp, const
         P->q[gi] += gam * c23;
         break;
     }
+    case FO_LAW_SVK:
+    case FO_LAW_NEOHOOKEAN: {
+        /* LargeStrainMechModel::get_sigma (LargeStrainMechModel.h:190-196): P = F S with
+         * SaintVenantKirchhoff S = lambda tr(E) I + 2 mu E, E = (F^T F - I)/2 (SaintVenantKirchhoff.h:36-41)
+         * or CompressibleNeoHookean S = lambda log(J) C^-1 + mu (I - C^-1) (CompressibleNeoHookean.h:36-49);
+         * param = {K, G}, lambda = K - 2G/3, mu = G.  det F <= 0 (the reference throws) gives NaN. */
+        const double mu = pr[1], lam = pr[0] - (2.0 / 3.0) * mu;
+        const double *F = eps;
+        double Cm[3][3], S[3][3];
+        for (int I = 0; I < 3; ++I)
+            for (int J = 0; J < 3; ++J) {
+                double a = 0.0;
+                for (int k = 0; k < 3; ++k)
+                    a += F[3 * k + I] * F[3 * k + J];
+                Cm[I][J] = a;
+            }
+        if (P->law[phase] == FO_LAW_SVK) {
+            double E[3][3], trE = 0.0;
+            for (int I = 0; I < 3; ++I)
+                for (int J = 0; J < 3; ++J)
+                    E[I][J] = 0.5 * (Cm[I][J] - (I == J ? 1.0 : 0.0));
+            trE = E[0][0] + E[1][1] + E[2][2];
+            for (int I = 0; I < 3; ++I)
+                for (int J = 0; J < 3; ++J)
+                    S[I][J] = (I == J ? lam * trE : 0.0) + 2.0 * mu * E[I][J];
+        } else {
+            const double J = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+                             F[2] * (F[3] * F[7] - F[4] * F[6]);
+            /* C^-1 by Gauss-Jordan elimination with partial pivoting */
+            double A[3][6];
+            for (int I = 0; I < 3; ++I)
+                for (int K = 0; K < 6; ++K)
+                    A[I][K] = K < 3 ? Cm[I][K] : (K - 3 == I ? 1.0 : 0.0);
+            for (int col = 0; col < 3; ++col) {
+                int piv = col;
+                for (int r2 = col + 1; r2 < 3; ++r2)
+                    if (fabs(A[r2][col]) > fabs(A[piv][col]))
+                        piv = r2;
+                for (int K = 0; K < 6; ++K) {
+                    const double t = A[col][K];
+                    A[col][K] = A[piv][K];
+                    A[piv][K] = t;
+                }
+                const double d = A[col][col];
+                for (int K = 0; K < 6; ++K)
+                    A[col][K] /= d;
+                for (int r2 = 0; r2 < 3; ++r2)
+                    if (r2 != col) {
+                        const double f = A[r2][col];
+                        for (int K = 0; K < 6; ++K)
+                            A[r2][K] -= f * A[col][K];
+                    }
+            }
+            const double logJ = J > 0.0 ? log(J) : NAN;
+            for (int I = 0; I < 3; ++I)
+                for (int K = 0; K < 3; ++K)
+                    S[I][K] = lam * logJ * A[I][3 + K] + mu * ((I == K ? 1.0 : 0.0) - A[I][3 + K]);
+        }
+        for (int i = 0; i < 3; ++i)
+            for (int J = 0; J < 3; ++J)
+                sig[3 * i + J] = F[3 * i] * S[0][J] + F[3 * i + 1] * S[1][J] + F[3 * i + 2] * S[2][J];
+        break;
+    }
     case FO_LAW_J2: {
         const double Kb = pr[0], G = pr[1], sy0 = pr[2], h = pr[3];
         const double c23 = sqrt(2.0 / 3.0);
@@ -790,7 +877,7 @@ static void elem_residual(const void *vctx, int x, int y, int z, const size_t id
     const res_ctx    *rc = (const res_ctx *)vctx;
     const fo_problem *P  = rc->P;
     const int         c = P->c, nstr = P->nstr, ncol = 8 * c;
-    double            ue[24], eps[6], sig[8 * 6];
+    double            ue[24], eps[9], sig[8 * 9];
     for (int i = 0; i < 8; ++i)
         for (int j = 0; j < c; ++j)
             ue[c * i + j] = rc->u[c * idx[i] + j] - rc->u[c * idx[0] + j];
@@ -847,7 +934,7 @@ static void fill_problem(fo_problem *P, int nx, int ny, int nz, int c, int ngp, 
                          const uint16_t *ms, int nphase, const int *law, const double *param, const double *g0,
                          const double *ep_t, const double *q_t, double *ep, double *q)
 {
-    P->nx = nx; P->ny = ny; P->nz = nz; P->c = c; P->nstr = (c == 1) ? 3 : 6; P->ngp = ngp;
+    P->nx = nx; P->ny = ny; P->nz = nz; P->c = c; P->nstr = nstr_of(c); P->ngp = ngp;
     P->ve = ve; P->B = B; P->ms = ms; P->nphase = nphase; P->law = law; P->param = param; P->g0 = g0;
     P->ep_t = ep_t; P->q_t = q_t; P->ep = ep; P->q = q;
 }
@@ -892,7 +979,7 @@ FO_API void fo_strain_stress(int nx, int ny, int nz, int c, int ngp, double ve, 
     for (int x = 0; x < nx; ++x) {
         double *acc = plane + (size_t)x * W;
         size_t  idx[8];
-        double  ue[24], eps[6], sig[6];
+        double  ue[24], eps[9], sig[9];
         for (int y = 0; y < ny; ++y)
             for (int z = 0; z < nz; ++z) {
                 elem_nodes(nx, ny, nz, x, y, z, idx);
@@ -900,7 +987,7 @@ FO_API void fo_strain_stress(int nx, int ny, int nz, int c, int ngp, double ve, 
                     for (int j = 0; j < c; ++j)
                         ue[c * i + j] = u[c * idx[i] + j];
                 const int phase = ms[idx[0]];
-                double    es[6] = {0}, ss[6] = {0};
+                double    es[9] = {0}, ss[9] = {0};
                 for (int gp = 0; gp < ngp; ++gp) {
                     const double *Bp = B + (size_t)gp * nstr * ncol;
                     for (int i = 0; i < nstr; ++i) {

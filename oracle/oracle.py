@@ -6,13 +6,18 @@ TEST INFRASTRUCTURE ONLY.  This module is the checker for the CUDA product.
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
 arm may import it; the product package never does.
 
-Parity unpinned: the reference (FANS v0.6.2) cannot be built in this image (MPI,
-FFTW3-MPI, parallel HDF5, Eigen and nlohmann_json are absent) and its own
-tests hold no golden numbers, only invariants.  The oracle is therefore pinned
-by (1) an independent numpy restatement (numpy.fft / LAPACK eigh) of the same
-reference lines, (2) known answers (homogeneous media, laminates), and (3) the
-reference tests' invariants evaluated on the reference fixture
-test/microstructures/sphere32.h5.
+Parity pinning: the reference (FANS v0.6.2) cannot be built in this image (MPI,
+FFTW3-MPI, parallel HDF5, Eigen and nlohmann_json are absent).  Its test inputs
+test/input_files/test_MixedBCs.json and test_MixedBCs_LargeStrain.json carry
+macroscopic states the reference computed on test/microstructures/sphere32.h5
+(the loading of their later load cases), and the oracle reproduces them
+(tests/test_oracle_reference_pins.py): small-strain mixed BCs with
+PseudoPlasticLinearHardening + linear elasticity, and CompressibleNeoHookean
+at large strain.  Everything else is anchored by (1) an independent numpy
+restatement (numpy.fft / LAPACK eigh) of the same reference lines, (2) known
+answers (homogeneous media, laminates, strain-energy derivatives), and (3) the
+reference tests' invariants on sphere32 -- for the laws the two files do not
+exercise, parity is unpinned.
 """
 from __future__ import annotations
 
@@ -30,7 +35,9 @@ FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
 LAW_THERMAL_ISO, LAW_ELASTIC_ISO, LAW_J2, LAW_THERMAL_TRI, LAW_ELASTIC_TRI = 0, 1, 2, 3, 4
 LAW_PSEUDO_LIN, LAW_PSEUDO_NL = 5, 6
 LAW_J2VISCO_LIN, LAW_J2VISCO_NL = 7, 8
-NONLINEAR_LAWS = (LAW_J2, LAW_PSEUDO_LIN, LAW_PSEUDO_NL, LAW_J2VISCO_LIN, LAW_J2VISCO_NL)
+LAW_SVK, LAW_NEOHOOKEAN = 9, 10
+LARGE_STRAIN_LAWS = (LAW_SVK, LAW_NEOHOOKEAN)
+NONLINEAR_LAWS = (LAW_J2, LAW_PSEUDO_LIN, LAW_PSEUDO_NL, LAW_J2VISCO_LIN, LAW_J2VISCO_NL) + LARGE_STRAIN_LAWS
 L1, L2, LINF = 0, 1, 2
 ABS, REL = 0, 1
 MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}
@@ -69,6 +76,8 @@ _lp = ctypes.POINTER(ctypes.c_long)
 def _declare(L):
     L.fo_bind_kinematic.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     L.fo_bind_kinematic.restype = None
+    L.fo_set_large_strain.argtypes = [ctypes.c_int]
+    L.fo_set_large_strain.restype = None
     i, d, sz = ctypes.c_int, ctypes.c_double, ctypes.c_size_t
     L.fo_build_B.argtypes = [i, i, _dp, _dp]
     L.fo_build_B.restype = i
@@ -111,7 +120,50 @@ def iso_elastic_C(K, G):
     return C
 
 
+_MANDEL_PAIRS = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+
+
+def spatial_tangent(F, S, Cm):
+    """LargeStrainMechModel::compute_spatial_tangent (LargeStrainMechModel.h:96-170):
+    A[3i+J, 3k+L] = d_ik S_LJ + sum_M F_iM sum_{P<=Q} C_MJPQ (F_kP d_QL + F_kQ d_PL)/2,
+    C_MJPQ read from the 6x6 Mandel tangent with its sqrt(2) shear factors divided out."""
+    def mandel(a, b):
+        return next(i for i, (x, y) in enumerate(_MANDEL_PAIRS) if (x, y) in ((a, b), (b, a)))
+
+    A = np.zeros((9, 9))
+    for i in range(3):
+        for J in range(3):
+            for k in range(3):
+                for L in range(3):
+                    v = S[L, J] if i == k else 0.0
+                    for M in range(3):
+                        mj = mandel(M, J)
+                        for P in range(3):
+                            for Q in range(P, 3):
+                                pq = mandel(P, Q)
+                                c = Cm[mj, pq] / (np.sqrt(2.0) if mj >= 3 else 1.0) / (np.sqrt(2.0) if pq >= 3 else 1.0)
+                                dE = (0.5 * F[k, P] if Q == L else 0.0) + (0.5 * F[k, Q] if P == L else 0.0)
+                                v += F[i, M] * c * dE
+                    A[3 * i + J, 3 * k + L] = v
+    return A
+
+
+def large_strain_tangent_at_identity(law, params):
+    """get_reference_stiffness of one phase of SaintVenantKirchhoff
+    (SaintVenantKirchhoff.h:61-80) or CompressibleNeoHookean
+    (CompressibleNeoHookean.h:108-121): both have S = 0 and the Mandel tangent
+    lambda 1 1^T + 2 mu I at F = I (CompressibleNeoHookean.h:52-104 with C^-1 = I)."""
+    K, G = float(params[0]), float(params[1])
+    lam, mu = K - 2.0 / 3.0 * G, G
+    Cm = np.zeros((6, 6))
+    Cm[:3, :3] = lam
+    Cm += 2.0 * mu * np.eye(6)
+    return spatial_tangent(np.eye(3), np.zeros((3, 3)), Cm)
+
+
 def law_C(law, params):
+    if law in LARGE_STRAIN_LAWS:
+        return large_strain_tangent_at_identity(law, params)
     if law == LAW_THERMAL_ISO:
         return params[0] * np.eye(3)
     if law in (LAW_ELASTIC_ISO,) + NONLINEAR_LAWS:
@@ -142,6 +194,8 @@ def model_reference_stiffness(law, phase_params):
         C[:3, :3] = lr
         C += 2 * mr * np.eye(6)
         return C
+    if law in LARGE_STRAIN_LAWS:
+        return np.mean([large_strain_tangent_at_identity(law, p) for p in pp], axis=0)
     if law in NONLINEAR_LAWS:  # J2PlasticityNew.h:111-121, PseudoPlastic.h:41-51
         Kb = np.mean([p[0] for p in pp])
         Gb = np.mean([p[1] for p in pp])
@@ -158,16 +212,18 @@ class OracleProblem:
     groups: list of (law, [phase ids], [per-phase parameter vectors]) in the
     order of the JSON 'materials' array."""
 
-    def __init__(self, ms, L, c, groups, fe_type="HEX8", kapparef=None):
+    def __init__(self, ms, L, c, groups, fe_type="HEX8", kapparef=None, strain_type="small"):
         self.ms = np.ascontiguousarray(ms, dtype=np.uint16)
         self.nx, self.ny, self.nz = self.ms.shape
         self.c = c
-        self.nstr = 3 if c == 1 else 6
+        self.large = c == 3 and strain_type == "large"
+        self.nstr = 3 if c == 1 else (9 if self.large else 6)
+        lib().fo_set_large_strain(int(self.large))
         self.fe = FE_TYPES[fe_type] if isinstance(fe_type, str) else fe_type
         self.L = np.asarray(L, dtype=float)
         self.le = np.array([self.L[0] / self.nx, self.L[1] / self.ny, self.L[2] / self.nz])
         self.ve = float(self.le[0] * self.le[1] * self.le[2])
-        B = np.zeros(8 * 6 * 24)
+        B = np.zeros(8 * 9 * 24)
         self.ngp = lib().fo_build_B(self.fe, c, _p(self.le), _p(B))
         self.B = np.ascontiguousarray(B[: self.ngp * self.nstr * 8 * c])
         nphase = 1 + max(max(ph) for _, ph, _ in groups)
@@ -219,6 +275,7 @@ class OracleProblem:
 
     def _common(self):
         lib().fo_bind_kinematic(_p(self.pb_t), _p(self.pb))
+        lib().fo_set_large_strain(int(self.large))
         return (self.nx, self.ny, self.nz, self.c, self.ngp, self.ve, _p(self.B), _p(self.ms, _u16p), self.nphase,
                 _p(self.law, _ip), _p(self.param), _p(self.g0), _p(self.ep_t), _p(self.q_t), _p(self.ep),
                 _p(self.q))
@@ -272,8 +329,8 @@ class OracleProblem:
         C0 = np.asarray(self.kapparef, dtype=float)
         self.mbc_M = np.linalg.pinv(C0[np.ix_(self.idx_F, self.idx_F)]) if self.idx_F else np.zeros((0, 0))
         g0 = np.asarray(self.g0, dtype=float).copy()
-        if step == 0:
-            g0 = np.zeros(self.nstr)
+        if step == 0:  # large strain starts from F = I (mixedBCs.h:192-201)
+            g0 = np.eye(3).ravel() if self.nstr == 9 else np.zeros(self.nstr)
             self.g0_prev = g0.copy()
         else:
             delta = g0 - self.g0_prev

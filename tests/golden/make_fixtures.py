@@ -4,9 +4,14 @@
   test/microstructures/sphere32.h5, decoded by fans_gb300.h5 (chunked, deflate)
   and put in [x][y][z] order as Reader::ReadMS does (ZYX on disk, reader.h:54);
   sphere32.json records the source file's SHA-256, shape and volume fraction.
-* reference_inputs.json -- the solver and material settings of the reference's
-  test/input_files/test_LinearElastic.json and test_LinearThermal.json (the
-  problem definitions its pytest suite runs on sphere32).
+* reference_inputs.json -- the solver, material and loading settings of the
+  reference's test/input_files/*.json (the problem definitions its pytest suite
+  runs on sphere32).  test_MixedBCs.json and test_MixedBCs_LargeStrain.json
+  carry reference outputs inside their loading: their later load cases are
+  loaded with the macroscopic strain / stress the first load case reached
+  (hydrostatic strain -2.01177817616389e-4 at stress -0.05; F11 = F22 =
+  0.832542244829 and P33 = 74.757449712464 at F33 = 2 on CompressibleNeoHookean),
+  which pins the oracle and the GPU path to numbers the reference computed.
 
 Run from the repository root with the reference checkout at REF (default
 /root/reference):  python tests/golden/make_fixtures.py [REF]
@@ -38,7 +43,8 @@ def main():
     with open(os.path.join(HERE, "sphere32.json"), "w") as f:
         json.dump(meta, f, indent=1)
     inputs = {}
-    for name in ("test_LinearElastic", "test_LinearThermal"):
+    for name in ("test_LinearElastic", "test_LinearThermal", "test_MixedBCs", "test_MixedBCs_LargeStrain",
+                 "test_CompressibleNeoHookean", "test_J2Plasticity", "test_PseudoPlastic"):
         with open(os.path.join(REF, "test", "input_files", name + ".json")) as f:
             j = json.load(f)
         inputs[name] = {k: j[k] for k in KEEP if k in j}

@@ -19,8 +19,8 @@ def random_ms(shape, vf=0.3, seed=0, nphase=2):
     return rng.integers(0, nphase, size=shape).astype(np.uint16)
 
 
-def oracle_problem(ms, c, groups, fe="HEX8", L=(1.0, 1.0, 1.0), kapparef=None):
-    return O.OracleProblem(ms, L, c, groups, fe, kapparef=kapparef)
+def oracle_problem(ms, c, groups, fe="HEX8", L=(1.0, 1.0, 1.0), kapparef=None, strain_type="small"):
+    return O.OracleProblem(ms, L, c, groups, fe, kapparef=kapparef, strain_type=strain_type)
 
 
 def gpu_context(P, precision="fp64", method="cg"):
@@ -28,10 +28,11 @@ def gpu_context(P, precision="fp64", method="cg"):
     from fans_gb300 import Context
 
     fe = {O.HEX8: "HEX8", O.HEX8R: "HEX8R", O.BBAR: "BBAR"}[P.fe]
-    ctx = Context((P.nx, P.ny, P.nz), tuple(P.L), P.c, fe, precision, method)
+    ctx = Context((P.nx, P.ny, P.nz), tuple(P.L), P.c, fe, precision, method, "large" if P.large else "small")
     ctx.set_microstructure(P.ms)
     nparams = {O.LAW_THERMAL_ISO: 1, O.LAW_ELASTIC_ISO: 2, O.LAW_J2: 4, O.LAW_THERMAL_TRI: 9, O.LAW_ELASTIC_TRI: 36,
-               O.LAW_PSEUDO_LIN: 4, O.LAW_PSEUDO_NL: 5, O.LAW_J2VISCO_LIN: 7, O.LAW_J2VISCO_NL: 9}
+               O.LAW_PSEUDO_LIN: 4, O.LAW_PSEUDO_NL: 5, O.LAW_J2VISCO_LIN: 7, O.LAW_J2VISCO_NL: 9,
+               O.LAW_SVK: 2, O.LAW_NEOHOOKEAN: 2}
     for ph in range(P.nphase):
         law = int(P.law[ph])
         ctx.set_phase_material(ph, law, P.param[ph, : nparams[law]])
