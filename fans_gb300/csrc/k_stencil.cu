@@ -647,13 +647,23 @@ cudaError_t launch_residual_df(const StencilArgs &a, cudaStream_t st)
 }
 
 // Per-phase sums of the element strain (centre gradient + g0) and element
-// counts: out[ph*NSTR + i], out[NPHM*NSTR + ph].  With linear laws the stress
-// sums follow on the host as C_ph times the strain sums (matmodel.h:203-225 by
-// linearity), so the averages need no per-element stress.
-template <int C, int NSTR, int NPHM>
+// counts for at most two phases: out[ph*NSTR + i], out[2*NSTR + ph].  With
+// linear laws the stress sums follow on the host as C_ph times the strain sums
+// (matmodel.h:203-225 by linearity), so the averages need no per-element stress.
+//
+// The element strain average is the centre gradient of u (the Gauss-point mean
+// of B for HEX8, HEX8R and BBAR): du_c/dx_d = (sum of u_c over the element's
+// four far-d corners - the four near-d corners) / (4 l_d).  Summed over the
+// phase-0 elements this is sum_n u_c(n) w_d(n) / (4 l_d), where w_d(n) =
+// (# phase-0 elements having n as a far-d corner) - (# having it as a near-d
+// corner) is an integer in [-4, 4] read from the 8 elements around node n.  Over
+// all elements the sum vanishes (periodicity), so phase 1 carries minus phase 0.
+// One thread per node: 3C FP64 FMAs instead of ~30C FP64 operations per
+// element -- FP64 is the scarce pipe on this part.
+template <int C, int NSTR>
 __global__ void __launch_bounds__(256) k_strain_sums(StrainStressArgs a)
 {
-    constexpr int NV = NPHM * (NSTR + 1);
+    constexpr int NV = 3 * C + 1; // sum_n u_c w_d at c*3 + d, then the phase-0 element count
     static_assert(NV <= kMaxRed, "reduction partial slots");
     __shared__ double red_smem[32 * NV];
     const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
@@ -662,44 +672,31 @@ __global__ void __launch_bounds__(256) k_strain_sums(StrainStressArgs a)
 #pragma unroll
     for (int i = 0; i < NV; ++i)
         acc[i] = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N; e += (long long)gridDim.x * blockDim.x) {
-        const int z = (int)(e % nz), y = (int)((e / nz) % ny), x = (int)(e / ((long long)nz * ny));
-        const int ph = a.ms[e];
-        const int x1 = x + 1 == nx ? 0 : x + 1, y1 = y + 1 == ny ? 0 : y + 1, z1 = z + 1 == nz ? 0 : z + 1;
-        const long long i0 = ((long long)x * ny + y) * nz, i1 = ((long long)x1 * ny + y) * nz;
-        const long long i2 = ((long long)x * ny + y1) * nz, i3 = ((long long)x1 * ny + y1) * nz;
-        double g[C][3];
+    for (int row = blockIdx.x; row < nx * ny; row += gridDim.x) {
+        const int x = row / ny, y = row % ny;
+        const int xm = x == 0 ? nx - 1 : x - 1, ym = y == 0 ? ny - 1 : y - 1;
+        const long long r00 = ((long long)x * ny + y) * nz, r10 = ((long long)xm * ny + y) * nz;
+        const long long r01 = ((long long)x * ny + ym) * nz, r11 = ((long long)xm * ny + ym) * nz;
+        for (int z = threadIdx.x; z < nz; z += blockDim.x) {
+            const int zm = z == 0 ? nz - 1 : z - 1;
+            // element with origin node - (a, b, c): node n is its corner (a, b, c)
+            const int p000 = a.ms[r00 + z] == 0, p001 = a.ms[r00 + zm] == 0;
+            const int p010 = a.ms[r01 + z] == 0, p011 = a.ms[r01 + zm] == 0;
+            const int p100 = a.ms[r10 + z] == 0, p101 = a.ms[r10 + zm] == 0;
+            const int p110 = a.ms[r11 + z] == 0, p111 = a.ms[r11 + zm] == 0;
+            const int far_x = p100 + p101 + p110 + p111, near_x = p000 + p001 + p010 + p011;
+            const int far_y = p010 + p011 + p110 + p111, near_y = p000 + p001 + p100 + p101;
+            const int far_z = p001 + p011 + p101 + p111, near_z = p000 + p010 + p100 + p110;
+            const double w[3] = {(double)(far_x - near_x), (double)(far_y - near_y), (double)(far_z - near_z)};
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const double *u = a.u + c * N;
-            const double u0 = u[i0 + z], u1 = u[i1 + z], u2 = u[i2 + z], u3 = u[i3 + z];
-            const double u4 = u[i0 + z1], u5 = u[i1 + z1], u6 = u[i2 + z1], u7 = u[i3 + z1];
-            g[c][0] = ((u1 - u0) + (u3 - u2) + (u5 - u4) + (u7 - u6)) * a.inv4l[0];
-            g[c][1] = ((u2 - u0) + (u3 - u1) + (u6 - u4) + (u7 - u5)) * a.inv4l[1];
-            g[c][2] = ((u4 - u0) + (u5 - u1) + (u6 - u2) + (u7 - u3)) * a.inv4l[2];
-        }
-        double eps[NSTR];
-        if (C == 1) {
+            for (int c = 0; c < C; ++c) {
+                const double u = a.u[c * N + r00 + z];
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
-                eps[i] = g[0][i];
-        } else {
-            const double sh = 7.071067811865476e-01;
-            eps[0] = g[0][0];
-            eps[1] = g[C > 1 ? 1 : 0][1];
-            eps[2] = g[C > 2 ? 2 : 0][2];
-            eps[3] = sh * (g[0][1] + g[C > 1 ? 1 : 0][0]);
-            eps[4] = sh * (g[0][2] + g[C > 2 ? 2 : 0][0]);
-            eps[5] = sh * (g[C > 1 ? 1 : 0][2] + g[C > 2 ? 2 : 0][1]);
-        }
-#pragma unroll
-        for (int k = 0; k < NPHM; ++k)
-            if (ph == k) {
-#pragma unroll
-                for (int i = 0; i < NSTR; ++i)
-                    acc[k * NSTR + i] += eps[i] + a.g0[i];
-                acc[NPHM * NSTR + k] += 1.0;
+                for (int d = 0; d < 3; ++d)
+                    acc[c * 3 + d] = fma(w[d], u, acc[c * 3 + d]);
             }
+            acc[3 * C] += (double)p000;
+        }
     }
     int ops[NV];
 #pragma unroll
@@ -708,21 +705,45 @@ __global__ void __launch_bounds__(256) k_strain_sums(StrainStressArgs a)
     block_reduce<NV>(acc, ops, red_smem);
     if (grid_partial_commit<NV>(acc, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
         grid_final<NV>(acc, ops, a.red.partials, gridDim.x, red_smem);
-        if (threadIdx.x == 0)
-            for (int i = 0; i < NV; ++i)
-                a.out_red[i] = acc[i];
+        if (threadIdx.x == 0) {
+            double G[C][3]; // sum over phase-0 elements of du_c/dx_d
+            for (int c = 0; c < C; ++c)
+                for (int d = 0; d < 3; ++d)
+                    G[c][d] = acc[c * 3 + d] * a.inv4l[d];
+            double sgrad[NSTR];
+            if (C == 1) {
+                for (int i = 0; i < 3; ++i)
+                    sgrad[i] = G[0][i];
+            } else {
+                const double sh = 7.071067811865476e-01;
+                sgrad[0] = G[0][0];
+                sgrad[1] = G[C > 1 ? 1 : 0][1];
+                sgrad[2] = G[C > 2 ? 2 : 0][2];
+                sgrad[3] = sh * (G[0][1] + G[C > 1 ? 1 : 0][0]);
+                sgrad[4] = sh * (G[0][2] + G[C > 2 ? 2 : 0][0]);
+                sgrad[5] = sh * (G[C > 1 ? 1 : 0][2] + G[C > 2 ? 2 : 0][1]);
+            }
+            const double n0 = acc[3 * C], n1 = (double)N - n0;
+            for (int i = 0; i < NSTR; ++i) {
+                a.out_red[i]        = sgrad[i] + n0 * a.g0[i];
+                a.out_red[NSTR + i] = -sgrad[i] + n1 * a.g0[i];
+            }
+            a.out_red[2 * NSTR]     = n0;
+            a.out_red[2 * NSTR + 1] = n1;
+        }
     }
 }
 
 cudaError_t launch_strain_sums(const StrainStressArgs &a, cudaStream_t st)
 {
-    const int nb = grid_blocks_for(a.g.N());
+    const long long rows = (long long)a.g.nx * a.g.ny;
+    const int       nb   = (int)(rows < 152 * 8 ? rows : 152 * 8);
     if (a.nph > 2)
         return cudaErrorInvalidValue;
     if (a.C == 1)
-        k_strain_sums<1, 3, 2><<<nb, 256, 0, st>>>(a);
+        k_strain_sums<1, 3><<<nb, 256, 0, st>>>(a);
     else
-        k_strain_sums<3, 6, 2><<<nb, 256, 0, st>>>(a);
+        k_strain_sums<3, 6><<<nb, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

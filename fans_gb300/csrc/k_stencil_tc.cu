@@ -26,7 +26,7 @@
 //   y: the far-y partial goes through a small shared exchange buffer and warp
 //      ey+1 adds it when it writes the node.
 // Every node is therefore a fixed-order sum (deterministic).  About 12 KB of
-// shared memory is used; 56 KB is requested so that at most four CTAs share an
+// shared memory is used; 48 KB is requested so that exactly four CTAs share an
 // SM, which is what their 4 x 128 tensor-memory columns allow.
 #include "kernels.cuh"
 
@@ -45,7 +45,9 @@ constexpr int NPL = PY * PZ;              // 165 nodes per plane incl. halo
 constexpr int XL  = 32;                   // planes per CTA
 constexpr int TCOLS  = 128;               // tensor memory: D [0, 64), A hi [64, 96), A lo [96, 128)
 constexpr int COL_AH = 64, COL_AL = 96;
-constexpr int SMEM_REQ = 56 * 1024;       // caps residency at 4 CTAs per SM (4 x 128 TMEM columns)
+// dynamic shared memory requested: with the 1 KB the driver reserves per block, 4 CTAs fit in an
+// SM's 228 KB and 5 do not -- residency is capped at the 4 x 128 tensor-memory columns an SM has
+constexpr int SMEM_REQ = 48 * 1024;
 constexpr unsigned kWaitLimit = 1u << 24; // bounded mbarrier wait
 static_assert(NEL == 128 && EYN == 4 && EZN == 32, "one M-tile per element plane, one warp per element row");
 

@@ -77,7 +77,7 @@ cudaError_t launch_strain_sums(const StrainStressArgs &a, cudaStream_t st);
 
 // ---------------------------------------------- tensor-core CG operator ---
 // FP32 fused d = s + beta d_old, K d and <d, K d> with the element matvecs on
-// tcgen05 (3xTF32); needs ny % 8 == 0, nz % 32 == 0 and at most 2 phases.
+// tcgen05 (3xTF32); at most 2 phases.
 bool        stencil_tc_supported(const Grid3 &g, int C, int nph);
 size_t      stencil_tc_weights(int C, int nph); // floats of the packed W (hi + lo)
 void        stencil_tc_pack_weights(int C, int nph, const float *K32, float *out);
