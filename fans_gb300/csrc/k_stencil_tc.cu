@@ -8,26 +8,29 @@
 // runs as tcgen05.mma kind::tf32 (M = 128 elements, N = 8C x phases, K = 8C)
 // with both operands split hi + lo (hi = the top 11 significant bits, lo = the
 // exact FP32 remainder; 3xTF32: lo*hi + hi*lo + hi*hi), which keeps the product
-// at FP32 accuracy.  A (the element rows) is written by each thread straight
-// into its tensor-memory lane with tcgen05.st; W sits in shared memory; D
-// accumulates in tensor memory.
+// at FP32 accuracy.  A (the element rows) is written straight into tensor memory
+// with tcgen05.st; W sits in shared memory; D accumulates in tensor memory.
 //
 // A CTA owns a 3 (y) x 31 (z) column of nodes, whose element plane is exactly
-// one M-tile (4 x 32 = 128 elements; warp w holds element row ey = w, lane l
-// element ez = l) and marches along x over XL planes.  Per step it stages node
-// plane X+1 (d = s + beta d_old from registers prefetched one step earlier;
-// written to d_new for owned nodes), builds the element rows of plane X into
-// tensor memory, issues the 9 MMAs, writes node plane X-1 (K d and <d, K d>)
-// while the tensor cores run, then reads its element's phase columns of D and
-// sums them into nodes without shared-memory atomics or colour copies:
-//   x: the rows of the element's far-x nodes are carried in registers to the
-//      next plane, where the same thread adds its near-x rows;
-//   z: one warp shuffle adds lane ez-1's far-z rows;
-//   y: the far-y partial goes through a small shared exchange buffer and warp
-//      ey+1 adds it when it writes the node.
-// Every node is therefore a fixed-order sum (deterministic).  About 12 KB of
-// shared memory is used; 48 KB is requested so that exactly four CTAs share an
-// SM, which is what their 4 x 128 tensor-memory columns allow.
+// one M-tile (4 x 32 = 128 elements), and marches along x over XL planes.  Its
+// warps specialise, so that consecutive planes overlap:
+//   producers (warps 0-3, element row ey = warp, column ez = lane): stage node
+//     plane X+1 (d = s + beta d_old from s and d_old that cp.async brought into
+//     shared memory three planes ahead; d_new for owned nodes) into a ring of R
+//     shared slots, then build the element rows of plane X, split hi/lo, into one
+//     of two A buffers in tensor memory;
+//   issuer (warp 8, one thread): the 9 MMAs of plane X into one of two D buffers;
+//   consumers (warps 4-7, same element mapping): read their element's phase
+//     columns of D and sum them into nodes without atomics or colour copies --
+//     x: the far-x rows are carried in registers to the next plane; z: one warp
+//     shuffle adds lane ez-1's far-z rows; y: the far-y partial goes through a
+//     small exchange buffer to warp ey+1 -- then write K d of node plane X and
+//     accumulate <d, K d>.  Every node is a fixed-order sum (deterministic).
+// The groups hand over through mbarriers (A full, D full, D free, node slot
+// staged, node slot free); every wait is bounded and an expired wait sets an
+// abort flag that releases all other waits, so the kernel always ends and
+// reports the error status.  256 tensor-memory columns per CTA (two A and two D
+// buffers) allow two CTAs per SM.
 #include "kernels.cuh"
 
 #include <cstring>
@@ -40,15 +43,21 @@ constexpr int BY = 3, BZ = 31;
 constexpr int PY = BY + 2, PZ = BZ + 2;   // node plane incl. halo: y0-1..y0+3, z0-1..z0+31
 constexpr int EYN = BY + 1, EZN = BZ + 1; // element plane: origins y0-1..y0+2, z0-1..z0+30
 constexpr int NEL = EYN * EZN;            // 128 elements = one M-tile
-constexpr int TPB = 128;
+constexpr int NGRP = 128;                 // threads per role group (one per element)
+constexpr int TPB = 2 * NGRP + 32;        // producers, consumers, issuer warp
 constexpr int NPL = PY * PZ;              // 165 nodes per plane incl. halo
 constexpr int XL  = 32;                   // planes per CTA
-constexpr int TCOLS  = 128;               // tensor memory: D [0, 64), A hi [64, 96), A lo [96, 128)
-constexpr int COL_AH = 64, COL_AL = 96;
-// dynamic shared memory requested: with the 1 KB the driver reserves per block, 4 CTAs fit in an
-// SM's 228 KB and 5 do not -- residency is capped at the 4 x 128 tensor-memory columns an SM has
-constexpr int SMEM_REQ = 48 * 1024;
-constexpr unsigned kWaitLimit = 1u << 24; // bounded mbarrier wait
+constexpr int R   = 4;                    // node-plane slots
+constexpr int RAWD = 4;                   // raw (s, d_old) planes in flight: fetched RAWD-1 planes ahead
+constexpr int TCOLS = 256;                // tensor memory: D0, D1, A0 (hi, lo), A1 (hi, lo)
+constexpr int COL_LO = 32;
+__host__ __device__ constexpr int col_d(int b) { return 64 * b; }        // D buffer b: 64 columns
+__host__ __device__ constexpr int col_a(int b) { return 128 + 64 * b; }  // A buffer b: hi, then lo at +COL_LO
+// dynamic shared memory requested: with the 1 KB reserved per block, 2 CTAs fit in an SM's 228 KB
+// and 3 do not -- residency is capped at the 2 x 256 tensor-memory columns an SM has
+constexpr int SMEM_REQ = 80 * 1024;
+constexpr unsigned kWaitLimit = 1u << 22; // bounded mbarrier waits (try_wait suspends between polls)
+enum { BAR_AFULL = 0, BAR_DFULL = 2, BAR_DFREE = 4, BAR_STAGED = 6, BAR_SFREE = 6 + R, NBAR = 6 + 2 * R };
 static_assert(NEL == 128 && EYN == 4 && EZN == 32, "one M-tile per element plane, one warp per element row");
 
 template <int C, int NPH>
@@ -61,14 +70,16 @@ struct TcCfg {
     static constexpr int NW      = (NROW + 15) / 16 * 16; // MMA N
     static constexpr int KSTEPS  = NCOL / 8;              // K = 8 per tf32 MMA
     static constexpr int W_BYTES = NW * NCOL * 4;
-    static constexpr int NPF     = (C * NPL + TPB - 1) / TPB; // prefetched node values per thread and field
+    static constexpr int NPF     = (C * NPL + NGRP - 1) / NGRP; // prefetched node values per producer and field
     static constexpr int al(int b) { return (b + 127) / 128 * 128; }
     static constexpr int OFF_W   = 0;                                  // [hi, lo][W_BYTES]
-    static constexpr int OFF_D   = al(OFF_W + 2 * W_BYTES);            // [3 slots][C][NPL] float
-    static constexpr int OFF_X   = al(OFF_D + 3 * C * NPL * 4);        // [2 parity][4 warps][C][32] float
-    static constexpr int OFF_BAR = al(OFF_X + 2 * EYN * C * 32 * 4);
-    static constexpr int SMEM    = OFF_BAR + 16 + 32 * 8;
-    static_assert(NW <= COL_AH && NCOL <= COL_AL - COL_AH && NCOL <= TCOLS - COL_AL, "tensor-memory map");
+    static constexpr int OFF_D   = al(OFF_W + 2 * W_BYTES);            // [R slots][C][NPL] float
+    static constexpr int OFF_RAW = al(OFF_D + R * C * NPL * 4);        // [RAWD][s, d_old][C][NPL] float
+    static constexpr int OFF_X   = al(OFF_RAW + RAWD * 2 * C * NPL * 4); // [2][EYN][C][32] float
+    static constexpr int OFF_BAR = al(OFF_X + 2 * EYN * C * 32 * 4);   // NBAR mbarriers, tmem slot, abort flag
+    static constexpr int OFF_RED = al(OFF_BAR + NBAR * 8 + 8);          // 32 doubles
+    static constexpr int SMEM    = OFF_RED + 32 * 8;
+    static_assert(NW <= 64 && NCOL <= COL_LO, "tensor-memory map");
     static_assert(SMEM <= SMEM_REQ, "shared memory");
 };
 
@@ -129,39 +140,74 @@ __device__ __forceinline__ void umma_tf32_ts(uint32_t dtmem, uint32_t atmem, uin
                  "r"(atmem), "l"(bd), "r"(idesc), "r"(acc));
 }
 
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Wait for the phase with the given parity; bounded, and released by the abort flag.
+__device__ __forceinline__ void mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag)
+{
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done || *abort_flag)
+            return;
+    }
+    *abort_flag = 1;
+}
+
+__device__ __forceinline__ void named_bar(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 template <int C, int NPH>
-__global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const float *__restrict__ Wg)
+__global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const float *__restrict__ Wg)
 {
     using Cfg = TcCfg<C, NPH>;
     constexpr int NCOL = Cfg::NCOL, NPF = Cfg::NPF;
     extern __shared__ __align__(16) unsigned char smem[];
-    float    *Dp        = reinterpret_cast<float *>(smem + Cfg::OFF_D);
-    float    *Xch       = reinterpret_cast<float *>(smem + Cfg::OFF_X);
-    uint64_t *mbar      = reinterpret_cast<uint64_t *>(smem + Cfg::OFF_BAR);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + Cfg::OFF_BAR + 8);
-    double   *red_smem  = reinterpret_cast<double *>(smem + Cfg::OFF_BAR + 16);
+    float        *Dp        = reinterpret_cast<float *>(smem + Cfg::OFF_D);
+    float        *Xch       = reinterpret_cast<float *>(smem + Cfg::OFF_X);
+    float        *Raw       = reinterpret_cast<float *>(smem + Cfg::OFF_RAW);
+    const uint32_t bar0     = smem_u32(smem + Cfg::OFF_BAR);
+    uint32_t     *tmem_slot = reinterpret_cast<uint32_t *>(smem + Cfg::OFF_BAR + NBAR * 8);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + Cfg::OFF_BAR + NBAR * 8 + 4);
+    double       *red_smem  = reinterpret_cast<double *>(smem + Cfg::OFF_RED);
+    auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
 
     const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
     const long long N = (long long)nx * ny * nz;
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     const int y0 = blockIdx.y * BY, z0 = blockIdx.z * BZ;
     const int xs = blockIdx.x * XL, xe = min(xs + XL, nx);
-    const float *sin  = reinterpret_cast<const float *>(a.x);
-    const float *dold = reinterpret_cast<const float *>(a.d_old);
-    float       *dnew = reinterpret_cast<float *>(a.d_new);
-    float       *yout = reinterpret_cast<float *>(a.y);
-    const float  beta = (float)a.scal->beta;
-
-    // this thread's element (row ey = warp, column ez = lane) and global (y, z)
-    const int       ey = warp, ez = lane;
-    const long long el_yz = (long long)pmod(y0 - 1 + ey, ny) * nz + pmod(z0 - 1 + ez, nz);
+    const int J  = xe - xs + 1; // element planes xs-1 .. xe-1
     const long long plane = (long long)ny * nz;
 
-    // ---- one-off setup: W (hi, lo), barrier, TMEM
+    // ---- setup: W (hi, lo), barriers, tensor memory
     for (int i = tid; i < 2 * Cfg::W_BYTES / 16; i += TPB)
         reinterpret_cast<float4 *>(smem + Cfg::OFF_W)[i] = reinterpret_cast<const float4 *>(Wg)[i];
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(bar(BAR_AFULL + b), NGRP);
+            mbar_init(bar(BAR_DFULL + b), 1);
+            mbar_init(bar(BAR_DFREE + b), NGRP);
+        }
+        for (int s = 0; s < R; ++s) {
+            mbar_init(bar(BAR_STAGED + s), NGRP);
+            mbar_init(bar(BAR_SFREE + s), NGRP);
+        }
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -170,105 +216,95 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-
-    // prefetch slots: value tid + k*TPB of the plane ([c][hy][hz]); global offset without x,
-    // plane-local offset, and whether it is an owned node (d_new written)
-    long long goff[NPF];
-    int       loff[NPF];
-    unsigned  owned_mask = 0, valid_mask = 0;
-#pragma unroll
-    for (int k = 0; k < NPF; ++k) {
-        const int idx = tid + k * TPB;
-        goff[k] = 0;
-        loff[k] = 0;
-        if (idx < C * NPL) {
-            const int c = idx / NPL, rem = idx % NPL, hy = rem / PZ, hz = rem % PZ;
-            const int y = y0 - 1 + hy, z = z0 - 1 + hz;
-            goff[k] = c * N + (long long)pmod(y, ny) * nz + pmod(z, nz);
-            loff[k] = c * NPL + rem;
-            valid_mask |= 1u << k;
-            if (hy >= 1 && hy <= BY && hz >= 1 && hz <= BZ && y < ny && z < nz)
-                owned_mask |= 1u << k;
-        }
-    }
-    // output node of this thread: node (ey, ez) of the halo plane, owned for ey >= 1, ez >= 1
-    const bool      out_ok = ey >= 1 && ez >= 1 && y0 - 1 + ey < ny && z0 - 1 + ez < nz;
-    const int       onode  = ey * PZ + ez;
-    const long long oyz    = out_ok ? (long long)(y0 - 1 + ey) * nz + (z0 - 1 + ez) : 0;
-
-    // node plane X: thread's share of (s, d_old) into registers
-    float sv[NPF], dv[NPF];
-    auto load_plane = [&](int X) {
-        const long long gx = (long long)wrap(X, nx) * plane;
-#pragma unroll
-        for (int k = 0; k < NPF; ++k)
-            if (valid_mask & (1u << k)) {
-                sv[k] = __ldg(sin + goff[k] + gx);
-                dv[k] = __ldg(dold + goff[k] + gx);
-            }
-    };
-    // d = s + beta d_old of the registered plane X into node slot ds (+ d_new for owned nodes)
-    auto store_plane = [&](int X, int ds) {
-        const bool      owned_x = X >= xs && X < xe;
-        const long long gx      = (long long)wrap(X, nx) * plane;
-#pragma unroll
-        for (int k = 0; k < NPF; ++k)
-            if (valid_mask & (1u << k)) {
-                const float v = sv[k] + beta * dv[k];
-                Dp[ds * C * NPL + loff[k]] = v;
-                if (owned_x && (owned_mask & (1u << k)))
-                    dnew[goff[k] + gx] = v;
-            }
-    };
-    // node plane Xo: this thread's near-y partial plus warp ey-1's far-y partial (exchange
-    // parity xp); d from node slot ds
-    float  pend[C];
-    double dot = 0.0;
-    auto output_plane = [&](int Xo, int xp, int ds) {
-        if (!out_ok)
-            return;
-        const long long gi = (long long)wrap(Xo, nx) * plane + oyz;
-        const float    *xc = Xch + ((xp * EYN + ey - 1) * C) * 32 + ez;
-        float           dl = 0.f;
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const float v = pend[c] + xc[c * 32];
-            yout[c * N + gi] = v;
-            dl += Dp[(ds * C + c) * NPL + onode] * v;
-        }
-        dot += (double)dl;
-    };
-
-    // ---- prologue: node plane xs-1 stored, node plane xs and the phases of element plane xs-1 in registers
-    load_plane(xs - 1);
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    store_plane(xs - 1, 0);
-    load_plane(xs);
-    int ph_cur = a.ms[(long long)wrap(xs - 1, nx) * plane + el_yz];
+    double         dot  = 0.0;
 
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Cfg::NW >> 3) << 17) | (8u << 24);
-    bool  ok = true;
-    float carry[4 * C]; // far-x rows (qa = 1) of this thread's element in plane X-1, [qb + 2 qc][c]
+    if (warp < 4) {
+        // ================================================================ producers
+        const int   ey = warp, ez = lane;
+        const float *sin  = reinterpret_cast<const float *>(a.x);
+        const float *dold = reinterpret_cast<const float *>(a.d_old);
+        float       *dnew = reinterpret_cast<float *>(a.d_new);
+        const float  beta = (float)a.scal->beta;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        // prefetch slots: value tid + k*NGRP of the plane ([c][hy][hz]): global offset without x,
+        // plane-local offset, owned node (d_new written)
+        long long goff[NPF];
+        int       loff[NPF];
+        unsigned  owned_mask = 0, valid_mask = 0;
 #pragma unroll
-    for (int i = 0; i < 4 * C; ++i)
-        carry[i] = 0.f;
-
-    for (int X = xs - 1; X < xe; ++X) {
-        const int j = X - xs + 1; // 0 .. xe-xs
-        // node plane X+1 into slot (j+1)%3: its last readers (element plane X-2, output of
-        // node plane X-2) finished before the previous step's completion barrier
-        store_plane(X + 1, (j + 1) % 3);
-        if (X + 2 <= xe)
-            load_plane(X + 2);
-        const int ph_next = X + 1 < xe ? (int)a.ms[(long long)wrap(X + 1, nx) * plane + el_yz] : 0;
-        __syncthreads(); // S2: node planes X, X+1 staged; exchange of node plane X-1 visible
-
-        // element row of plane X, split hi/lo, into this thread's tensor-memory lane
-        {
-            const float *P0 = Dp + (j % 3) * C * NPL, *P1 = Dp + ((j + 1) % 3) * C * NPL;
+        for (int k = 0; k < NPF; ++k) {
+            const int idx = tid + k * NGRP;
+            goff[k] = 0;
+            loff[k] = 0;
+            if (idx < C * NPL) {
+                const int c = idx / NPL, rem = idx % NPL, hy = rem / PZ, hz = rem % PZ;
+                const int y = y0 - 1 + hy, z = z0 - 1 + hz;
+                goff[k] = c * N + (long long)pmod(y, ny) * nz + pmod(z, nz);
+                loff[k] = c * NPL + rem;
+                valid_mask |= 1u << k;
+                if (hy >= 1 && hy <= BY && hz >= 1 && hz <= BZ && y < ny && z < nz)
+                    owned_mask |= 1u << k;
+            }
+        }
+        // node plane index m (node plane xs-1+m): s and d_old copied asynchronously into raw
+        // ring slot m % RAWD, RAWD-1 planes ahead of their use; each thread copies and later
+        // reads only its own entries, so cp.async.wait_group orders everything it needs
+        auto fetch = [&](int m) {
+            if (m <= J) {
+                const long long gx  = (long long)wrap(xs - 1 + m, nx) * plane;
+                float          *raw = Raw + (m % RAWD) * 2 * C * NPL;
+#pragma unroll
+                for (int k = 0; k < NPF; ++k)
+                    if (valid_mask & (1u << k)) {
+                        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(raw + loff[k])),
+                                     "l"(sin + goff[k] + gx)
+                                     : "memory");
+                        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                                         smem_u32(raw + C * NPL + loff[k])),
+                                     "l"(dold + goff[k] + gx)
+                                     : "memory");
+                    }
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        };
+        // d = s + beta d_old of node plane m into slot m % R (+ d_new for owned nodes)
+        auto stage = [&](int m) {
+            asm volatile("cp.async.wait_group %0;" ::"n"(RAWD - 2) : "memory"); // plane m has landed
+            const int       X       = xs - 1 + m;
+            const bool      owned_x = X >= xs && X < xe;
+            const long long gx      = (long long)wrap(X, nx) * plane;
+            const float    *raw     = Raw + (m % RAWD) * 2 * C * NPL;
+            float          *slot    = Dp + (m % R) * C * NPL;
+#pragma unroll
+            for (int k = 0; k < NPF; ++k)
+                if (valid_mask & (1u << k)) {
+                    const float v = raw[loff[k]] + beta * raw[C * NPL + loff[k]];
+                    slot[loff[k]] = v;
+                    if (owned_x && (owned_mask & (1u << k)))
+                        dnew[goff[k] + gx] = v;
+                }
+            mbar_arrive(bar(BAR_STAGED + m % R));
+        };
+        for (int m = 0; m < RAWD - 1; ++m)
+            fetch(m);
+        stage(0);
+        fetch(RAWD - 1);
+        for (int j = 0; j < J; ++j) {
+            const int m = j + 1, b = j & 1; // node plane to stage; A buffer
+            if (m >= R)                     // consumers are done with node plane m - R
+                mbar_wait(bar(BAR_SFREE + m % R), (uint32_t)(((m - R) / R) & 1), abort_flag);
+            stage(m);
+            fetch(m + RAWD - 1);            // into the raw slot node plane m-1 used
+            named_bar(1, NGRP);     // node planes j and j+1 staged by all producers
+            if (j >= 2)             // the MMAs of plane j-2 have read A buffer b
+                mbar_wait(bar(BAR_DFULL + b), (uint32_t)(((j - 2) >> 1) & 1), abort_flag);
+            __syncwarp(); // tcgen05.st is warp-aligned
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // element row of plane j, split hi/lo, into this thread's lane of A buffer b
+            const float *P0 = Dp + (j % R) * C * NPL, *P1 = Dp + ((j + 1) % R) * C * NPL;
             float u0[C], v[NCOL];
 #pragma unroll
             for (int c = 0; c < C; ++c)
@@ -289,113 +325,135 @@ __global__ void __launch_bounds__(TPB, 4) k_stencil_tc(StencilArgs a, const floa
             }
 #pragma unroll
             for (int k0 = 0; k0 < NCOL; k0 += 8) {
-                tmem_st8(lane_base + (uint32_t)(COL_AH + k0), h + k0);
-                tmem_st8(lane_base + (uint32_t)(COL_AL + k0), l + k0);
+                tmem_st8(lane_base + (uint32_t)(col_a(b) + k0), h + k0);
+                tmem_st8(lane_base + (uint32_t)(col_a(b) + COL_LO + k0), l + k0);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(bar(BAR_AFULL + b));
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads(); // S3: A of plane X in tensor memory
-
-        if (tid == 0) {
+    } else if (warp < 8) {
+        // ================================================================ consumers
+        const int       ey = warp - 4, ez = lane;
+        const long long el_yz = (long long)pmod(y0 - 1 + ey, ny) * nz + pmod(z0 - 1 + ez, nz);
+        float          *yout  = reinterpret_cast<float *>(a.y);
+        const uint32_t  lane_base = tmem + ((uint32_t)(ey * 32) << 16);
+        const bool      out_ok = ey >= 1 && ez >= 1 && y0 - 1 + ey < ny && z0 - 1 + ez < nz;
+        const int       onode  = ey * PZ + ez;
+        const long long oyz    = out_ok ? (long long)(y0 - 1 + ey) * nz + (z0 - 1 + ez) : 0;
+        float carry[4 * C]; // far-x rows of this element in the previous plane, [qb + 2 qc][c]
+#pragma unroll
+        for (int i = 0; i < 4 * C; ++i)
+            carry[i] = 0.f;
+        int ph_cur = NPH > 1 ? a.ms[(long long)wrap(xs - 1, nx) * plane + el_yz] : 0;
+        for (int j = 0; j < J; ++j) {
+            const int X = xs - 1 + j, b = j & 1;
+            const int ph_next = (NPH > 1 && j + 1 < J) ? (int)a.ms[(long long)wrap(X + 1, nx) * plane + el_yz] : 0;
+            mbar_wait(bar(BAR_DFULL + b), (uint32_t)((j >> 1) & 1), abort_flag);
+            __syncwarp(); // tcgen05.ld is warp-aligned
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t wbase = smem_u32(smem + Cfg::OFF_W);
-            // 3xTF32: lo*hi + hi*lo + hi*hi (small terms first)
-#pragma unroll
-            for (int s = 0; s < Cfg::KSTEPS; ++s)
-                umma_tf32_ts(tmem, tmem + COL_AL + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc,
-                             s > 0 ? 1u : 0u);
-#pragma unroll
-            for (int s = 0; s < Cfg::KSTEPS; ++s)
-                umma_tf32_ts(tmem, tmem + COL_AH + 8 * s,
-                             umma_desc<Cfg::SBO, Cfg::LBO>(wbase + Cfg::W_BYTES + s * 256), idesc, 1u);
-#pragma unroll
-            for (int s = 0; s < Cfg::KSTEPS; ++s)
-                umma_tf32_ts(tmem, tmem + COL_AH + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, 1u);
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(mbar))
-                         : "memory");
-        }
-
-        // node plane X-1 (its exchange was written before S2) while the MMAs run
-        if (X - 1 >= xs)
-            output_plane(X - 1, (X - 1) & 1, (j + 2) % 3);
-
-        uint32_t done = 1;
-        if (tid == 0) { // one poller; the other threads wait at the barrier below
-            done = 0;
-            for (unsigned it = 0; it < kWaitLimit && !done; ++it)
-                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                             " selp.u32 %0, 1, 0, p;\n}\n"
-                             : "=r"(done)
-                             : "r"(smem_u32(mbar)), "r"((uint32_t)(j & 1))
-                             : "memory");
-        }
-        if (!__syncthreads_and(done ? 1 : 0)) { // S4: D ready; output of node plane X-1 done
-            ok = false;
-            break;
-        }
-
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        {
-            // this element's phase rows: out[q*C + c], local node q = qa + 2 qb + 4 qc
             float out[NCOL];
             {
                 float v[Cfg::NW];
 #pragma unroll
                 for (int c0 = 0; c0 < Cfg::NW; c0 += 16)
-                    tmem_ld16(lane_base + (uint32_t)c0, v + c0);
+                    tmem_ld16(lane_base + (uint32_t)(col_d(b) + c0), v + c0);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
                 for (int r = 0; r < NCOL; ++r)
                     out[r] = (NPH > 1 && ph_cur == 1) ? v[NCOL + r] : v[r];
             }
-            // x: near-x rows plus the far-x rows carried from element plane X-1
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(bar(BAR_DFREE + b));
+            // x: near-x rows plus the far-x rows carried from the previous plane
             float P[4 * C];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) { // b = qb + 2 qc
-                const int q0 = 2 * b;     // qa = 0
+            for (int g = 0; g < 4; ++g) { // g = qb + 2 qc, near-x node q = 2g, far-x node 2g + 1
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
-                    P[b * C + c]     = out[q0 * C + c] + carry[b * C + c];
-                    carry[b * C + c] = out[(q0 + 1) * C + c];
+                    P[g * C + c]     = out[2 * g * C + c] + carry[g * C + c];
+                    carry[g * C + c] = out[(2 * g + 1) * C + c];
                 }
             }
-            // z: node (ey + qb, ez) gets lane ez-1's far-z rows (qc = 1)
+            // z: node (ey + qb, ez) gets lane ez-1's far-z rows
             float Z[2 * C];
 #pragma unroll
             for (int qb = 0; qb < 2; ++qb)
 #pragma unroll
                 for (int c = 0; c < C; ++c)
                     Z[qb * C + c] = P[qb * C + c] + __shfl_up_sync(0xffffffffu, P[(qb + 2) * C + c], 1);
-            // y: far-y partial (node ey+1) to the exchange; near-y partial kept for the output
-            float *xc = Xch + ((X & 1) * EYN + ey) * C * 32 + ez;
+            // y: far-y partial to the exchange, read back by warp ey+1
+            float *xw = Xch + (b * EYN + ey) * C * 32 + ez;
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                xc[c * 32] = Z[C + c];
-                pend[c]    = Z[c];
+            for (int c = 0; c < C; ++c)
+                xw[c * 32] = Z[C + c];
+            named_bar(2, NGRP);
+            if (X >= xs) {
+                mbar_wait(bar(BAR_STAGED + j % R), (uint32_t)((j / R) & 1), abort_flag); // node plane X
+                if (out_ok) {
+                    const long long gi = (long long)wrap(X, nx) * plane + oyz;
+                    const float    *xr = Xch + (b * EYN + ey - 1) * C * 32 + ez;
+                    const float    *dp = Dp + (j % R) * C * NPL + onode;
+                    float           dl = 0.f;
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        const float v = Z[c] + xr[c * 32];
+                        yout[c * N + gi] = v;
+                        dl += dp[c * NPL] * v;
+                    }
+                    dot += (double)dl;
+                }
+            }
+            mbar_arrive(bar(BAR_SFREE + j % R));
+            ph_cur = ph_next;
+        }
+    } else if (lane == 0) {
+        // ================================================================ MMA issuer
+        const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Cfg::NW >> 3) << 17) | (8u << 24);
+        const uint32_t wbase = smem_u32(smem + Cfg::OFF_W);
+        for (int j = 0; j < J; ++j) {
+            const int b = j & 1;
+            mbar_wait(bar(BAR_AFULL + b), (uint32_t)((j >> 1) & 1), abort_flag);
+            if (j >= 2) // consumers have read D buffer b of plane j-2
+                mbar_wait(bar(BAR_DFREE + b), (uint32_t)(((j - 2) >> 1) & 1), abort_flag);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!*abort_flag) {
+                const uint32_t d = tmem + col_d(b), ah = tmem + col_a(b), al = tmem + col_a(b) + COL_LO;
+                // 3xTF32: lo*hi + hi*lo + hi*hi (small terms first)
+#pragma unroll
+                for (int s = 0; s < Cfg::KSTEPS; ++s)
+                    umma_tf32_ts(d, al + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, s > 0 ? 1u : 0u);
+#pragma unroll
+                for (int s = 0; s < Cfg::KSTEPS; ++s)
+                    umma_tf32_ts(d, ah + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + Cfg::W_BYTES + s * 256), idesc,
+                                 1u);
+#pragma unroll
+                for (int s = 0; s < Cfg::KSTEPS; ++s)
+                    umma_tf32_ts(d, ah + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, 1u);
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 bar(BAR_DFULL + b))
+                             : "memory");
+            } else {
+                mbar_arrive(bar(BAR_DFULL + b)); // keep the consumers' phases moving
             }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        ph_cur = ph_next;
     }
+
     __syncthreads();
-    if (ok)
-        output_plane(xe - 1, (xe - 1) & 1, (xe - xs) % 3);
-    else if (tid == 0)
-        a.scal->converged = -3; // tensor-core completion wait timed out
+    if (*abort_flag && tid == 0)
+        a.scal->converged = -3; // a tensor-core pipeline wait expired
 
     // <d, K d> over the grid (solverCG.h:101)
     if (a.reduce) {
-        double    v[1]   = {dot};
+        double    vv[1]  = {dot};
         const int ops[1] = {RED_SUM};
-        block_reduce<1>(v, ops, red_smem);
+        block_reduce<1>(vv, ops, red_smem);
         const int nb = gridDim.x * gridDim.y * gridDim.z;
-        if (grid_partial_commit<1>(v, a.red.partials, a.red.counter + a.red_site, nb)) {
-            grid_final<1>(v, ops, a.red.partials, nb, red_smem);
+        if (grid_partial_commit<1>(vv, a.red.partials, a.red.counter + a.red_site, nb)) {
+            grid_final<1>(vv, ops, a.red.partials, nb, red_smem);
             if (threadIdx.x == 0) {
-                a.scal->dAd   = v[0];
-                a.scal->alpha = a.scal->delta / v[0];
+                a.scal->dAd   = vv[0];
+                a.scal->alpha = a.scal->delta / vv[0];
             }
         }
     }
