@@ -105,7 +105,7 @@ def algo_bytes(kernel, n, C=3, w=4):
         "fft_x_green": 2 * spec + nt * n * n * nzh * w,  # + Green's table
         "fft_y_inv": 2 * spec,
         "fft_z_inv": spec + 2 * C * w * N,       # read spectrum + r, write s
-        "cg_update": (5 * C * w + 2 * 8 * C) * N,  # read r Kd d s, write r; u64 read+write
+        "cg_update": 7 * C * w * N,              # read r, Kd, e, d, s; write r, e (FP32)
         "residual64": (2 * 8 * C + 1) * N,
         "norm": (8 * C + 4 * C) * N,
         "strain_stress": (8 * C + 1) * N,

@@ -1,0 +1,106 @@
+"""The J2 workload: 128^3 periodic spheres (seed 4, r = 8, vf 0.25), matrix
+J2PlasticityNew_LinearIsotropicHardening (E 70, nu 0.33 -> K 68.6275, G 26.3158;
+yield 0.25, hardening 2), elastic inclusions (K 222.222, G 166.667), eps_11 =
+0.0005 k for k = 1..20 (J2PlasticityNew.h:43-121, solverCG.h:120-160,
+solver.h:283-311).  The solves stop at Linfinity 1e-10 absolute, as the
+reference's test_J2Plasticity.json does: with extrapolateDisplacement the
+elastic steps start almost converged, and a relative tolerance would then ask
+for a residual below round-off.
+
+The oracle cannot run 20 nonlinear steps at 128^3 inside a test, so:
+* the same workload down-sampled to 32^3 is compared with the oracle step by
+  step (stress averages 1e-7, committed plastic strains 1e-6 of their maximum);
+* at 128^3 eight steps of 0.001 (eps_11 to 0.008): the first step is
+  elastic (equal to the elastic solve), the tangent drops once the matrix
+  yields and stays positive (hardening), and plastic strain appears in the
+  matrix only."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import gpu_context, oracle_problem, rel
+
+pytestmark = pytest.mark.gpu
+
+J2 = [(O.LAW_J2, [0], [[68.6275, 26.3158, 0.25, 2.0]]), (O.LAW_ELASTIC_ISO, [1], [[222.222, 166.667]])]
+ELASTIC = [(O.LAW_ELASTIC_ISO, [0, 1], [[68.6275, 26.3158], [222.222, 166.667]])]
+
+
+def _ms(n):
+    from fans_gb300.microstructure import spheres
+
+    ms, _ = spheres(128, 8, 0.25, 4)
+    step = 128 // n
+    return np.ascontiguousarray(ms[::step, ::step, ::step]).astype(np.uint16)
+
+
+def _path(ctx, steps, P=None, de=0.0005):
+    out = []
+    for k in range(1, steps + 1):
+        g = np.zeros(6)
+        g[0] = de * k
+        ctx.set_gradient(g)
+        st = ctx.solve()
+        assert st["converged"], (k, st)
+        out.append(ctx.homogenized_stress())
+        if P is not None:
+            P.set_gradient(g)
+            P.solve(measure="Linfinity", type="absolute", tol=1e-10, n_it=2000)
+            assert rel(out[-1], P.homogenized_stress()) < 1e-7, k
+        ctx.extrapolate_displacement()
+        if P is not None:
+            P.extrapolate_displacement()
+    return np.array(out)
+
+
+def test_j2_workload_downsampled_matches_oracle():
+    ms = _ms(32)
+    P = oracle_problem(ms, 3, J2, "HEX8")
+    ctx = gpu_context(P)
+    ctx.set_tolerance("Linfinity", "absolute", 1e-10, 2000)
+    sig = _path(ctx, 20, P)
+    ep = ctx.get_field(9).reshape(-1, 8, 6)  # committed plastic strain per Gauss point
+    assert np.abs(ep).max() > 0
+    assert rel(ep, P.ep_t) < 1e-6
+    assert sig[-1, 0] > sig[0, 0]
+    ctx.close()
+
+
+def test_j2_workload_128_curve_properties():
+    ms = _ms(128)
+    assert abs(ms.mean() - 0.25) < 0.02
+    from fans_gb300 import Context
+
+    P = oracle_problem(ms[:4, :4, :4], 3, J2, "HEX8")  # the reference-stiffness rule only
+
+    ctx = Context((128, 128, 128), (1.0, 1.0, 1.0), 3, "HEX8", "fp64", "cg")
+    ctx.set_microstructure(ms)
+    ctx.set_phase_material(0, O.LAW_J2, [68.6275, 26.3158, 0.25, 2.0])
+    ctx.set_phase_material(1, O.LAW_ELASTIC_ISO, [222.222, 166.667])
+    ctx.set_reference(P.kapparef)
+    ctx.set_tolerance("Linfinity", "absolute", 1e-10, 2000)
+    sig = _path(ctx, 8, de=0.001)
+    ep = ctx.get_field(5).reshape(-1, 6)
+    # plastic strain only in the matrix, and it is there at the end of the path
+    assert np.abs(ep[ms.reshape(-1) == 1]).max() == 0.0
+    assert np.abs(ep[ms.reshape(-1) == 0]).max() > 0.0
+    ctx.close()
+
+    # the elastic reference: the same microstructure with an elastic matrix
+    el = Context((128, 128, 128), (1.0, 1.0, 1.0), 3, "HEX8", "fp64", "cg")
+    el.set_microstructure(ms)
+    el.set_phase_material(0, O.LAW_ELASTIC_ISO, [68.6275, 26.3158])
+    el.set_phase_material(1, O.LAW_ELASTIC_ISO, [222.222, 166.667])
+    el.set_reference(O.OracleProblem(ms[:4, :4, :4], (1, 1, 1), 3, ELASTIC, "HEX8").kapparef)
+    el.set_tolerance("L2", "relative", 1e-10, 2000)
+    g = np.zeros(6)
+    g[0] = 0.001
+    el.set_gradient(g)
+    assert el.solve()["converged"]
+    s_el = el.homogenized_stress()
+    el.close()
+    # the first step is elastic (J2 and the elastic solve agree), later ones soften and harden
+    assert rel(sig[0], s_el) < 1e-6
+    tangent = np.diff(sig[:, 0]) / 0.001
+    assert tangent[-1] < 0.8 * tangent[0]  # the matrix has yielded
+    assert (tangent > 0).all()  # linear isotropic hardening keeps the tangent positive
