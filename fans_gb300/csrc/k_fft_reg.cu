@@ -51,12 +51,24 @@ __global__ void __launch_bounds__(KCol<T>::value * N1) k_y_reg(ConvPlan<T> p)
 }
 
 // ----------------------------------------------------- x pass + Green's op ---
+// One CTA per ky and KX kz columns (64-byte row segments), all kx and all C
+// components: forward FFT along x, the C x C Green multiply, inverse FFT along
+// x.  The CTA's slice of the Green's table is copied into shared memory with
+// cp.async at the start, so its reads overlap the forward transform; the
+// smaller tile lets two CTAs share an SM and overlap their load, compute and
+// store phases.
+template <typename T>
+struct KXCol {
+    static constexpr int value = 64 / (int)sizeof(cplx<T>);
+};
+
 template <typename T, int N1, int N2, int C>
-__global__ void __launch_bounds__(C * KCol<T>::value * N1) k_x_green_reg(ConvPlan<T> p)
+__global__ void __launch_bounds__(C * KXCol<T>::value * N1, 2) k_x_green_reg(ConvPlan<T> p)
 {
-    constexpr int KC = KCol<T>::value, n = N1 * N2, NT = C * (C + 1) / 2;
+    constexpr int KC = KXCol<T>::value, n = N1 * N2, NT = C * (C + 1) / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cplx<T>  *F  = reinterpret_cast<cplx<T> *>(smem_raw); // [C][n][KC]
+    cplx<T>  *F  = reinterpret_cast<cplx<T> *>(smem_raw);        // [C][n][KC]
+    T        *Gs = reinterpret_cast<T *>(F + (size_t)C * n * KC); // [n][KC][NT]
     const int nx = n, ny = p.g.ny;
     const int t = threadIdx.x, comp = t / (KC * N1), rem = t % (KC * N1), w = rem / KC, l = rem % KC;
     const int kz0 = blockIdx.x * KC, ky = blockIdx.y;
@@ -65,6 +77,22 @@ __global__ void __launch_bounds__(C * KCol<T>::value * N1) k_x_green_reg(ConvPla
     cplx<T> *gbase = p.spec + ((long long)comp * nx * ny + ky) * p.nzp + kz0 + l; // + x * ny * nzp
     const long long xstride = (long long)ny * p.nzp;
     cplx<T> *Fc = F + (size_t)comp * n * KC;
+
+    // Green's table slice [kx][kz0 .. kz0+nk)[NT] -> Gs, asynchronously
+    for (int i = t; i < n * nk * NT; i += blockDim.x) {
+        const int kx = i / (nk * NT), r2 = i % (nk * NT);
+        const T  *src = p.G + (((long long)kx * ny + ky) * p.nzh + kz0) * NT + r2;
+        T        *dst = Gs + (size_t)kx * KC * NT + r2;
+        if constexpr (sizeof(T) == 4)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                         "l"(src)
+                         : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                         "l"(src)
+                         : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 
     // forward FFT along x
     cplx<T> v[N2];
@@ -88,6 +116,7 @@ __global__ void __launch_bounds__(C * KCol<T>::value * N1) k_x_green_reg(ConvPla
         for (int k1 = 0; k1 < N1; ++k1)
             Fc[(w + N2 * k1) * KC + l] = u[k1];
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 
     // Green's operator: C x C real symmetric per frequency (solver.h:400-406)
@@ -95,7 +124,7 @@ __global__ void __launch_bounds__(C * KCol<T>::value * N1) k_x_green_reg(ConvPla
         const int kx = i / KC, ll = i % KC;
         if (ll >= nk)
             continue;
-        const T *g = p.G + (((long long)kx * ny + ky) * p.nzh + kz0 + ll) * NT;
+        const T *g = Gs + ((size_t)kx * KC + ll) * NT;
         T        gm[NT];
 #pragma unroll
         for (int q = 0; q < NT; ++q)
@@ -288,16 +317,17 @@ void go_y(const ConvPlan<T> &p, cudaStream_t st)
 template <typename T, int N1, int N2>
 cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
 {
-    constexpr int KC = KCol<T>::value;
+    constexpr int KC = KXCol<T>::value;
     dim3          g((p.nzh + KC - 1) / KC, p.g.ny);
+    const size_t  n = (size_t)N1 * N2;
     if (p.C == 1) {
-        const size_t sm = sizeof(cplx<T>) * (size_t)N1 * N2 * KC;
+        const size_t sm = sizeof(cplx<T>) * n * KC + sizeof(T) * n * KC * 1;
         cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 1>);
         if (e != cudaSuccess)
             return e;
         k_x_green_reg<T, N1, N2, 1><<<g, KC * N1, sm, st>>>(p);
     } else {
-        const size_t sm = sizeof(cplx<T>) * (size_t)3 * N1 * N2 * KC;
+        const size_t sm = sizeof(cplx<T>) * 3 * n * KC + sizeof(T) * n * KC * 6;
         cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 3>);
         if (e != cudaSuccess)
             return e;

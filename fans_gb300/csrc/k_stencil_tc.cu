@@ -46,7 +46,7 @@ constexpr int NEL = EYN * EZN;            // 128 elements = one M-tile
 constexpr int NGRP = 128;                 // threads per role group (one per element)
 constexpr int TPB = 2 * NGRP + 32;        // producers, consumers, issuer warp
 constexpr int NPL = PY * PZ;              // 165 nodes per plane incl. halo
-constexpr int XL  = 32;                   // planes per CTA
+constexpr int XL  = 64;                   // planes per CTA
 constexpr int R   = 4;                    // node-plane slots
 constexpr int RAWD = 4;                   // raw (s, d_old) planes in flight: fetched RAWD-1 planes ahead
 constexpr int TCOLS = 256;                // tensor memory: D0, D1, A0 (hi, lo), A1 (hi, lo)
