@@ -159,6 +159,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The job's figure for a time-like per-rank value: N independent replicas
+    (one process per GPU) finish when the slowest rank does, so the max over
+    ranks.  `dist` is torch.distributed when the process group is up, else None."""
+    if dist is None:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_problem(n, seed=0):
     from fans_gb300.microstructure import spheres
 
@@ -385,11 +398,7 @@ def main():
     clk = clocks.stop()
     ktimes = ctx.kernel_times()
     ctx.set_timing(False)
-    ms_step = ms_total / args.steps
-    if dist:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ms_total / args.steps, dist, "cuda")
     iters = [s["iterations"] for s in stats[:6]]
     refinements = [s["refinements"] for s in stats[:6]]
     launches = sum(c for _, c in ktimes.values())
@@ -410,7 +419,7 @@ def main():
     t0 = time.perf_counter()
     e2e_ms_dev, _ = timed_steps(ctx, args.steps, e2e_step)
     e2e_wall = (time.perf_counter() - t0) * 1e3 / args.steps
-    e2e_ms = max(e2e_ms_dev / args.steps, 0.0)
+    e2e_ms = max_over_ranks(max(e2e_ms_dev / args.steps, 0.0), dist, "cuda")
     scal_bytes = 144
     h2d = 2 * n ** 3 + 2 * 2 * 8 + 36 * 8 + 6 * 6 * 8
     d2h = 6 * 6 * 8 + scal_bytes * (sum(iters) + sum(refinements) + 6) + 4
