@@ -13,13 +13,14 @@
 //
 // A CTA owns a 3 (y) x 31 (z) column of nodes, whose element plane is exactly
 // one M-tile (4 x 32 = 128 elements), and marches along x over XL planes.  Its
-// warps specialise, so that consecutive planes overlap:
+// warps specialise, so that the work around consecutive MMAs overlaps:
 //   producers (warps 0-3, element row ey = warp, column ez = lane): stage node
 //     plane X+1 (d = s + beta d_old from s and d_old that cp.async brought into
 //     shared memory three planes ahead; d_new for owned nodes) into a ring of R
-//     shared slots, then build the element rows of plane X, split hi/lo, into one
-//     of two A buffers in tensor memory;
-//   issuer (warp 8, one thread): the 9 MMAs of plane X into one of two D buffers;
+//     shared slots, then -- once the MMAs of plane X-1 have read A -- build the
+//     element rows of plane X, split hi/lo, into A in tensor memory;
+//   issuer (warp 8, one thread): the 9 MMAs of plane X into D once A is full and
+//     the consumers have read the previous D;
 //   consumers (warps 4-7, same element mapping): read their element's phase
 //     columns of D and sum them into nodes without atomics or colour copies --
 //     x: the far-x rows are carried in registers to the next plane; z: one warp
@@ -29,8 +30,10 @@
 // The groups hand over through mbarriers (A full, D full, D free, node slot
 // staged, node slot free); every wait is bounded and an expired wait sets an
 // abort flag that releases all other waits, so the kernel always ends and
-// reports the error status.  256 tensor-memory columns per CTA (two A and two D
-// buffers) allow two CTAs per SM.
+// reports the error status.  A and D are single-buffered (128 tensor-memory
+// columns per CTA), so three CTAs share an SM and keep its tensor pipe fed: the
+// SM's tensor pipe is shared, and more CTAs fill the gaps between one CTA's MMA
+// bursts better than deeper buffering within a CTA.
 #include "kernels.cuh"
 
 #include <cstring>
@@ -49,15 +52,13 @@ constexpr int NPL = PY * PZ;              // 165 nodes per plane incl. halo
 constexpr int XL  = 64;                   // planes per CTA
 constexpr int R   = 4;                    // node-plane slots
 constexpr int RAWD = 4;                   // raw (s, d_old) planes in flight: fetched RAWD-1 planes ahead
-constexpr int TCOLS = 256;                // tensor memory: D0, D1, A0 (hi, lo), A1 (hi, lo)
-constexpr int COL_LO = 32;
-__host__ __device__ constexpr int col_d(int b) { return 64 * b; }        // D buffer b: 64 columns
-__host__ __device__ constexpr int col_a(int b) { return 128 + 64 * b; }  // A buffer b: hi, then lo at +COL_LO
-// dynamic shared memory requested: with the 1 KB reserved per block, 2 CTAs fit in an SM's 228 KB
-// and 3 do not -- residency is capped at the 2 x 256 tensor-memory columns an SM has
-constexpr int SMEM_REQ = 80 * 1024;
+constexpr int TCOLS = 128;                // tensor memory: A (hi at 0, lo at 32), D at 64
+constexpr int COL_LO = 32, COL_A = 0, COL_D = 64;
+// dynamic shared memory requested: with the 1 KB reserved per block, 3 CTAs fit in an SM's 228 KB
+// and 4 do not (4 x 128 tensor-memory columns would fit, 4 x 288 threads' registers would not)
+constexpr int SMEM_REQ = 64 * 1024;
 constexpr unsigned kWaitLimit = 1u << 22; // bounded mbarrier waits (try_wait suspends between polls)
-enum { BAR_AFULL = 0, BAR_DFULL = 2, BAR_DFREE = 4, BAR_STAGED = 6, BAR_SFREE = 6 + R, NBAR = 6 + 2 * R };
+enum { BAR_AFULL = 0, BAR_DFULL = 1, BAR_DFREE = 2, BAR_STAGED = 3, BAR_SFREE = 3 + R, NBAR = 3 + 2 * R };
 static_assert(NEL == 128 && EYN == 4 && EZN == 32, "one M-tile per element plane, one warp per element row");
 
 template <int C, int NPH>
@@ -79,7 +80,7 @@ struct TcCfg {
     static constexpr int OFF_BAR = al(OFF_X + 2 * EYN * C * 32 * 4);   // NBAR mbarriers, tmem slot, abort flag
     static constexpr int OFF_RED = al(OFF_BAR + NBAR * 8 + 8);          // 32 doubles
     static constexpr int SMEM    = OFF_RED + 32 * 8;
-    static_assert(NW <= 64 && NCOL <= COL_LO, "tensor-memory map");
+    static_assert(NW <= TCOLS - COL_D && NCOL <= COL_LO && COL_LO + NCOL <= COL_D, "tensor-memory map");
     static_assert(SMEM <= SMEM_REQ, "shared memory");
 };
 
@@ -172,7 +173,7 @@ __device__ __forceinline__ void named_bar(int id, int nthreads)
 }
 
 template <int C, int NPH>
-__global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const float *__restrict__ Wg)
+__global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const float *__restrict__ Wg)
 {
     using Cfg = TcCfg<C, NPH>;
     constexpr int NCOL = Cfg::NCOL, NPF = Cfg::NPF;
@@ -198,11 +199,9 @@ __global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const floa
     for (int i = tid; i < 2 * Cfg::W_BYTES / 16; i += TPB)
         reinterpret_cast<float4 *>(smem + Cfg::OFF_W)[i] = reinterpret_cast<const float4 *>(Wg)[i];
     if (tid == 0) {
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(bar(BAR_AFULL + b), NGRP);
-            mbar_init(bar(BAR_DFULL + b), 1);
-            mbar_init(bar(BAR_DFREE + b), NGRP);
-        }
+        mbar_init(bar(BAR_AFULL), NGRP);
+        mbar_init(bar(BAR_DFULL), 1);
+        mbar_init(bar(BAR_DFREE), NGRP);
         for (int s = 0; s < R; ++s) {
             mbar_init(bar(BAR_STAGED + s), NGRP);
             mbar_init(bar(BAR_SFREE + s), NGRP);
@@ -293,17 +292,17 @@ __global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const floa
         stage(0);
         fetch(RAWD - 1);
         for (int j = 0; j < J; ++j) {
-            const int m = j + 1, b = j & 1; // node plane to stage; A buffer
+            const int m = j + 1; // node plane to stage
             if (m >= R)                     // consumers are done with node plane m - R
                 mbar_wait(bar(BAR_SFREE + m % R), (uint32_t)(((m - R) / R) & 1), abort_flag);
             stage(m);
             fetch(m + RAWD - 1);            // into the raw slot node plane m-1 used
             named_bar(1, NGRP);     // node planes j and j+1 staged by all producers
-            if (j >= 2)             // the MMAs of plane j-2 have read A buffer b
-                mbar_wait(bar(BAR_DFULL + b), (uint32_t)(((j - 2) >> 1) & 1), abort_flag);
+            if (j >= 1)             // the MMAs of plane j-1 have read A
+                mbar_wait(bar(BAR_DFULL), (uint32_t)((j - 1) & 1), abort_flag);
             __syncwarp(); // tcgen05.st is warp-aligned
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // element row of plane j, split hi/lo, into this thread's lane of A buffer b
+            // element row of plane j, split hi/lo, into this thread's lane of A
             const float *P0 = Dp + (j % R) * C * NPL, *P1 = Dp + ((j + 1) % R) * C * NPL;
             float u0[C], v[NCOL];
 #pragma unroll
@@ -325,12 +324,12 @@ __global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const floa
             }
 #pragma unroll
             for (int k0 = 0; k0 < NCOL; k0 += 8) {
-                tmem_st8(lane_base + (uint32_t)(col_a(b) + k0), h + k0);
-                tmem_st8(lane_base + (uint32_t)(col_a(b) + COL_LO + k0), l + k0);
+                tmem_st8(lane_base + (uint32_t)(COL_A + k0), h + k0);
+                tmem_st8(lane_base + (uint32_t)(COL_A + COL_LO + k0), l + k0);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            mbar_arrive(bar(BAR_AFULL + b));
+            mbar_arrive(bar(BAR_AFULL));
         }
     } else if (warp < 8) {
         // ================================================================ consumers
@@ -347,24 +346,30 @@ __global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const floa
             carry[i] = 0.f;
         int ph_cur = NPH > 1 ? a.ms[(long long)wrap(xs - 1, nx) * plane + el_yz] : 0;
         for (int j = 0; j < J; ++j) {
-            const int X = xs - 1 + j, b = j & 1;
+            const int X = xs - 1 + j, b = j & 1; // b: exchange parity
             const int ph_next = (NPH > 1 && j + 1 < J) ? (int)a.ms[(long long)wrap(X + 1, nx) * plane + el_yz] : 0;
-            mbar_wait(bar(BAR_DFULL + b), (uint32_t)((j >> 1) & 1), abort_flag);
+            mbar_wait(bar(BAR_DFULL), (uint32_t)(j & 1), abort_flag);
             __syncwarp(); // tcgen05.ld is warp-aligned
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float out[NCOL];
-            {
-                float v[Cfg::NW];
+            float out[NCOL]; // this element's phase columns, 16 at a time
 #pragma unroll
-                for (int c0 = 0; c0 < Cfg::NW; c0 += 16)
-                    tmem_ld16(lane_base + (uint32_t)(col_d(b) + c0), v + c0);
+            for (int c0 = 0; c0 < Cfg::NW; c0 += 16) {
+                float v[16];
+                tmem_ld16(lane_base + (uint32_t)(COL_D + c0), v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int r = 0; r < NCOL; ++r)
-                    out[r] = (NPH > 1 && ph_cur == 1) ? v[NCOL + r] : v[r];
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int col = c0 + jj, k = col / NCOL, r = col % NCOL;
+                    if (col < Cfg::NROW) {
+                        if (k == 0)
+                            out[r] = v[jj];
+                        else if (ph_cur == k)
+                            out[r] = v[jj];
+                    }
+                }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            mbar_arrive(bar(BAR_DFREE + b));
+            mbar_arrive(bar(BAR_DFREE));
             // x: near-x rows plus the far-x rows carried from the previous plane
             float P[4 * C];
 #pragma unroll
@@ -412,13 +417,12 @@ __global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const floa
         const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Cfg::NW >> 3) << 17) | (8u << 24);
         const uint32_t wbase = smem_u32(smem + Cfg::OFF_W);
         for (int j = 0; j < J; ++j) {
-            const int b = j & 1;
-            mbar_wait(bar(BAR_AFULL + b), (uint32_t)((j >> 1) & 1), abort_flag);
-            if (j >= 2) // consumers have read D buffer b of plane j-2
-                mbar_wait(bar(BAR_DFREE + b), (uint32_t)(((j - 2) >> 1) & 1), abort_flag);
+            mbar_wait(bar(BAR_AFULL), (uint32_t)(j & 1), abort_flag);
+            if (j >= 1) // consumers have read D of plane j-1
+                mbar_wait(bar(BAR_DFREE), (uint32_t)((j - 1) & 1), abort_flag);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (!*abort_flag) {
-                const uint32_t d = tmem + col_d(b), ah = tmem + col_a(b), al = tmem + col_a(b) + COL_LO;
+                const uint32_t d = tmem + COL_D, ah = tmem + COL_A, al = tmem + COL_A + COL_LO;
                 // 3xTF32: lo*hi + hi*lo + hi*hi (small terms first)
 #pragma unroll
                 for (int s = 0; s < Cfg::KSTEPS; ++s)
@@ -431,10 +435,10 @@ __global__ void __launch_bounds__(TPB, 2) k_stencil_tc(StencilArgs a, const floa
                 for (int s = 0; s < Cfg::KSTEPS; ++s)
                     umma_tf32_ts(d, ah + 8 * s, umma_desc<Cfg::SBO, Cfg::LBO>(wbase + s * 256), idesc, 1u);
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 bar(BAR_DFULL + b))
+                                 bar(BAR_DFULL))
                              : "memory");
             } else {
-                mbar_arrive(bar(BAR_DFULL + b)); // keep the consumers' phases moving
+                mbar_arrive(bar(BAR_DFULL)); // keep the consumers' phases moving
             }
         }
     }
