@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(UpdateArgs a)
                     u[i] = u[i] - (TU)alpha * (TU)d[i];
                 const T av = rv < (T)0 ? -rv : rv;
                 const T t  = measure == 1 ? av * av : av;
-                cn         = mx ? (t > cn ? t : cn) : cn + t;
+                cn         = mx ? ((t > cn || t != t) ? t : cn) : cn + t; // NaN-keeping max
                 crs += rv * s[i];
             }
         }

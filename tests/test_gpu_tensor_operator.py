@@ -2,9 +2,11 @@
 CUDA-core FP32 operator and the FP64 oracle.
 
 Mixed-precision solves are run twice on the same context settings, once with
-the tensor-core operator (default where the grid allows it: n_y % 8 == 0,
-n_z % 32 == 0, at most two phases) and once with FANSGPU_STENCIL=simt, which
-selects the CUDA-core operator at context creation.  Both are FP32-accurate
+the tensor-core operator (the default for at most two phases, any grid) and
+once with FANSGPU_STENCIL=simt, which selects the CUDA-core operator at
+context creation.  The shapes include ragged tiles in every direction (the
+operator's CTAs own 64 x 3 x 31 nodes) and grids whose FFT lengths have no
+register plan.  Both are FP32-accurate
 operators inside the same reliable-update CG, so they take the same number of
 iterations (within 1) and give the same solution to the accuracy the FP64
 refreshes pin (1e-9 relative on the stress average); both meet the oracle's
@@ -39,7 +41,9 @@ def _solve(P, g0, simt):
 
 
 @pytest.mark.parametrize("c,groups,shape", [(3, ELASTIC, (32, 32, 32)), (3, ELASTIC, (16, 8, 64)),
-                                            (1, THERMAL, (32, 16, 32)), (3, ELASTIC, (20, 24, 32))])
+                                            (1, THERMAL, (32, 16, 32)), (3, ELASTIC, (20, 24, 32)),
+                                            (3, ELASTIC, (12, 14, 18)), (3, ELASTIC, (70, 4, 66)),
+                                            (1, THERMAL, (6, 10, 36))])
 def test_tensor_operator_matches_cuda_core_operator(c, groups, shape):
     ms = random_ms(shape, vf=0.3, seed=21)
     P = oracle_problem(ms, c, groups, "HEX8")
