@@ -226,68 +226,108 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
 // ------------------------------------------------------------------ z inv ---
 // Hermitian pack of the half spectrum, half-length inverse, real rows scaled by
 // `sign`; fused partial <r, s> (solverCG.h:90-92) with delta/beta in the last block.
+// Persistent: each CTA loops over blocks of R rows, and while one block is
+// transformed cp.async brings the next block's spectrum rows (and, for the
+// fused dot, its r rows) into the other buffer, so the DRAM reads overlap the
+// transforms instead of alternating with them.
 template <typename T, int N1, int N2, int R>
-__global__ void __launch_bounds__(R * N1) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
+__global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
 {
-    constexpr int M = N1 * N2, EP = N1 + 1;
-    __shared__ cplx<T> X[R * (M + N2)]; // spectrum rows (stride M+1), then the exchange (R*N2*EP)
-    __shared__ cplx<T> Zp[R * M];
-    __shared__ double  red_smem[32];
+    constexpr int M = N1 * N2, EP = N1 + 1, XS = R * (M + N2); // spectrum rows (stride M+1), then the exchange
+    extern __shared__ __align__(16) unsigned char zsm[];
+    cplx<T>          *Xb = reinterpret_cast<cplx<T> *>(zsm); // [2][XS]
+    cplx<T>          *Rb = Xb + 2 * XS;                      // [2][R*M] r rows
+    cplx<T>          *Zp = Rb + 2 * R * M;                   // [R*M] packed half-length rows
+    __shared__ double red_smem[32];
     const int       t = threadIdx.x, L = t / N1, w = t % N1;
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
-    const long long row0  = (long long)blockIdx.x * R;
-    for (int i = t; i < R * (M + 1); i += blockDim.x) {
-        const int Lr = i / (M + 1), k = i % (M + 1);
-        X[i] = (row0 + Lr < nrows) ? p.spec[(row0 + Lr) * p.nzp + k] : cplx<T>{0, 0};
-    }
-    __syncthreads();
-    for (int i = t; i < R * M; i += blockDim.x) {
-        const int Lr = i / M, k = i % M;
-        cplx<T>   xk = X[Lr * (M + 1) + k];
-        cplx<T>   xm = X[Lr * (M + 1) + (M - k)];
-        if (k == 0) {
-            xk.y = 0;
-            xm.y = 0;
-        }
-        xm.y      = -xm.y;
-        cplx<T> Ev = cadd(xk, xm);
-        cplx<T> Od = cmulc(csub(xk, xm), p.tw_r2c[k]);
-        Zp[i]      = cplx<T>{Ev.x - Od.y, Ev.y + Od.x};
-    }
-    __syncthreads();
-    cplx<T> *E = X; // reuse as the exchange buffer: R * N2 * EP = R * (M + N2)
-    cplx<T>  v[N2];
-#pragma unroll
-    for (int j2 = 0; j2 < N2; ++j2)
-        v[j2] = Zp[L * M + w + N1 * j2];
-    line_phase1<T, N1, N2, true>(v, w, p.tw_z);
-#pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2)
-        E[(L * N2 + k2) * EP + w] = v[k2];
-    __syncthreads();
-    const long long row   = row0 + L;
-    const bool      valid = row < nrows && w < N2;
-    T               dot   = (T)0;
-    if (valid) {
-        cplx<T> u[N1];
-#pragma unroll
-        for (int j1 = 0; j1 < N1; ++j1)
-            u[j1] = E[(L * N2 + w) * EP + j1];
-        Dft<T, N1, true>::run(u);
-        cplx<T>       *sout = reinterpret_cast<cplx<T> *>(a.s) + row * M;
-        const cplx<T> *rin  = reinterpret_cast<const cplx<T> *>(a.r) + row * M;
-        const T        sg   = (T)a.sign;
-#pragma unroll
-        for (int k1 = 0; k1 < N1; ++k1) {
-            const int m = w + N2 * k1;
-            cplx<T>   z = {sg * u[k1].x, sg * u[k1].y};
-            sout[m]     = z;
+    const long long nblk  = (nrows + R - 1) / R;
+    auto fetch = [&](long long blk, int b) {
+        if (blk < nblk) {
+            const long long row0 = blk * R;
+            const int       nval = (int)(nrows - row0 < R ? nrows - row0 : R);
+            cplx<T>        *X    = Xb + b * XS;
+            for (int i = t; i < R * (M + 1); i += blockDim.x) {
+                const int Lr = i / (M + 1), k = i % (M + 1);
+                if (Lr < nval)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                                     (uint32_t)__cvta_generic_to_shared(X + i)),
+                                 "l"(p.spec + (row0 + Lr) * p.nzp + k), "n"(sizeof(cplx<T>))
+                                 : "memory");
+                else
+                    X[i] = cplx<T>{0, 0};
+            }
             if (a.reduce) {
-                const cplx<T> rv = rin[m];
-                dot += rv.x * z.x + rv.y * z.y;
+                constexpr int  Q    = 16 / (int)sizeof(cplx<T>); // complex values per 16-byte copy
+                const cplx<T> *rin0 = reinterpret_cast<const cplx<T> *>(a.r) + row0 * M;
+                cplx<T>       *Rr   = Rb + b * R * M;
+                for (int i = t * Q; i < nval * M; i += blockDim.x * Q)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                                     (uint32_t)__cvta_generic_to_shared(Rr + i)),
+                                 "l"(rin0 + i)
+                                 : "memory");
             }
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    T dot = (T)0;
+    fetch(blockIdx.x, 0);
+    int it = 0;
+    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++it) {
+        const int b = it & 1;
+        fetch(blk + gridDim.x, b ^ 1);                       // the next block, into the other buffer
+        asm volatile("cp.async.wait_group 1;" ::: "memory"); // this block's copies (this thread's) ...
+        __syncthreads();                                     // ... and everyone else's
+        cplx<T>        *X    = Xb + b * XS;
+        const long long row0 = blk * R;
+        for (int i = t; i < R * M; i += blockDim.x) {
+            const int Lr = i / M, k = i % M;
+            cplx<T>   xk = X[Lr * (M + 1) + k];
+            cplx<T>   xm = X[Lr * (M + 1) + (M - k)];
+            if (k == 0) {
+                xk.y = 0;
+                xm.y = 0;
+            }
+            xm.y      = -xm.y;
+            cplx<T> Ev = cadd(xk, xm);
+            cplx<T> Od = cmulc(csub(xk, xm), p.tw_r2c[k]);
+            Zp[i]      = cplx<T>{Ev.x - Od.y, Ev.y + Od.x};
+        }
+        __syncthreads();
+        cplx<T> *E = X; // the spectrum rows are consumed: reuse as the exchange (R * N2 * EP = XS)
+        cplx<T>  v[N2];
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2)
+            v[j2] = Zp[L * M + w + N1 * j2];
+        line_phase1<T, N1, N2, true>(v, w, p.tw_z);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2)
+            E[(L * N2 + k2) * EP + w] = v[k2];
+        __syncthreads();
+        const long long row = row0 + L;
+        if (row < nrows && w < N2) {
+            cplx<T> u[N1];
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1)
+                u[j1] = E[(L * N2 + w) * EP + j1];
+            Dft<T, N1, true>::run(u);
+            cplx<T>       *sout = reinterpret_cast<cplx<T> *>(a.s) + row * M;
+            const cplx<T> *rr   = Rb + b * R * M + L * M;
+            const T        sg   = (T)a.sign;
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) {
+                const int m = w + N2 * k1;
+                cplx<T>   z = {sg * u[k1].x, sg * u[k1].y};
+                sout[m]     = z;
+                if (a.reduce) {
+                    const cplx<T> rv = rr[m];
+                    dot += rv.x * z.x + rv.y * z.y;
+                }
+            }
+        }
+        __syncthreads(); // buffers b and Zp are free for the fetch two blocks on
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     if (a.reduce) {
         double    vv[1]  = {(double)dot};
         const int ops[1] = {RED_SUM};
@@ -351,11 +391,24 @@ void go_zf(const ConvPlan<T> &p, const T *r, cudaStream_t st)
 }
 
 template <typename T, int N1, int N2>
-void go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
+cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
 {
-    constexpr int   R     = ZRows<T, N1>::value;
+    constexpr int   R     = ZRows<T, N1>::value, M = N1 * N2;
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
-    k_z_inv_reg<T, N1, N2, R><<<(int)((nrows + R - 1) / R), R * N1, 0, st>>>(p, a);
+    const long long nblk  = (nrows + R - 1) / R;
+    static int      nsm   = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const int    grid = (int)(nblk < 2LL * nsm ? nblk : 2LL * nsm); // persistent: two CTAs per SM
+    const size_t sm   = sizeof(cplx<T>) * (size_t)(2 * R * (M + N2) + 3 * R * M);
+    cudaError_t  e    = allow_max_dyn_smem(k_z_inv_reg<T, N1, N2, R>);
+    if (e != cudaSuccess)
+        return e;
+    k_z_inv_reg<T, N1, N2, R><<<grid, R * N1, sm, st>>>(p, a);
+    return cudaSuccess;
 }
 
 // call F<N1, N2>() for the register plan of length n; false if none
@@ -413,7 +466,9 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
     mark(3);
     with_plan(p.g.ny, [&]<int N1, int N2>() { go_y<T, N1, N2, true>(p, st); });
     mark(4);
-    with_plan_z(p.M, [&]<int N1, int N2>() { go_zi<T, N1, N2>(p, a, st); });
+    with_plan_z(p.M, [&]<int N1, int N2>() { e = go_zi<T, N1, N2>(p, a, st); });
+    if (e != cudaSuccess)
+        return e;
     mark(5);
     return cudaGetLastError();
 }
