@@ -29,7 +29,7 @@ FIELD_PLASTIC_STRAIN, FIELD_HARDENING = 5, 6
 FIELD_STRAIN_GP, FIELD_STRESS_GP, FIELD_PLASTIC_STRAIN_GP, FIELD_HARDENING_GP = 7, 8, 9, 10
 FIELD_PLASTIC_FLAG = 11
 FIELD_KINEMATIC, FIELD_KINEMATIC_GP = 12, 13
-VOXEL_STIFFNESS_SCALE = 0
+VOXEL_STIFFNESS_SCALE, VOXEL_YIELD_STRESS = 0, 1
 
 FE_TYPES = {"HEX8": HEX8, "HEX8R": HEX8R, "BBAR": BBAR}
 MEASURES = {"L1": L1, "L2": L2, "Linfinity": LINF}
@@ -45,7 +45,7 @@ EXPORTS = [
     "fansgpu_green_table", "fansgpu_version", "fansgpu_reset", "fansgpu_get_stream", "fansgpu_set_timing",
     "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc", "fansgpu_set_refresh",
     "fansgpu_enable_mixed_bc", "fansgpu_disable_mixed_bc", "fansgpu_get_gradient", "fansgpu_set_voxel_field",
-    "fansgpu_store_solution", "fansgpu_stiffness_gradient", "fansgpu_solve_batch",
+    "fansgpu_store_solution", "fansgpu_stiffness_gradient", "fansgpu_solve_batch", "fansgpu_yield_stress_adjoint",
 ]
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
                 "residual64", "norm", "green_table", "strain_stress"]
@@ -132,6 +132,7 @@ def _declare(L):
     L.fansgpu_store_solution.argtypes = [vp, ip]
     L.fansgpu_stiffness_gradient.argtypes = [vp, ip, dp, dp]
     L.fansgpu_solve_batch.argtypes = [ctypes.POINTER(vp), ip, ctypes.POINTER(Stats), i32p]
+    L.fansgpu_yield_stress_adjoint.argtypes = [vp, ip, dp, ip, dp, ctypes.c_double, dp, dp, i32p]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

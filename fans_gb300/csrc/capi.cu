@@ -92,6 +92,7 @@ struct fansgpu_ctx {
 
     // per-voxel stiffness scale and stored solutions for the stiffness sensitivity
     double             *vscale = nullptr, *zero_g0 = nullptr, *stored_u = nullptr;
+    double             *vyield = nullptr; // per-voxel initial yield stress of J2PlasticityNew elements
     std::vector<double> stored_g0;
     std::vector<char>   stored_ok;
 
@@ -583,6 +584,7 @@ ElementArgs element_args(fansgpu_ctx *ctx, const double *u, int mode)
     a.red_site     = SITE_EL;
     a.phase_filter = -1;
     a.scale        = ctx->vscale;
+    a.sy           = ctx->vyield;
     return a;
 }
 
@@ -1276,7 +1278,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d,
                     ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc, ctx->pb_t, ctx->pb,
-                    ctx->vscale, ctx->zero_g0, ctx->stored_u};
+                    ctx->vscale, ctx->zero_g0, ctx->stored_u, ctx->vyield};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -1552,25 +1554,27 @@ int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *value
 {
     if (!ctx)
         return FANSGPU_EINVAL;
-    if (field != FANSGPU_VOXEL_STIFFNESS_SCALE)
+    if (field != FANSGPU_VOXEL_STIFFNESS_SCALE && field != FANSGPU_VOXEL_YIELD_STRESS)
         return fail(ctx, FANSGPU_EINVAL, "unknown voxel field %d", field);
+    const bool yield = field == FANSGPU_VOXEL_YIELD_STRESS;
+    double   *&dst   = yield ? ctx->vyield : ctx->vscale;
     if (!values) { // back to the phase table alone
-        if (ctx->vscale)
-            cudaFree(ctx->vscale);
-        ctx->vscale = nullptr;
+        if (dst)
+            cudaFree(dst);
+        dst = nullptr;
         return 0;
     }
     for (long long i = 0; i < ctx->N; ++i)
         if (!(values[i] > 0.0) || !std::isfinite(values[i]))
-            return fail(ctx, FANSGPU_EINVAL, "stiffness scale must be positive and finite (voxel %lld)", i);
+            return fail(ctx, FANSGPU_EINVAL, "%s must be positive and finite (voxel %lld)",
+                        yield ? "yield stress" : "stiffness scale", i);
     int rc;
-    if ((!ctx->vscale && (rc = dalloc(ctx, &ctx->vscale, ctx->N))) || (rc = ensure_rows(ctx)) ||
+    if ((!dst && (rc = dalloc(ctx, &dst, ctx->N))) || (rc = ensure_rows(ctx)) ||
         (!ctx->zero_g0 && (rc = dalloc(ctx, &ctx->zero_g0, 9))))
         return rc;
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->zero_g0, 0, sizeof(double) * 9, ctx->st));
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->staging, values, sizeof(double) * ctx->N, cudaMemcpyHostToDevice, ctx->st));
-    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->vscale, ctx->staging, sizeof(double) * ctx->N, cudaMemcpyDeviceToDevice,
-                                    ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(dst, ctx->staging, sizeof(double) * ctx->N, cudaMemcpyDeviceToDevice, ctx->st));
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
     return 0;
 }
@@ -1636,6 +1640,218 @@ int fansgpu_stiffness_gradient(fansgpu_ctx *ctx, int32_t n, const double *W, dou
         e = cudaStreamSynchronize(ctx->st);
     cudaFree(g0w);
     return e == cudaSuccess ? 0 : fail(ctx, FANSGPU_ECUDA, "stiffness gradient: %s", cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// Yield-stress adjoint of a strain-controlled J2PlasticityNew load path.
+
+// The adjoint kernel's arguments for the state of one load step.
+AdjArgs adj_args(fansgpu_ctx *ctx, const double *u_n, const double *g0_n, const double *ep_in, const double *q_in)
+{
+    AdjArgs a{};
+    a.g     = ctx->g;
+    a.ngp   = ctx->ngp;
+    a.u     = u_n;
+    a.g0    = g0_n;
+    a.ep_in = ep_in;
+    a.q_in  = q_in;
+    a.ms    = ctx->d_ms;
+    a.B     = ctx->Bgp_d;
+    a.law   = ctx->law_d;
+    a.Cph   = ctx->Cph;
+    a.prm   = ctx->prm_d;
+    a.sy    = ctx->vyield;
+    a.ve    = ctx->ve;
+    a.rows  = ctx->rows;
+    return a;
+}
+
+// Linear CG (the flexible CG recurrences of solverCG.h:62-117 with the Green's
+// operator as preconditioner) for K_n^T lambda + f_n = 0 from lambda = 0, to a
+// relative L2 residual of rel_tol.  `a` carries the step's state, mu_n and the
+// seed; the context's CG vectors are its scratch.
+int adjoint_solve(fansgpu_ctx *ctx, AdjArgs a, double *lam, double rel_tol, int *iters)
+{
+    const long long n = ctx->n;
+    int             rc;
+    *iters = 0;
+    FANS_CUDA_CHECK(cudaMemsetAsync(lam, 0, sizeof(double) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s, 0, sizeof(double) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->dd[0], 0, sizeof(double) * n, ctx->st));
+    ctx->cur_d = 0;
+    if ((rc = init_scalars(ctx)))
+        return rc;
+    a.mode = ADJ_RESIDUAL;
+    a.x    = lam;
+    FANS_CUDA_CHECK(launch_adjoint(a, ctx->st));
+    FANS_CUDA_CHECK(launch_gather(ctx->rows, ctx->r, ctx->g, ctx->C, ctx->st));
+    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, FANSGPU_L2, ctx->scal, 1, nullptr, ctx->red, SITE_NORM,
+                                               ctx->st));
+    if ((rc = sync_scalars(ctx)))
+        return rc;
+    const double err0 = ctx->scal_h->err;
+    if (!std::isfinite(err0))
+        return fail(ctx, FANSGPU_ENAN, "yield-stress adjoint: non-finite adjoint load");
+    double err = err0;
+    while (err > rel_tol * err0 && *iters < ctx->tol.n_it) {
+        ConvArgs ca{ctx->r, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+        FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
+        double *dn = ctx->dd[ctx->cur_d ^ 1];
+        FANS_CUDA_CHECK(cudaMemcpyAsync(dn, ctx->dd[ctx->cur_d], sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                        ctx->st));
+        FANS_CUDA_CHECK(launch_direction(dn, ctx->s, n, ctx->scal, ctx->st));
+        a.mode = ADJ_OPERATOR;
+        a.x    = dn;
+        FANS_CUDA_CHECK(launch_adjoint(a, ctx->st));
+        FANS_CUDA_CHECK(launch_gather(ctx->rows, ctx->Kd, ctx->g, ctx->C, ctx->st));
+        FANS_CUDA_CHECK(launch_dot(dn, ctx->Kd, n, &ctx->scal->dAd, ctx->red, SITE_DOT, ctx->st));
+        FANS_CUDA_CHECK(launch_set_alpha(ctx->scal, ctx->st));
+        ctx->cur_d ^= 1;
+        UpdateArgs ua{n, ctx->r, ctx->Kd, lam, dn, ctx->s, FANSGPU_L2, 1, ctx->scal, ctx->red, SITE_UPDATE};
+        FANS_CUDA_CHECK((launch_cg_update<double, double>(ua, ctx->st)));
+        if ((rc = sync_scalars(ctx)))
+            return rc;
+        ++*iters;
+        err = ctx->scal_h->err;
+        if (ctx->scal_h->converged < 0 || !std::isfinite(err))
+            return fail(ctx, FANSGPU_ENAN, "yield-stress adjoint: non-finite residual at iteration %d", *iters);
+    }
+    if (err > rel_tol * err0)
+        return fail(ctx, FANSGPU_ENOTCONV, "yield-stress adjoint: CG reached %d iterations at relative residual %g",
+                    *iters, err / err0);
+    return 0;
+}
+
+// Device buffers of one adjoint run, freed on every exit path.
+struct AdjBuffers {
+    double *U = nullptr, *ck = nullptr, *seg = nullptr, *mu = nullptr, *lam = nullptr, *grad = nullptr,
+           *path = nullptr, *cw = nullptr, *rsave = nullptr;
+    ~AdjBuffers()
+    {
+        for (double *p : {U, ck, seg, mu, lam, grad, path, cw, rsave})
+            if (p)
+                cudaFree(p);
+    }
+};
+
+int fansgpu_yield_stress_adjoint(fansgpu_ctx *ctx, int32_t n_steps, const double *g0_path, int32_t every,
+                                 const double *w, double rel_tol, double *stress_final, double *grad,
+                                 int32_t *iterations)
+{
+    if (!ctx || !g0_path || !w || !grad)
+        return FANSGPU_EINVAL;
+    if (n_steps < 1 || every < 1)
+        return fail(ctx, FANSGPU_EINVAL, "yield-stress adjoint: n_steps >= 1 and checkpoint_every >= 1 required");
+    if (!(rel_tol > 0.0 && rel_tol < 1.0))
+        return fail(ctx, FANSGPU_EINVAL, "yield-stress adjoint: rel_tol must lie in (0, 1)");
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    if (ctx->C != 3 || ctx->nstr != 6)
+        return fail(ctx, FANSGPU_EUNSUPPORTED, "yield-stress adjoint: small-strain mechanics only");
+    if (ctx->mixed_active || ctx->vscale || ctx->desc.method != FANSGPU_CG)
+        return fail(ctx, FANSGPU_EUNSUPPORTED,
+                    "yield-stress adjoint: strain control with the CG solver and no stiffness scale field only");
+    bool any_j2 = false;
+    for (int ph = 0; ph < ctx->nph; ++ph) {
+        const int law = ctx->law[ph];
+        if (law == FANSGPU_LAW_J2_LINEAR)
+            any_j2 = true;
+        else if (law != FANSGPU_LAW_ELASTIC_ISO && law != FANSGPU_LAW_ELASTIC_TRI)
+            return fail(ctx, FANSGPU_EUNSUPPORTED,
+                        "yield-stress adjoint: phase %d: only J2PlasticityNew and linear elastic laws", ph);
+    }
+    if (!any_j2 || !ctx->ep_t)
+        return fail(ctx, FANSGPU_EUNSUPPORTED, "yield-stress adjoint: no J2PlasticityNew phase");
+    const long long N = ctx->N, n = ctx->n, nal = 7LL * ctx->ngp * N, nep = 6LL * ctx->ngp * N;
+    const int       nseg = (n_steps + every - 1) / every;
+    AdjBuffers      b;
+    if ((rc = dalloc(ctx, &b.U, (size_t)n_steps * n)) || (rc = dalloc(ctx, &b.ck, (size_t)nseg * nal)) ||
+        (every > 1 && (rc = dalloc(ctx, &b.seg, (size_t)(every - 1) * nal))) || (rc = dalloc(ctx, &b.mu, nal)) ||
+        (rc = dalloc(ctx, &b.lam, n)) || (rc = dalloc(ctx, &b.grad, N)) ||
+        (rc = dalloc(ctx, &b.path, (size_t)n_steps * 6)) || (rc = dalloc(ctx, &b.cw, 6)) ||
+        (rc = dalloc(ctx, &b.rsave, n)))
+        return rc;
+    auto alpha = [&](int m, int c, int sgi) -> double * { // committed state after step m (c <= m < c + every)
+        return m == c ? b.ck + (size_t)sgi * nal : b.seg + (size_t)(m - c - 1) * nal;
+    };
+
+    // forward: the load path as runSolver drives it (main.cpp:23-42), keeping
+    // every converged u_n and the committed state at every checkpoint
+    FANS_CUDA_CHECK(cudaMemcpyAsync(b.ck, ctx->ep_t, sizeof(double) * nep, cudaMemcpyDeviceToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(b.ck + nep, ctx->q_t, sizeof(double) * ctx->ngp * N, cudaMemcpyDeviceToDevice,
+                                    ctx->st));
+    for (int k = 1; k <= n_steps; ++k) {
+        if ((rc = fansgpu_set_gradient(ctx, g0_path + 6 * (k - 1))))
+            return rc;
+        fansgpu_stats st{};
+        if ((rc = fansgpu_solve(ctx, &st)))
+            return rc == FANSGPU_ENOTCONV
+                       ? fail(ctx, rc, "yield-stress adjoint: load step %d did not converge (%d iterations)", k,
+                              st.iterations)
+                       : rc;
+        if (iterations)
+            iterations[k - 1] = st.iterations;
+        FANS_CUDA_CHECK(cudaMemcpyAsync(b.U + (size_t)(k - 1) * n, ctx->u, sizeof(double) * n,
+                                        cudaMemcpyDeviceToDevice, ctx->st));
+        if (k % every == 0 && k < n_steps) {
+            double *c = b.ck + (size_t)(k / every) * nal;
+            FANS_CUDA_CHECK(cudaMemcpyAsync(c, ctx->ep_t, sizeof(double) * nep, cudaMemcpyDeviceToDevice, ctx->st));
+            FANS_CUDA_CHECK(cudaMemcpyAsync(c + nep, ctx->q_t, sizeof(double) * ctx->ngp * N,
+                                            cudaMemcpyDeviceToDevice, ctx->st));
+        }
+        if (k < n_steps && (rc = fansgpu_extrapolate_displacement(ctx)))
+            return rc;
+    }
+    double sig[9];
+    if ((rc = fansgpu_homogenized_stress(ctx, sig)))
+        return rc;
+    if (stress_final)
+        for (int i = 0; i < 6; ++i)
+            stress_final[i] = sig[i];
+    FANS_CUDA_CHECK(cudaMemcpyAsync(b.rsave, ctx->r, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+
+    // reverse sweep, one checkpoint segment at a time: replay the segment's
+    // committed states from its checkpoint, then run its steps backwards
+    double cw[6];
+    for (int i = 0; i < 6; ++i)
+        cw[i] = w[i] / ((double)N * ctx->ngp);
+    FANS_CUDA_CHECK(cudaMemcpyAsync(b.path, g0_path, sizeof(double) * 6 * n_steps, cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(b.cw, cw, sizeof(cw), cudaMemcpyHostToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(b.mu, 0, sizeof(double) * nal, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(b.grad, 0, sizeof(double) * N, ctx->st));
+    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+        const int c = sgi * every, end = std::min(c + every, (int)n_steps);
+        for (int m = c + 1; m < end; ++m) {
+            const double *ain = alpha(m - 1, c, sgi);
+            AdjArgs       a   = adj_args(ctx, b.U + (size_t)(m - 1) * n, b.path + 6 * (m - 1), ain, ain + nep);
+            double       *out = alpha(m, c, sgi);
+            a.mode            = ADJ_REPLAY;
+            a.ep_out          = out;
+            a.q_out           = out + nep;
+            FANS_CUDA_CHECK(launch_adjoint(a, ctx->st));
+        }
+        for (int m = end; m > c; --m) {
+            const double *ain = alpha(m - 1, c, sgi);
+            AdjArgs       a   = adj_args(ctx, b.U + (size_t)(m - 1) * n, b.path + 6 * (m - 1), ain, ain + nep);
+            a.mu_ep           = b.mu;
+            a.mu_q            = b.mu + nep;
+            a.cw              = m == n_steps ? b.cw : nullptr;
+            int its           = 0;
+            if ((rc = adjoint_solve(ctx, a, b.lam, rel_tol, &its)))
+                return rc;
+            if (iterations)
+                iterations[n_steps + m - 1] = its;
+            a.mode = ADJ_STEP;
+            a.x    = b.lam;
+            a.grad = b.grad;
+            FANS_CUDA_CHECK(launch_adjoint(a, ctx->st));
+        }
+    }
+    FANS_CUDA_CHECK(cudaMemcpyAsync(grad, b.grad, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->st));
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->r, b.rsave, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
 }
 
 int fansgpu_disable_mixed_bc(fansgpu_ctx *ctx)

@@ -14,6 +14,7 @@
 // Internal variables are SoA: eps_p[6][n_gp][N], q[n_gp][N] (trial and
 // committed copies), in FP64.
 #include "../../include/fans_gb300.h"
+#include "j2_law.cuh"
 #include "kernels.cuh"
 
 namespace fansgpu {
@@ -22,61 +23,6 @@ namespace {
 
 constexpr int kElThreads = 128;
 constexpr int kPrm       = 8; // law parameters per phase
-
-__device__ __forceinline__ void elem_nodes(int nx, int ny, int nz, long long e, long long idx[8])
-{
-    const int z = (int)(e % nz), y = (int)((e / nz) % ny), x = (int)(e / ((long long)nz * ny));
-    const int x1 = x + 1 == nx ? 0 : x + 1, y1 = y + 1 == ny ? 0 : y + 1, z1 = z + 1 == nz ? 0 : z + 1;
-    idx[0] = ((long long)x * ny + y) * nz + z;
-    idx[1] = ((long long)x1 * ny + y) * nz + z;
-    idx[2] = ((long long)x * ny + y1) * nz + z;
-    idx[3] = ((long long)x1 * ny + y1) * nz + z;
-    idx[4] = ((long long)x * ny + y) * nz + z1;
-    idx[5] = ((long long)x1 * ny + y) * nz + z1;
-    idx[6] = ((long long)x * ny + y1) * nz + z1;
-    idx[7] = ((long long)x1 * ny + y1) * nz + z1;
-}
-
-// J2PlasticityNew::get_sigma (J2PlasticityNew.h:43-108), one Gauss point.
-__device__ __forceinline__ void j2_sigma(const double *prm, const double (&e)[6], const double (&ep_in)[6], double q_in,
-                                         double (&sig)[6], double (&ep_out)[6], double &q_out)
-{
-    const double K = prm[0], G = prm[1], sy0 = prm[2], h = prm[3];
-    const double c23 = sqrt(2.0 / 3.0);
-    double       s[6], st[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        s[i] = 2.0 * G * (e[i] - ep_in[i]);
-    const double lam = K - 2.0 / 3.0 * G;
-    const double tr  = e[0] + e[1] + e[2];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        s[i] += lam * tr;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        st[i] = s[i];
-    const double mean = (s[0] + s[1] + s[2]) / 3.0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        st[i] -= mean;
-    double n2 = 0.0;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        n2 += st[i] * st[i];
-    const double s_t    = sqrt(n2);
-    const double sy     = sy0 + q_in * h;
-    const double phi    = s_t - c23 * sy;
-    double       dgamma = phi / (2.0 * G + 2.0 / 3.0 * h);
-    if (dgamma < 0.0)
-        dgamma = 0.0;
-    const bool on = s_t > 1e-12;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        ep_out[i] = on ? ep_in[i] + dgamma * st[i] / s_t : ep_in[i];
-        sig[i]    = on ? s[i] - dgamma * 2.0 * G * st[i] / s_t : s[i];
-    }
-    q_out = q_in + c23 * dgamma;
-}
 
 // LargeStrainMechModel::get_sigma (LargeStrainMechModel.h:190-196) for
 // SaintVenantKirchhoff (S = lambda tr(E) I + 2 mu E, E = (F^T F - I)/2,
@@ -323,7 +269,8 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
 #pragma unroll
             for (int i = 0; i < 6; ++i)
                 ep_in[i] = a.ep_t[(long long)i * NGP * N + base];
-            j2_sigma(a.prm + ph * kPrm, e, ep_in, a.q_t[base], sig, ep_out, q_out);
+            const double *pj = a.prm + ph * kPrm;
+            j2_sigma(pj, a.sy ? a.sy[el] : pj[2], e, ep_in, a.q_t[base], sig, ep_out, q_out);
             if (a.ep) {
 #pragma unroll
                 for (int i = 0; i < 6; ++i)

@@ -108,6 +108,7 @@ struct ElementArgs {
     double        *strain_gp, *stress_gp; // [N][ngp][nstr] or null
     double        *flag;                  // [N] element mean of the Gauss-point plastic flags, or null
     const double  *scale;                 // [N] per-voxel stiffness scale (sigma *= scale[e]), or null
+    const double  *sy;                    // [N] per-voxel initial yield stress of J2 elements, or null (phase value)
     double        *out_red;         // [0,nstr) sum eps, [nstr,2nstr) sum sig, [2nstr] count
     GridRed        red;
     int            red_site;
@@ -127,6 +128,34 @@ struct SensArgs {
     double        *grad;  // [N]
 };
 cudaError_t launch_sensitivity(const SensArgs &a, cudaStream_t st);
+// Yield-stress adjoint of a strain-controlled J2PlasticityNew load path, one
+// kernel over (element, Gauss point) with the state of load step n: u_n, g0_n
+// and the committed internal variables alpha_{n-1} before the step.
+//   ADJ_OPERATOR: rows = B^T K_alg tau(x), tau = (v_e/n_gp) B x_e      (K_n^T x)
+//   ADJ_RESIDUAL: rows = B^T VJP_e(tau(x) + cw, mu_n)                   (K_n^T x + f_n)
+//   ADJ_STEP:     mu <- VJP_alpha(tau(x) + cw, mu_n), grad[e] += sum_gp VJP_sy
+//   ADJ_REPLAY:   alpha_n = return map(eps_n, alpha_{n-1}) into ep_out/q_out
+enum AdjMode { ADJ_OPERATOR = 0, ADJ_RESIDUAL = 1, ADJ_STEP = 2, ADJ_REPLAY = 3 };
+struct AdjArgs {
+    Grid3          g;
+    int            ngp, mode;
+    const double  *u, *g0;       // state of step n: u_n [3][N], g0_n (6)
+    const double  *x;            // adjoint field [3][N] (lambda or a CG direction)
+    const double  *ep_in, *q_in; // alpha_{n-1}: [6][ngp][N], [ngp][N]
+    double        *ep_out, *q_out; // ADJ_REPLAY: alpha_n
+    double        *mu_ep, *mu_q;   // mu_n, same layout; ADJ_STEP overwrites it with mu_{n-1}
+    const double  *cw;           // 6 doubles: w/(N n_gp), the seed of <sigma_N> (last step), or null
+    const uint8_t *ms;
+    const double  *B;            // ngp x 6 x 24
+    const int     *law;
+    const double  *Cph;          // per phase 6 x 6 (linear elastic laws)
+    const double  *prm;          // per phase, 8 law parameters
+    const double  *sy;           // [N] per-voxel initial yield stress, or null
+    double         ve;
+    double        *rows;         // [24][N]
+    double        *grad;         // [N], accumulated
+};
+cudaError_t launch_adjoint(const AdjArgs &a, cudaStream_t st);
 cudaError_t launch_set_alpha(CgScalars *scal, cudaStream_t st); // alpha = delta / dAd
 cudaError_t launch_gather(const double *rows, double *r, const Grid3 &g, int C, cudaStream_t st);
 cudaError_t launch_dot(const double *a, const double *b, long long n, double *out, GridRed red, int site,

@@ -48,3 +48,13 @@ class MicroSimulation:
 
     def close(self):
         self.solver.close()
+
+
+def __getattr__(name):
+    """The torch.autograd.Function front ends of the adjoints (fans_gb300.autograd),
+    importable from the binding without importing torch for MicroSimulation alone."""
+    if name in ("EffectiveStiffness", "YieldPathStress"):
+        from . import autograd
+
+        return getattr(autograd, name)
+    raise AttributeError(name)

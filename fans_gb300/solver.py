@@ -207,6 +207,30 @@ class Context:
         assert a.shape == self.n
         self._chk(self.lib.fansgpu_set_voxel_field(self.ctx, C.VOXEL_STIFFNESS_SCALE, _ptr(a)))
 
+    def set_voxel_yield_stress(self, sy):
+        """Per-voxel initial yield stress of J2PlasticityNew voxels ([x][y][z]); None clears it."""
+        if sy is None:
+            self._chk(self.lib.fansgpu_set_voxel_field(self.ctx, C.VOXEL_YIELD_STRESS, None))
+            return
+        a = np.ascontiguousarray(sy, dtype=float)
+        assert a.shape == self.n
+        self._chk(self.lib.fansgpu_set_voxel_field(self.ctx, C.VOXEL_YIELD_STRESS, _ptr(a)))
+
+    def yield_stress_adjoint(self, g0_path, w, checkpoint_every=5, rel_tol=1e-10):
+        """fansgpu_yield_stress_adjoint: run the strain-controlled path g0_path
+        (n_steps x 6) and return the final <sigma>, d(w . <sigma>)/d sigma_y per
+        voxel ([x][y][z]) and the forward / adjoint CG iterations per step."""
+        path = np.ascontiguousarray(g0_path, dtype=float).reshape(-1, 6)
+        w = np.ascontiguousarray(w, dtype=float).ravel()
+        assert w.size == 6
+        stress, grad = np.zeros(6), np.zeros(self.n)
+        its = np.zeros(2 * len(path), dtype=np.int32)
+        self._chk(self.lib.fansgpu_yield_stress_adjoint(
+            self.ctx, len(path), _ptr(path), int(checkpoint_every), _ptr(w), float(rel_tol), _ptr(stress), _ptr(grad),
+            its.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        return {"stress": stress, "grad": grad, "forward_iterations": its[: len(path)],
+                "adjoint_iterations": its[len(path):]}
+
     def store_solution(self, slot):
         self._chk(self.lib.fansgpu_store_solution(self.ctx, int(slot)))
 

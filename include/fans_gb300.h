@@ -185,6 +185,10 @@ int fansgpu_enable_mixed_bc(fansgpu_ctx *ctx, int32_t n_e, const int32_t *idx_e,
  * E(x) = s(x) E_phase at fixed Poisson ratio.  NULL clears it.  With a scale
  * set, solves run the FP64 path with the element kernel as operator. */
 #define FANSGPU_VOXEL_STIFFNESS_SCALE 0
+/* FANSGPU_VOXEL_YIELD_STRESS replaces the initial yield stress sigma_y of
+ * J2PlasticityNew (J2PlasticityNew.h:43-108, a per-phase parameter there) by
+ * values[e] > 0 in voxel e; other laws ignore it.  NULL clears it. */
+#define FANSGPU_VOXEL_YIELD_STRESS 1
 int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *values);
 
 /* Adjoint of the homogenized stiffness w.r.t. the per-voxel scale.  After
@@ -196,6 +200,30 @@ int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *value
  * row-major; grad holds n_x*n_y*n_z doubles [x][y][z].  Linear laws only. */
 int fansgpu_store_solution(fansgpu_ctx *ctx, int32_t slot);
 int fansgpu_stiffness_gradient(fansgpu_ctx *ctx, int32_t n, const double *W, double *grad);
+
+/* Adjoint of the final homogenized stress of a strain-controlled load path
+ * w.r.t. the per-voxel initial yield stress (J2PlasticityNew with linear
+ * isotropic hardening, linear elastic phases beside it; small strain, CG).
+ * Runs the path as runSolver does (main.cpp:23-42): for k = 1..n_steps,
+ * g0 = g0_path[k-1] (6 Mandel components), solve (committing the internal
+ * variables), extrapolate the displacement; starting from the context's
+ * current u and committed state.  It keeps every converged u_k and the
+ * committed internal variables every `checkpoint_every` steps, then sweeps
+ * backwards: per step one linear CG solve with the consistent tangent
+ * (K_k^T lambda_k = -f_k, relative L2 tolerance rel_tol, at most the
+ * context's n_it iterations), the states inside a checkpoint segment being
+ * recomputed from its checkpoint by the return map alone.
+ * Returns stress_final = <sigma> after the last step (n_str doubles, may be
+ * NULL), grad[e] = d(w . stress_final)/d sigma_y(e) ([x][y][z] doubles, zero in
+ * elastic voxels) and, if iterations is not NULL, the forward CG iterations of
+ * each step followed by the adjoint CG iterations of each step (2 n_steps
+ * ints).  The context ends in the state after the last step.  The gradient is
+ * that of the discrete converged path: the committed state at entry is taken
+ * as independent of sigma_y.  Device memory: n_steps displacement fields,
+ * ceil(n_steps / checkpoint_every) + checkpoint_every internal-variable sets. */
+int fansgpu_yield_stress_adjoint(fansgpu_ctx *ctx, int32_t n_steps, const double *g0_path, int32_t checkpoint_every,
+                                 const double *w, double rel_tol, double *stress_final, double *grad,
+                                 int32_t *iterations);
 
 /* Solver::disableMixedBC (solver.h:75-78). */
 int fansgpu_disable_mixed_bc(fansgpu_ctx *ctx);
