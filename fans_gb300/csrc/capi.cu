@@ -21,6 +21,12 @@ using namespace fansgpu;
 
 static std::string g_create_error;
 
+// Controls of the device-resident inner loop of the mixed CG.
+struct LoopCtl {
+    double err0, last_true, tol, reliable;
+    int    iter, n_it, relative, cap;
+};
+
 struct fansgpu_ctx {
     fansgpu_desc desc{};
     Grid3        g{};
@@ -108,7 +114,13 @@ struct fansgpu_ctx {
     // CUDA graphs of one mixed CG iteration (one per d ping-pong parity)
     bool            use_graphs   = true;
     bool            graphs_valid = false;
-    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr}; // device-resident inner loop, by starting d parity
+    cudaGraphExec_t iter_exec[2]  = {nullptr, nullptr}; // one iteration, by d parity (host-driven loop)
+    bool            loop_on_device = true; // false inside fansgpu_solve_batch: per-iteration graphs interleave
+                                           // better across many concurrent streams
+    LoopCtl        *ctl = nullptr, *ctl_h = nullptr;    // its controls (device, pinned host copy)
+    double         *hist = nullptr;                     // err of every iteration, by iteration number
+    int             hist_cap = 0;
     bool   tc_allowed = true; // FANSGPU_STENCIL=simt at create time selects the CUDA-core operator
 };
 
@@ -750,6 +762,130 @@ cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
     return e;
 }
 
+// After one graph-resident iteration (one thread): count it, record its
+// residual estimate, and halt the loop wherever the host loop would do more
+// than continue -- a reliable update or convergence test (est <= reliable *
+// last_true or est_rel <= tol), n_it reached, or an error flag (non-finite
+// norm, tensor-core wait timeout).  `first` is the check between the body's two
+// iterations: it gates the second through the IF node, and ends the WHILE loop
+// when it halts; the second check alone decides whether the loop goes on.
+__global__ void k_loop_check(LoopCtl *c, const CgScalars *scal, double *hist, cudaGraphConditionalHandle h_while,
+                             cudaGraphConditionalHandle h_if, int first)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    const int    it  = ++c->iter;
+    const double err = scal->err;
+    if (it < c->cap)
+        hist[it] = err;
+    const double est_rel = c->relative ? err / c->err0 : err;
+    const bool   halt = scal->converged < 0 || !(err == err) || est_rel <= c->tol || err <= c->reliable * c->last_true ||
+                      it >= c->n_it || it + 1 >= c->cap;
+    if (first) {
+        cudaGraphSetConditional(h_if, halt ? 0u : 1u);
+        if (halt)
+            cudaGraphSetConditional(h_while, 0u);
+    } else {
+        cudaGraphSetConditional(h_while, halt ? 0u : 1u);
+    }
+}
+
+// The inner loop as one CUDA graph per starting parity of the d ping-pong:
+//   WHILE(h_while) { iteration(p); check; IF(h_if) { iteration(p ^ 1); check } }
+// The two iterations are captured once and added as child graphs.
+int build_loop_graphs(fansgpu_ctx *ctx)
+{
+    int rc;
+    if (!ctx->ctl) {
+        if ((rc = dalloc(ctx, &ctx->ctl, 1)))
+            return rc;
+        FANS_CUDA_CHECK(cudaMallocHost((void **)&ctx->ctl_h, sizeof(LoopCtl)));
+    }
+    cudaGraph_t it[2] = {nullptr, nullptr};
+    cudaError_t e     = cudaSuccess;
+    for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
+        e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess)
+            break;
+        const cudaError_t ce = enqueue_mixed_iteration(ctx, p);
+        e                    = cudaStreamEndCapture(ctx->st, &it[p]);
+        if (ce != cudaSuccess)
+            e = ce;
+    }
+    for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
+        if (ctx->iter_exec[p])
+            cudaGraphExecDestroy(ctx->iter_exec[p]);
+        ctx->iter_exec[p] = nullptr;
+        e                 = cudaGraphInstantiate(&ctx->iter_exec[p], it[p], 0);
+    }
+    for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
+        if (ctx->graph_exec[p])
+            cudaGraphExecDestroy(ctx->graph_exec[p]);
+        ctx->graph_exec[p] = nullptr;
+        cudaGraph_t top    = nullptr;
+        e                  = cudaGraphCreate(&top, 0);
+        cudaGraphConditionalHandle hw = 0, hi = 0;
+        cudaGraphNodeParams        wp{}, ip{};
+        cudaGraphNode_t            wn, n1, n2, n3, m1, m2;
+        cudaGraph_t                body = nullptr, ib = nullptr;
+        if (e == cudaSuccess)
+            e = cudaGraphConditionalHandleCreate(&hw, top, 1, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            wp.type               = cudaGraphNodeTypeConditional;
+            wp.conditional.handle = hw;
+            wp.conditional.type   = cudaGraphCondTypeWhile;
+            wp.conditional.size   = 1;
+            e                     = cudaGraphAddNode(&wn, top, nullptr, nullptr, 0, &wp);
+        }
+        if (e == cudaSuccess) {
+            body = wp.conditional.phGraph_out[0];
+            e    = cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault);
+        }
+        LoopCtl         *c  = ctx->ctl;
+        const CgScalars *sc = ctx->scal;
+        double          *h  = ctx->hist;
+        int              f1 = 1, f0 = 0;
+        void            *a1[] = {&c, &sc, &h, &hw, &hi, &f1};
+        void            *a0[] = {&c, &sc, &h, &hw, &hi, &f0};
+        cudaKernelNodeParams kp{};
+        kp.func     = (void *)k_loop_check;
+        kp.gridDim  = dim3(1);
+        kp.blockDim = dim3(32);
+        if (e == cudaSuccess)
+            e = cudaGraphAddChildGraphNode(&n1, body, nullptr, 0, it[p]);
+        if (e == cudaSuccess) {
+            kp.kernelParams = a1;
+            e               = cudaGraphAddKernelNode(&n2, body, &n1, 1, &kp);
+        }
+        if (e == cudaSuccess) {
+            ip.type               = cudaGraphNodeTypeConditional;
+            ip.conditional.handle = hi;
+            ip.conditional.type   = cudaGraphCondTypeIf;
+            ip.conditional.size   = 1;
+            e                     = cudaGraphAddNode(&n3, body, &n2, nullptr, 1, &ip);
+        }
+        if (e == cudaSuccess) {
+            ib = ip.conditional.phGraph_out[0];
+            e  = cudaGraphAddChildGraphNode(&m1, ib, nullptr, 0, it[p ^ 1]);
+        }
+        if (e == cudaSuccess) {
+            kp.kernelParams = a0;
+            e               = cudaGraphAddKernelNode(&m2, ib, &m1, 1, &kp);
+        }
+        if (e == cudaSuccess)
+            e = cudaGraphInstantiate(&ctx->graph_exec[p], top, 0);
+        if (top)
+            cudaGraphDestroy(top);
+    }
+    for (cudaGraph_t g : it)
+        if (g)
+            cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+        return fail(ctx, FANSGPU_ECUDA, "inner-loop graph: %s", cudaGetErrorString(e));
+    ctx->graphs_valid = true;
+    return 0;
+}
+
 // Mixed precision: FANS's flexible CG run on FP32 fields (stencil, FFT
 // preconditioner, recursive residual) with FP64 dot products, an FP64
 // solution and reliable updates -- the true residual R(u) recomputed in FP64
@@ -780,38 +916,51 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     *refinements      = 0;
     double err_rel    = err_value(ctx, ctx->scal_h->err);
     double last_true  = ctx->scal_h->err;
+    if (ctx->use_graphs && !ctx->timing && ctx->hist_cap < ctx->tol.n_it + 2) {
+        if (ctx->hist)
+            cudaFree(ctx->hist);
+        ctx->hist = nullptr;
+        if ((rc = dalloc(ctx, &ctx->hist, (size_t)ctx->tol.n_it + 2)))
+            return rc;
+        ctx->hist_cap     = ctx->tol.n_it + 2;
+        ctx->graphs_valid = false; // the graphs hold the history pointer
+    }
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
+        int done = 1; // iterations run by this pass
         if (ctx->use_graphs && !ctx->timing && ctx->iter > 0) { // the first iteration runs uncaptured
-            // one CUDA graph per d ping-pong parity holds the iteration's 7 launches
-            if (!ctx->graphs_valid) {
-                for (int k = 0; k < 2; ++k) {
-                    if (ctx->graph_exec[k])
-                        cudaGraphExecDestroy(ctx->graph_exec[k]);
-                    ctx->graph_exec[k] = nullptr;
-                    cudaGraph_t g      = nullptr;
-                    FANS_CUDA_CHECK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-                    const cudaError_t ce = enqueue_mixed_iteration(ctx, k);
-                    const cudaError_t ee = cudaStreamEndCapture(ctx->st, &g);
-                    if (ce != cudaSuccess || ee != cudaSuccess) {
-                        if (g)
-                            cudaGraphDestroy(g);
-                        return fail(ctx, FANSGPU_ECUDA, "iteration graph capture: %s",
-                                    cudaGetErrorString(ce != cudaSuccess ? ce : ee));
-                    }
-                    const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec[k], g, 0);
-                    cudaGraphDestroy(g);
-                    if (ie != cudaSuccess)
-                        return fail(ctx, FANSGPU_ECUDA, "iteration graph instantiate: %s", cudaGetErrorString(ie));
-                }
-                ctx->graphs_valid = true;
-            }
+            if (!ctx->graphs_valid && (rc = build_loop_graphs(ctx)))
+                return rc;
+        }
+        if (ctx->use_graphs && !ctx->timing && ctx->iter > 0 && !ctx->loop_on_device) {
+            FANS_CUDA_CHECK(cudaGraphLaunch(ctx->iter_exec[ctx->cur_d], ctx->st));
+            if ((rc = sync_scalars(ctx)))
+                return rc;
+        } else if (ctx->use_graphs && !ctx->timing && ctx->iter > 0) {
+            // iterate on the device until the check kernel halts the loop
+            *ctx->ctl_h = LoopCtl{ctx->err_all[0], last_true, ctx->tol.tolerance, ctx->reliable_delta, ctx->iter,
+                                  ctx->tol.n_it, ctx->tol.type == FANSGPU_RELATIVE, ctx->hist_cap};
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->ctl, ctx->ctl_h, sizeof(LoopCtl), cudaMemcpyHostToDevice, ctx->st));
             FANS_CUDA_CHECK(cudaGraphLaunch(ctx->graph_exec[ctx->cur_d], ctx->st));
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->ctl_h, ctx->ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, ctx->st));
+            if ((rc = sync_scalars(ctx)))
+                return rc;
+            done = ctx->ctl_h->iter - ctx->iter;
+            if (done < 1 || ctx->iter + done > ctx->tol.n_it)
+                return fail(ctx, FANSGPU_ECUDA, "inner-loop graph ran %d iterations from %d", done, ctx->iter);
+            if (done > 1) { // the iterations it did not halt on only extend the history
+                std::vector<double> h(done - 1);
+                FANS_CUDA_CHECK(cudaMemcpyAsync(h.data(), ctx->hist + ctx->iter + 1, sizeof(double) * (done - 1),
+                                                cudaMemcpyDeviceToHost, ctx->st));
+                FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+                ctx->err_all.insert(ctx->err_all.end(), h.begin(), h.end());
+                ctx->iter += done - 1;
+            }
         } else {
             FANS_CUDA_CHECK(enqueue_mixed_iteration(ctx, ctx->cur_d));
+            if ((rc = sync_scalars(ctx)))
+                return rc;
         }
-        ctx->cur_d ^= 1;
-        if ((rc = sync_scalars(ctx)))
-            return rc;
+        ctx->cur_d ^= done & 1;
         ctx->iter++;
         if (ctx->scal_h->converged == -3)
             return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out at iteration %d",
@@ -1162,8 +1311,10 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     ctx->desc        = *desc;
     if (const char *ev = std::getenv("FANSGPU_STENCIL"))
         ctx->tc_allowed = std::strcmp(ev, "simt") != 0;
-    if (const char *ev = std::getenv("FANSGPU_GRAPHS"))
-        ctx->use_graphs = std::strcmp(ev, "0") != 0;
+    if (const char *ev = std::getenv("FANSGPU_GRAPHS")) { // "0": no graphs; "iter": one graph per iteration
+        ctx->use_graphs     = std::strcmp(ev, "0") != 0;
+        ctx->loop_on_device = std::strcmp(ev, "iter") != 0;
+    }
     ctx->g           = Grid3{n[0], n[1], n[2]};
     ctx->C           = desc->howmany;
     ctx->nstr        = desc->strain_type == FANSGPU_LARGE_STRAIN ? 9 : nstr_of(ctx->C);
@@ -1278,12 +1429,14 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d,
                     ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc, ctx->pb_t, ctx->pb,
-                    ctx->vscale, ctx->zero_g0, ctx->stored_u, ctx->vyield};
+                    ctx->vscale, ctx->zero_g0, ctx->stored_u, ctx->vyield, ctx->ctl, ctx->hist};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
     if (ctx->scal_h)
         cudaFreeHost(ctx->scal_h);
+    if (ctx->ctl_h)
+        cudaFreeHost(ctx->ctl_h);
     if (ctx->ev0)
         cudaEventDestroy(ctx->ev0);
     if (ctx->ev1)
@@ -1291,6 +1444,9 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
     for (auto e : ctx->tpool)
         cudaEventDestroy(e);
     for (auto g : ctx->graph_exec)
+        if (g)
+            cudaGraphExecDestroy(g);
+    for (auto g : ctx->iter_exec)
         if (g)
             cudaGraphExecDestroy(g);
     if (ctx->st)
@@ -1934,8 +2090,12 @@ int fansgpu_solve_batch(fansgpu_ctx *const *ctxs, int32_t n, fansgpu_stats *stat
     std::atomic<int>         next{0};
     for (int t = 0; t < nt; ++t)
         pool.emplace_back([&]() {
-            for (int i = next++; i < n; i = next++)
-                rc[i] = fansgpu_solve(ctxs[i], stats ? &stats[i] : nullptr);
+            for (int i = next++; i < n; i = next++) {
+                const bool keep         = ctxs[i]->loop_on_device;
+                ctxs[i]->loop_on_device = false;
+                rc[i]                   = fansgpu_solve(ctxs[i], stats ? &stats[i] : nullptr);
+                ctxs[i]->loop_on_device = keep;
+            }
         });
     for (auto &th : pool)
         th.join();
