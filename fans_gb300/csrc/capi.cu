@@ -16,6 +16,9 @@
 #include <vector>
 #include <thread>
 #include <atomic>
+#include <array>
+#include <map>
+#include <mutex>
 
 using namespace fansgpu;
 
@@ -122,6 +125,10 @@ struct fansgpu_ctx {
     double         *hist = nullptr;                     // err of every iteration, by iteration number
     int             hist_cap = 0;
     bool   tc_allowed = true; // FANSGPU_STENCIL=simt at create time selects the CUDA-core operator
+    bool   tc_slower  = false; // the autotuner measured the CUDA-core operator faster on this grid
+    int    tune       = 1;     // FANSGPU_TUNE: 1 FFT tiles (default), 3 + operator, 0 defaults, 2 forced
+    int    tune_force[3] = {0, 0, 0}; // forced z / y / x tile variants
+    bool   tuned      = false;
 };
 
 namespace fansgpu {
@@ -369,6 +376,8 @@ int upload_law_tables(fansgpu_ctx *ctx)
     return 0;
 }
 
+int autotune(fansgpu_ctx *ctx);
+
 // Per-phase tables, reference stiffness and Green's operator (lazy).
 int setup(fansgpu_ctx *ctx)
 {
@@ -431,7 +440,8 @@ int setup(fansgpu_ctx *ctx)
         ctx->K32h = K32;
         ctx->use_tc = false;
         ctx->graphs_valid = false;
-        if (ctx->tc_allowed && ctx->desc.precision == FANSGPU_MIXED && stencil_tc_supported(ctx->g, C, ctx->nph)) {
+        if (ctx->tc_allowed && !ctx->tc_slower && ctx->desc.precision == FANSGPU_MIXED &&
+            stencil_tc_supported(ctx->g, C, ctx->nph)) {
             std::vector<float> w(stencil_tc_weights(C, ctx->nph));
             stencil_tc_pack_weights(C, ctx->nph, K32.data(), w.data());
             if (ctx->Wtc)
@@ -521,7 +531,7 @@ int setup(fansgpu_ctx *ctx)
         FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
         ctx->force_dirty = false;
     }
-    return 0;
+    return autotune(ctx);
 }
 
 // y = K x (+F) in FP64 (optionally FP32), no fusion.
@@ -726,13 +736,8 @@ int solve_cg64(fansgpu_ctx *ctx)
 
 // One inner iteration of the mixed CG on the context stream: s = -G*r with
 // delta/beta, d = s + beta d_old with K d and alpha, then the FP32 update.
-cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
+StencilArgs mixed_operator_args(fansgpu_ctx *ctx, int cd)
 {
-    const long long n = ctx->n;
-    ConvArgs        ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
-    cudaError_t     e = run_conv<float>(ctx, ctx->cp32, ca);
-    if (e != cudaSuccess)
-        return e;
     StencilArgs sa{};
     sa.g        = ctx->g;
     sa.C        = ctx->C;
@@ -749,8 +754,19 @@ cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
     sa.scal     = ctx->scal;
     sa.red      = ctx->red;
     sa.red_site = SITE_STENCIL;
-    int e0      = tk_mark(ctx);
-    e           = ctx->use_tc ? launch_stencil_tc(sa, ctx->Wtc, ctx->nph, ctx->st) : launch_stencil<float>(sa, ctx->st);
+    return sa;
+}
+
+cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
+{
+    const long long n = ctx->n;
+    ConvArgs        ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+    cudaError_t     e = run_conv<float>(ctx, ctx->cp32, ca);
+    if (e != cudaSuccess)
+        return e;
+    const StencilArgs sa = mixed_operator_args(ctx, cd);
+    int               e0 = tk_mark(ctx);
+    e = ctx->use_tc ? launch_stencil_tc(sa, ctx->Wtc, ctx->nph, ctx->st) : launch_stencil<float>(sa, ctx->st);
     if (e != cudaSuccess)
         return e;
     tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
@@ -760,6 +776,97 @@ cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
     e      = launch_cg_update<float, float>(ua, ctx->st);
     tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
     return e;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuning: the register FFT passes' tile variants (per precision) and, with
+// FANSGPU_TUNE=all, tensor-core against CUDA-core operator on the mixed path.
+// Runs once per context on its first setup, timed with CUDA events on the
+// context stream on scratch fields (the solve re-initialises them); results
+// are cached per grid for the process, so equal grids get equal choices.  The
+// operator is left out by default: timed alone on a small grid the CUDA-core
+// operator can win (it fills more SMs), while many contexts sharing the GPU
+// (fansgpu_solve_batch) run faster on the tensor-core one.
+struct TuneChoice {
+    int v64[3], v32[3];
+    int tc_slower;
+};
+std::mutex                             g_tune_mu;
+std::map<std::array<int, 6>, TuneChoice> g_tune_cache;
+
+float time_mixed_operator(fansgpu_ctx *ctx, bool tc)
+{
+    const StencilArgs sa = mixed_operator_args(ctx, 0);
+    cudaEvent_t       e0 = nullptr, e1 = nullptr;
+    float             ms = 1e30f;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return ms;
+    auto launch = [&] {
+        return tc ? launch_stencil_tc(sa, ctx->Wtc, ctx->nph, ctx->st) : launch_stencil<float>(sa, ctx->st);
+    };
+    if (launch() == cudaSuccess && cudaEventRecord(e0, ctx->st) == cudaSuccess) {
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; ++k)
+            ok = launch() == cudaSuccess;
+        if (ok && cudaEventRecord(e1, ctx->st) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess)
+            cudaEventElapsedTime(&ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms;
+}
+
+int autotune(fansgpu_ctx *ctx)
+{
+    if (ctx->tuned)
+        return 0;
+    ctx->tuned       = true;
+    const bool mixed = ctx->desc.precision == FANSGPU_MIXED;
+    auto apply = [&](const TuneChoice &c) {
+        ctx->cp64.var_z = c.v64[0];
+        ctx->cp64.var_y = c.v64[1];
+        ctx->cp64.var_x = c.v64[2];
+        ctx->cp32.var_z = c.v32[0];
+        ctx->cp32.var_y = c.v32[1];
+        ctx->cp32.var_x = c.v32[2];
+        if (c.tc_slower && ctx->use_tc) {
+            ctx->tc_slower = true;
+            ctx->use_tc    = false;
+        }
+        ctx->graphs_valid = false;
+    };
+    if (ctx->tune == 0)
+        return 0;
+    if (ctx->tune == 2) {
+        TuneChoice c{};
+        for (int k = 0; k < 3; ++k)
+            c.v64[k] = c.v32[k] = ctx->tune_force[k];
+        apply(c);
+        return 0;
+    }
+    const std::array<int, 6> key{ctx->g.nx, ctx->g.ny, ctx->g.nz, ctx->C, ctx->desc.precision,
+                                 (ctx->use_tc ? 1 : 0) + 2 * (ctx->tune == 3)};
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto                        it = g_tune_cache.find(key);
+    if (it == g_tune_cache.end()) {
+        TuneChoice c{};
+        FANS_CUDA_CHECK(tune_convolution_reg<double>(ctx->cp64, ctx->r, ctx->Kd, ctx->st));
+        c.v64[0] = ctx->cp64.var_z;
+        c.v64[1] = ctx->cp64.var_y;
+        c.v64[2] = ctx->cp64.var_x;
+        if (mixed) {
+            FANS_CUDA_CHECK(tune_convolution_reg<float>(ctx->cp32, ctx->r32, ctx->Kd32, ctx->st));
+            c.v32[0] = ctx->cp32.var_z;
+            c.v32[1] = ctx->cp32.var_y;
+            c.v32[2] = ctx->cp32.var_x;
+            if (ctx->use_tc && ctx->tune == 3)
+                c.tc_slower = time_mixed_operator(ctx, false) < time_mixed_operator(ctx, true) ? 1 : 0;
+        }
+        FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+        it = g_tune_cache.emplace(key, c).first;
+    }
+    apply(it->second);
+    return 0;
 }
 
 // After one graph-resident iteration (one thread): count it, record its
@@ -1311,6 +1418,17 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     ctx->desc        = *desc;
     if (const char *ev = std::getenv("FANSGPU_STENCIL"))
         ctx->tc_allowed = std::strcmp(ev, "simt") != 0;
+    if (const char *ev = std::getenv("FANSGPU_TUNE")) { // "0": default tiles; "all": + operator; "zyx": forced
+        if (std::strcmp(ev, "0") == 0)
+            ctx->tune = 0;
+        else if (std::strcmp(ev, "all") == 0)
+            ctx->tune = 3;
+        else if (std::strlen(ev) == 3 && std::strspn(ev, "01") == 3) {
+            ctx->tune = 2;
+            for (int k = 0; k < 3; ++k)
+                ctx->tune_force[k] = ev[k] - '0';
+        }
+    }
     if (const char *ev = std::getenv("FANSGPU_GRAPHS")) { // "0": no graphs; "iter": one graph per iteration
         ctx->use_graphs     = std::strcmp(ev, "0") != 0;
         ctx->loop_on_device = std::strcmp(ev, "iter") != 0;
@@ -1508,6 +1626,21 @@ int fansgpu_set_refresh(fansgpu_ctx *ctx, double factor)
     if (!(factor > 0.0 && factor < 1.0))
         return fail(ctx, FANSGPU_EINVAL, "refresh factor must lie in (0, 1)");
     ctx->reliable_delta = factor;
+    return 0;
+}
+
+int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out)
+{
+    if (!ctx || !out)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const ConvPlan<double> &a = ctx->cp64;
+    const ConvPlan<float>  &b = ctx->cp32;
+    const int32_t v[7] = {a.var_z, a.var_y, a.var_x, b.var_z, b.var_y, b.var_x, ctx->use_tc ? 1 : 0};
+    for (int k = 0; k < 7; ++k)
+        out[k] = v[k];
     return 0;
 }
 

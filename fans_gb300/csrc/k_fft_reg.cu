@@ -13,16 +13,23 @@ namespace fansgpu {
 
 namespace {
 
+// Tile shapes with two variants each, picked per grid by tune_convolution_reg
+// (variant 0 is the default): kz columns per CTA of the y and x passes (row
+// segments of 128 / 64 bytes for y, 64 / 32 bytes for x) and threads per CTA of
+// the z passes.
 template <typename T>
-struct KCol {
-    static constexpr int value = 128 / (int)sizeof(cplx<T>); // kz columns per CTA: one 128-byte row segment
+struct Tiles {
+    static constexpr int cs   = (int)sizeof(cplx<T>);
+    static constexpr int y[2] = {128 / cs, 64 / cs};
+    static constexpr int x[2] = {64 / cs, 32 / cs > 1 ? 32 / cs : 2};
+    static constexpr int z[2] = {sizeof(T) == 4 ? 256 : 128, sizeof(T) == 4 ? 128 : 64};
 };
 
 // ------------------------------------------------------------------ y pass ---
-template <typename T, int N1, int N2, bool INV>
-__global__ void __launch_bounds__(KCol<T>::value * N1) k_y_reg(ConvPlan<T> p)
+template <typename T, int N1, int N2, bool INV, int KC>
+__global__ void __launch_bounds__(KC * N1) k_y_reg(ConvPlan<T> p)
 {
-    constexpr int KC = KCol<T>::value, n = N1 * N2;
+    constexpr int n = N1 * N2;
     __shared__ cplx<T> S[n * KC];
     const int t = threadIdx.x, l = t % KC, w = t / KC;
     const int kz0 = blockIdx.x * KC, x = blockIdx.y, comp = blockIdx.z;
@@ -57,15 +64,15 @@ __global__ void __launch_bounds__(KCol<T>::value * N1) k_y_reg(ConvPlan<T> p)
 // cp.async at the start, so its reads overlap the forward transform; the
 // smaller tile lets two CTAs share an SM and overlap their load, compute and
 // store phases.
-template <typename T>
-struct KXCol {
-    static constexpr int value = 64 / (int)sizeof(cplx<T>);
+template <typename T, int KC>
+struct KXCtas { // resident CTAs per SM the register budget is set for
+    static constexpr int value = (sizeof(T) == 4 && KC * (int)sizeof(cplx<T>) <= 32) ? 4 : 2;
 };
 
-template <typename T, int N1, int N2, int C>
-__global__ void __launch_bounds__(C * KXCol<T>::value * N1, 2) k_x_green_reg(ConvPlan<T> p)
+template <typename T, int N1, int N2, int C, int KC>
+__global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_reg(ConvPlan<T> p)
 {
-    constexpr int KC = KXCol<T>::value, n = N1 * N2, NT = C * (C + 1) / 2;
+    constexpr int n = N1 * N2, NT = C * (C + 1) / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T>  *F  = reinterpret_cast<cplx<T> *>(smem_raw);        // [C][n][KC]
     T        *Gs = reinterpret_cast<T *>(F + (size_t)C * n * KC); // [n][KC][NT]
@@ -346,54 +353,45 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
 }
 
 // --------------------------------------------------------------- dispatch ---
-template <typename T, int N1, int N2, bool INV>
+template <typename T, int N1, int N2, bool INV, int KC>
 void go_y(const ConvPlan<T> &p, cudaStream_t st)
 {
-    constexpr int KC = KCol<T>::value;
-    dim3          g((p.nzh + KC - 1) / KC, p.g.nx, p.C);
-    k_y_reg<T, N1, N2, INV><<<g, KC * N1, 0, st>>>(p);
+    dim3 g((p.nzh + KC - 1) / KC, p.g.nx, p.C);
+    k_y_reg<T, N1, N2, INV, KC><<<g, KC * N1, 0, st>>>(p);
 }
 
-template <typename T, int N1, int N2>
+template <typename T, int N1, int N2, int KC>
 cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
 {
-    constexpr int KC = KXCol<T>::value;
-    dim3          g((p.nzh + KC - 1) / KC, p.g.ny);
-    const size_t  n = (size_t)N1 * N2;
+    dim3         g((p.nzh + KC - 1) / KC, p.g.ny);
+    const size_t n = (size_t)N1 * N2;
     if (p.C == 1) {
         const size_t sm = sizeof(cplx<T>) * n * KC + sizeof(T) * n * KC * 1;
-        cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 1>);
+        cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 1, KC>);
         if (e != cudaSuccess)
             return e;
-        k_x_green_reg<T, N1, N2, 1><<<g, KC * N1, sm, st>>>(p);
+        k_x_green_reg<T, N1, N2, 1, KC><<<g, KC * N1, sm, st>>>(p);
     } else {
         const size_t sm = sizeof(cplx<T>) * 3 * n * KC + sizeof(T) * n * KC * 6;
-        cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 3>);
+        cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 3, KC>);
         if (e != cudaSuccess)
             return e;
-        k_x_green_reg<T, N1, N2, 3><<<g, 3 * KC * N1, sm, st>>>(p);
+        k_x_green_reg<T, N1, N2, 3, KC><<<g, 3 * KC * N1, sm, st>>>(p);
     }
     return cudaSuccess;
 }
 
-// rows per CTA of the z passes: 256 (FP32) or 128 (FP64) threads
-template <typename T, int N1>
-struct ZRows {
-    static constexpr int value = (sizeof(T) == 4 ? 256 : 128) / N1;
-};
-
-template <typename T, int N1, int N2>
+template <typename T, int N1, int N2, int R>
 void go_zf(const ConvPlan<T> &p, const T *r, cudaStream_t st)
 {
-    constexpr int   R     = ZRows<T, N1>::value;
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
     k_z_fwd_reg<T, N1, N2, R><<<(int)((nrows + R - 1) / R), R * N1, 0, st>>>(p, r);
 }
 
-template <typename T, int N1, int N2>
+template <typename T, int N1, int N2, int R>
 cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
 {
-    constexpr int   R     = ZRows<T, N1>::value, M = N1 * N2;
+    constexpr int   M     = N1 * N2;
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
     const long long nblk  = (nrows + R - 1) / R;
     static int      nsm   = 0;
@@ -455,25 +453,105 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
             cudaEventRecord(a.ev[i], st);
     };
     cudaError_t e = cudaSuccess;
+    using TL      = Tiles<T>;
+    const T *r    = reinterpret_cast<const T *>(a.r);
     mark(0);
-    with_plan_z(p.M, [&]<int N1, int N2>() { go_zf<T, N1, N2>(p, reinterpret_cast<const T *>(a.r), st); });
+    with_plan_z(p.M, [&]<int N1, int N2>() {
+        p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
+    });
     mark(1);
-    with_plan(p.g.ny, [&]<int N1, int N2>() { go_y<T, N1, N2, false>(p, st); });
+    with_plan(p.g.ny, [&]<int N1, int N2>() {
+        p.var_y ? go_y<T, N1, N2, false, TL::y[1]>(p, st) : go_y<T, N1, N2, false, TL::y[0]>(p, st);
+    });
     mark(2);
-    with_plan(p.g.nx, [&]<int N1, int N2>() { e = go_x<T, N1, N2>(p, st); });
+    with_plan(p.g.nx, [&]<int N1, int N2>() {
+        e = p.var_x ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
+    });
     if (e != cudaSuccess)
         return e;
     mark(3);
-    with_plan(p.g.ny, [&]<int N1, int N2>() { go_y<T, N1, N2, true>(p, st); });
+    with_plan(p.g.ny, [&]<int N1, int N2>() {
+        p.var_y ? go_y<T, N1, N2, true, TL::y[1]>(p, st) : go_y<T, N1, N2, true, TL::y[0]>(p, st);
+    });
     mark(4);
-    with_plan_z(p.M, [&]<int N1, int N2>() { e = go_zi<T, N1, N2>(p, a, st); });
+    with_plan_z(p.M, [&]<int N1, int N2>() {
+        e = p.var_z ? go_zi<T, N1, N2, TL::z[1] / N1>(p, a, st) : go_zi<T, N1, N2, TL::z[0] / N1>(p, a, st);
+    });
     if (e != cudaSuccess)
         return e;
     mark(5);
     return cudaGetLastError();
 }
 
+// The autotuner of the register passes: for each of the z, y and x passes,
+// time its two tile variants on this plan's buffers (r in, s out, no fused
+// dot; one warm-up and three timed launches each, CUDA events on `st`) and
+// keep the faster in p.var_*.  The variants compute the same values per line,
+// so the choice changes the speed only (the fused dot of the z inverse pass
+// sums in another block order).
+template <typename T>
+cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, cudaStream_t st)
+{
+    if (!conv_reg_supported(p.g))
+        return cudaSuccess;
+    using TL = Tiles<T>;
+    ConvArgs    a{r, s, 1.0, 0, nullptr, GridRed{}, 0, nullptr};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e  = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    auto timed = [&](auto &&launch) -> float {
+        float ms = 1e30f;
+        if (e != cudaSuccess)
+            return ms;
+        launch();
+        if ((e = cudaEventRecord(e0, st)) != cudaSuccess)
+            return ms;
+        for (int k = 0; k < 3; ++k)
+            launch();
+        if ((e = cudaEventRecord(e1, st)) == cudaSuccess && (e = cudaEventSynchronize(e1)) == cudaSuccess &&
+            (e = cudaGetLastError()) == cudaSuccess)
+            cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
+    float t[2];
+    for (int v = 0; v < 2; ++v)
+        t[v] = timed([&] {
+            with_plan_z(p.M, [&]<int N1, int N2>() {
+                if (v) {
+                    go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st);
+                    e = go_zi<T, N1, N2, TL::z[1] / N1>(p, a, st);
+                } else {
+                    go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
+                    e = go_zi<T, N1, N2, TL::z[0] / N1>(p, a, st);
+                }
+            });
+        });
+    p.var_z = t[1] < t[0] ? 1 : 0;
+    for (int v = 0; v < 2; ++v)
+        t[v] = timed([&] {
+            with_plan(p.g.ny, [&]<int N1, int N2>() {
+                v ? go_y<T, N1, N2, false, TL::y[1]>(p, st) : go_y<T, N1, N2, false, TL::y[0]>(p, st);
+            });
+        });
+    p.var_y = t[1] < t[0] ? 1 : 0;
+    for (int v = 0; v < 2; ++v)
+        t[v] = timed([&] {
+            with_plan(p.g.nx, [&]<int N1, int N2>() {
+                e = v ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
+            });
+        });
+    p.var_x = t[1] < t[0] ? 1 : 0;
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    return e;
+}
+
 template cudaError_t launch_convolution_reg<double>(const ConvPlan<double> &, const ConvArgs &, cudaStream_t);
 template cudaError_t launch_convolution_reg<float>(const ConvPlan<float> &, const ConvArgs &, cudaStream_t);
+template cudaError_t tune_convolution_reg<double>(ConvPlan<double> &, const double *, double *, cudaStream_t);
+template cudaError_t tune_convolution_reg<float>(ConvPlan<float> &, const float *, float *, cudaStream_t);
 
 } // namespace fansgpu

@@ -186,6 +186,7 @@ struct ConvPlan {
     const T       *G;              // nx*ny*nzh*C(C+1)/2
     int            kc_y, kc_x;     // kz columns per CTA in the y / x passes
     int            use_reg;        // register-resident passes (conv_reg_supported)
+    int            var_z, var_y, var_x; // register passes: tile variant (0 default, 1 the alternative)
 };
 
 // s = sign * IFFT(G . FFT(r)); with reduce, <r, s> -> scal (delta0, delta,
@@ -208,6 +209,10 @@ size_t conv_smem_bytes(const ConvPlan<T> &p, int pass);
 bool conv_reg_supported(const Grid3 &g);
 template <typename T>
 cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st);
+// Times the register passes' tile variants on p's buffers (r in, s out) and
+// stores the faster ones in p.var_z / var_y / var_x.
+template <typename T>
+cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, cudaStream_t st);
 
 // Green's table (solver.h:145-204) in FP64, optionally also rounded to FP32.
 struct GreenArgs {

@@ -168,6 +168,13 @@ class Context:
         """Mixed precision: FP32-residual reduction that triggers an FP64 refresh."""
         self._chk(self.lib.fansgpu_set_refresh(self.ctx, float(factor)))
 
+    def tuning(self):
+        """fansgpu_tuning: {"fp64": (z, y, x), "fp32": (z, y, x), "tensor_core": bool}."""
+        out = np.zeros(7, dtype=np.int32)
+        self._chk(self.lib.fansgpu_tuning(self.ctx, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        return {"fp64": tuple(int(v) for v in out[:3]), "fp32": tuple(int(v) for v in out[3:6]),
+                "tensor_core": bool(out[6])}
+
     def set_timing(self, on=True):
         self._chk(self.lib.fansgpu_set_timing(self.ctx, int(bool(on))))
 

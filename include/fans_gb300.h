@@ -191,6 +191,13 @@ int fansgpu_enable_mixed_bc(fansgpu_ctx *ctx, int32_t n_e, const int32_t *idx_e,
 #define FANSGPU_VOXEL_YIELD_STRESS 1
 int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *values);
 
+/* The tile shapes the context's first setup chose (autotuned unless
+ * FANSGPU_TUNE=0 or forced): out[0..2] = FP64 z, y, x pass variants, out[3..5]
+ * the FP32 ones (0 = default tile, 1 = the smaller one), out[6] = 1 when the
+ * mixed path runs the tensor-core operator.  New on the GPU path (FANS's FFTW
+ * plans are chosen by FFTW_MEASURE, solver.h:221-222). */
+int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out);
+
 /* Adjoint of the homogenized stiffness w.r.t. the per-voxel scale.  After
  * solves with g0 = e_k, fansgpu_store_solution(ctx, k) keeps v_u and g0 (slots
  * 0..5).  fansgpu_stiffness_gradient returns grad[e] = d(sum_ij W_ij C_ij)/d s_e
