@@ -388,20 +388,31 @@ def main():
     for _ in range(args.warmup):
         homogenize(ctx, kref)
 
-    # timed region: K steps, CUDA events on the solver stream, per-kernel events on
+    # timed region: K steps as a user runs them (the device-resident CG loop in
+    # CUDA graphs), CUDA events on the solver stream
     stats: list = []
-    ctx.set_timing(True)
     clocks = ClockSampler()
     barrier()
     ms_total, Ceff = timed_steps(ctx, args.steps, lambda: homogenize(ctx, kref, stats))
     barrier()
-    clk = clocks.stop()
-    ktimes = ctx.kernel_times()
-    ctx.set_timing(False)
     ms_step = max_over_ranks(ms_total / args.steps, dist, "cuda")
     iters = [s["iterations"] for s in stats[:6]]
     refinements = [s["refinements"] for s in stats[:6]]
-    launches = sum(c for _, c in ktimes.values())
+    # kernel-timed region: the same K steps again with a CUDA event pair around
+    # every launch on the solver stream (graphs off) -> per-kernel breakdown and
+    # the roofline's average launch duration
+    ctx.set_timing(True)
+    barrier()
+    timed_steps(ctx, args.steps, lambda: homogenize(ctx, kref))
+    barrier()
+    clk = clocks.stop()
+    ktimes = ctx.kernel_times()
+    ctx.set_timing(False)
+    # launches in the timed region: the timed kernels, plus per solve one fold per
+    # refresh and at the end, and one loop-check kernel per graph-resident iteration
+    # (every iteration but the first)
+    launches = sum(c for _, c in ktimes.values()) + sum(
+        (s["refinements"] + 1) + max(s["iterations"] - 1, 0) for s in stats)
 
     # e2e through the C ABI from pinned host buffers
     pinned = torch.empty(n ** 3, dtype=torch.int16, pin_memory=True)
@@ -424,7 +435,7 @@ def main():
     h2d = 2 * n ** 3 + 2 * 2 * 8 + 36 * 8 + 6 * 6 * 8
     d2h = 6 * 6 * 8 + scal_bytes * (sum(iters) + sum(refinements) + 6) + 4
 
-    # roofline of the dominant kernel (by device time in the timed region)
+    # roofline of the dominant kernel (by device time in the kernel-timed region)
     hbm, peak_kind = peaks()
     dom = max((k for k in ktimes if ktimes[k][1] > 0 and algo_bytes(k, n) is not None),
               key=lambda k: ktimes[k][0])

@@ -56,3 +56,35 @@ def test_tuned_context_matches_oracle():
     P.solve(tol=1e-10, n_it=500)
     assert rel(ctx.homogenized_stress(), P.homogenized_stress()) < 1e-8
     ctx.close()
+
+
+def _mixed_run(monkeypatch, graphs, n_it=500):
+    monkeypatch.setenv("FANSGPU_GRAPHS", graphs)
+    P = _problem()
+    ctx = gpu_context(P, precision="mixed")
+    ctx.set_tolerance("L2", "relative", 1e-9, n_it)
+    out = []
+    for g in (np.array([1.0, 0, 0, 0, 0, 0]), np.array([0, 0.5, 0, 0.3, 0, 0])):
+        ctx.reset()
+        ctx.set_gradient(g)
+        st = ctx.solve()
+        out.append((st["iterations"], st["refinements"], st["converged"], ctx.error_history(),
+                    ctx.homogenized_stress()))
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("n_it", [500, 17])
+def test_graph_modes_take_the_same_decisions(monkeypatch, n_it):
+    """The device-resident loop (WHILE/IF graph nodes and the check kernel), one
+    graph per iteration and plain launches run the same kernels: iteration counts,
+    refreshes, the whole error history and the stresses agree bitwise, also when
+    n_it stops the solve before convergence."""
+    ref = _mixed_run(monkeypatch, "0", n_it)
+    for mode in ("iter", "1"):
+        got = _mixed_run(monkeypatch, mode, n_it)
+        for (i0, r0, c0, h0, s0), (i1, r1, c1, h1, s1) in zip(ref, got):
+            assert (i0, r0, c0) == (i1, r1, c1), mode
+            assert np.array_equal(h0, h1), mode
+            assert np.array_equal(s0, s1), mode
+    assert ref[0][2] == (n_it == 500)
