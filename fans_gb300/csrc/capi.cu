@@ -61,6 +61,7 @@ struct fansgpu_ctx {
     bool                u_zero = true; // v_u known to be zero (fresh context / reset): R(u) = F
     double *K64 = nullptr, *f64 = nullptr, *Cph = nullptr, *Bbar_d = nullptr, *g0_d = nullptr, *K0c = nullptr;
     double *Bgp_d = nullptr; // Gauss-point B matrices, ngp x n_str x 8C
+    double *Bb_d  = nullptr; // basic B (dN_q/dx_j) per Gauss point, ngp x 3 x 8: HEX8 / HEX8R mechanics
     float  *K32 = nullptr;
     double *G64 = nullptr;
     float  *G32 = nullptr;
@@ -590,6 +591,7 @@ ElementArgs element_args(fansgpu_ctx *ctx, const double *u, int mode)
     a.u     = u;
     a.ms    = ctx->d_ms;
     a.B     = ctx->Bgp_d;
+    a.Bb    = ctx->Bb_d;
     a.g0    = ctx->g0_d;
     a.law   = ctx->law_d;
     a.Cph   = ctx->Cph;
@@ -1495,6 +1497,15 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     cudaMemsetAsync(ctx->r, 0, sizeof(double) * nn, ctx->st);
     cudaMemcpyAsync(ctx->Bbar_d, ctx->Bbar.data(), sizeof(double) * ns * NC, cudaMemcpyHostToDevice, ctx->st);
     cudaMemcpyAsync(ctx->Bgp_d, ctx->B.data(), sizeof(double) * ctx->B.size(), cudaMemcpyHostToDevice, ctx->st);
+    if (ctx->C == 3 && (desc->fe_type == FANSGPU_HEX8 || desc->fe_type == FANSGPU_HEX8R)) {
+        // the element kernels' 72-term kinematics, small and large strain (BBAR's volumetric
+        // average fills the normal rows, so it keeps the dense B)
+        const std::vector<double> bb = fe::gauss_basic_B(desc->fe_type, ctx->le);
+        if ((rc = dalloc(ctx, &ctx->Bb_d, bb.size())))
+            return bail(rc);
+        cudaMemcpyAsync(ctx->Bb_d, bb.data(), sizeof(double) * bb.size(), cudaMemcpyHostToDevice, ctx->st);
+        cudaStreamSynchronize(ctx->st); // bb is a host temporary
+    }
     // trig tables for the Green's operator (solver.h:156-158)
     {
         std::vector<double> t;
@@ -1545,7 +1556,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
-                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d,
+                    ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d, ctx->Bb_d,
                     ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc, ctx->pb_t, ctx->pb,
                     ctx->vscale, ctx->zero_g0, ctx->stored_u, ctx->vyield, ctx->ctl, ctx->hist};
     for (void *p : ptrs)
@@ -1946,6 +1957,7 @@ AdjArgs adj_args(fansgpu_ctx *ctx, const double *u_n, const double *g0_n, const 
     a.q_in  = q_in;
     a.ms    = ctx->d_ms;
     a.B     = ctx->Bgp_d;
+    a.Bb    = ctx->Bb_d;
     a.law   = ctx->law_d;
     a.Cph   = ctx->Cph;
     a.prm   = ctx->prm_d;

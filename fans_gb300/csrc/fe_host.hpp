@@ -93,6 +93,27 @@ inline int gauss_B(int fe_type, int C, const double le[3], std::vector<double> &
     return 8;
 }
 
+// Basic B (dN_q/dx_j, matmodel.h:158-188) at the Gauss points of HEX8 (8, in
+// gauss_B's order) or HEX8R (1, the centre): ngp x 3 x 8.
+inline std::vector<double> gauss_basic_B(int fe_type, const double le[3])
+{
+    const double p = 0.5 + std::sqrt(3.) / 6., m = 0.5 - std::sqrt(3.) / 6.;
+    const double xi[8][3] = {{m, m, m}, {p, m, m}, {m, p, m}, {p, p, m}, {m, m, p}, {p, m, p}, {m, p, p}, {p, p, p}};
+    const int    ngp      = fe_type == 1 ? 1 : 8;
+    std::vector<double> out(ngp * 24);
+    for (int g = 0; g < ngp; ++g) {
+        double b[3][8];
+        if (fe_type == 1)
+            basic_B(0.5, 0.5, 0.5, le, b);
+        else
+            basic_B(xi[g][0], xi[g][1], xi[g][2], le, b);
+        for (int j = 0; j < 3; ++j)
+            for (int q = 0; q < 8; ++q)
+                out[g * 24 + j * 8 + q] = b[j][q];
+    }
+    return out;
+}
+
 // Constitutive matrix of a linear law (nstr x nstr, row-major).
 // law 0 thermal iso: kappa I (LinearThermal.h:186);
 // law 1 elastic iso: lambda on the normal 3x3 block + 2 mu I (LinearElastic.h:28-35);

@@ -22,6 +22,80 @@ __device__ __forceinline__ void elem_nodes(int nx, int ny, int nz, long long e, 
     idx[7] = ((long long)x1 * ny + y1) * nz + z1;
 }
 
+// Small-strain element kinematics from the basic B at a Gauss point,
+// b[j * 8 + q] = dN_q/dx_j (Compute_basic_B, matmodel.h:158-188).  The Mandel
+// B (matmodel.h:284-304) has 72 nonzeros of its 6 x 24: the displacement
+// gradient G_ij = sum_q b_j[q] u_i[q] (72 FMAs) gives
+//   eps = (G00, G11, G22, s(G01 + G10), s(G02 + G20), s(G12 + G21)) + off,
+// s = sqrt(1/2), and B^T sig = sum_j b_j[q] T_ij with T the stress tensor
+// (T01 = s sig3, T02 = s sig4, T12 = s sig5).  u_e is in the element's node
+// order, ue[3 q + c].
+__device__ __forceinline__ void strain_basic_b(const double *b, const double (&ue)[24], const double *off,
+                                               double (&e)[6])
+{
+    double G[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                acc += b[j * 8 + q] * ue[3 * q + i];
+            G[i][j] = acc;
+        }
+    const double s = 7.071067811865476e-01;
+    e[0]           = G[0][0];
+    e[1]           = G[1][1];
+    e[2]           = G[2][2];
+    e[3]           = s * (G[0][1] + G[1][0]);
+    e[4]           = s * (G[0][2] + G[2][0]);
+    e[5]           = s * (G[1][2] + G[2][1]);
+    if (off)
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            e[i] += off[i];
+}
+
+__device__ __forceinline__ void bt_sigma_basic_b(const double *b, const double (&sig)[6], double (&v)[24])
+{
+    const double s    = 7.071067811865476e-01;
+    const double T[3][3] = {{sig[0], s * sig[3], s * sig[4]}, {s * sig[3], sig[1], s * sig[5]},
+                            {s * sig[4], s * sig[5], sig[2]}};
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            v[3 * q + i] = b[q] * T[i][0] + b[8 + q] * T[i][1] + b[16 + q] * T[i][2];
+}
+
+// Large strain: the deformation-gradient B_F (LargeStrainMechModel.h:209-225,
+// row 3i + J, column 3q + i = dN_q/dX_J) has 72 nonzeros of its 9 x 24:
+// F_iJ = sum_q b_J[q] u_i[q] + off_iJ and (B_F^T P)_{3q+i} = sum_J b_J[q] P_iJ.
+__device__ __forceinline__ void defgrad_basic_b(const double *b, const double (&ue)[24], const double *off,
+                                                double (&F)[9])
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int J = 0; J < 3; ++J) {
+            double acc = 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                acc += b[J * 8 + q] * ue[3 * q + i];
+            F[3 * i + J] = acc + off[3 * i + J];
+        }
+}
+
+__device__ __forceinline__ void bt_piola_basic_b(const double *b, const double (&P)[9], double (&v)[24])
+{
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            v[3 * q + i] = b[q] * P[3 * i] + b[8 + q] * P[3 * i + 1] + b[16 + q] * P[3 * i + 2];
+}
+
 // J2PlasticityNew::get_sigma (J2PlasticityNew.h:43-108), one Gauss point, Mandel
 // vectors.  prm = {K, G, sigma_y, h}; sy0 is the initial yield stress in use
 // (prm[2], or the voxel's own value when a per-voxel field is set).

@@ -31,9 +31,12 @@ constexpr int kAdjThreads = 128;
 constexpr int kAdjPrm     = 8; // law parameters per phase
 
 // eps = B_gp x_e + off, x_e relative to the element's node 0 (as the residual
-// forms it, solver.h:252), SoA x [3][N].
-__device__ __forceinline__ void gp_strain(const double *Bg, const double *__restrict__ x, const long long (&idx)[8],
-                                          long long N, bool valid, const double *off, double (&e)[6])
+// forms it, solver.h:252), SoA x [3][N]; with the basic B (Bb) by the same
+// 72-term kinematics as the element kernel, so that replayed states match the
+// forward ones bit for bit.
+__device__ __forceinline__ void gp_strain(const double *Bg, const double *Bb, const double *__restrict__ x,
+                                          const long long (&idx)[8], long long N, bool valid, const double *off,
+                                          double (&e)[6])
 {
     double ue[24];
     if (valid) {
@@ -48,6 +51,10 @@ __device__ __forceinline__ void gp_strain(const double *Bg, const double *__rest
 #pragma unroll
         for (int k = 0; k < 24; ++k)
             ue[k] = 0.0;
+    }
+    if (Bb) {
+        strain_basic_b(Bb, ue, off, e);
+        return;
     }
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
@@ -64,14 +71,19 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs a)
 {
     static_assert(32 % NGP == 0 && 24 % NGP == 0, "group layout");
     __shared__ double Bs[NGP * 6 * 24];
+    __shared__ double Bbs[NGP * 24];
     for (int i = threadIdx.x; i < NGP * 6 * 24; i += blockDim.x)
         Bs[i] = a.B[i];
+    if (a.Bb)
+        for (int i = threadIdx.x; i < NGP * 24; i += blockDim.x)
+            Bbs[i] = a.Bb[i];
     __syncthreads();
     const int       nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
     const long long N  = (long long)nx * ny * nz;
     const long long T  = (N * NGP + 31) / 32 * 32;
     const int       gp = (int)(threadIdx.x % NGP);
     const double   *Bg = Bs + gp * 6 * 24;
+    const double   *Bb = a.Bb ? Bbs + gp * 24 : nullptr;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T; t += (long long)gridDim.x * blockDim.x) {
         const long long el    = t / NGP;
         const bool      valid = el < N;
@@ -86,7 +98,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs a)
                 idx[q] = 0;
         const long long base = (long long)gp * N + el;
         double          e[6], ep_in[6], q_in = 0.0;
-        gp_strain(Bg, a.u, idx, N, valid, a.g0, e);
+        gp_strain(Bg, Bb, a.u, idx, N, valid, a.g0, e);
 #pragma unroll
         for (int i = 0; i < 6; ++i)
             ep_in[i] = valid ? a.ep_in[(long long)i * NGP * N + base] : 0.0;
@@ -111,7 +123,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs a)
             }
         } else {
             double tau[6];
-            gp_strain(Bg, a.x, idx, N, valid, nullptr, tau);
+            gp_strain(Bg, Bb, a.x, idx, N, valid, nullptr, tau);
             const double w    = a.ve / NGP;
             const bool   seed = MODE != ADJ_OPERATOR && a.cw; // the operator is the linear part alone
 #pragma unroll
@@ -154,14 +166,17 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(AdjArgs a)
                     a.grad[el] += g;
             } else {
                 double v[24];
+                if (Bb)
+                    bt_sigma_basic_b(Bb, ge, v);
+                else
 #pragma unroll
-                for (int k = 0; k < 24; ++k) {
-                    double acc = 0.0;
+                    for (int k = 0; k < 24; ++k) {
+                        double acc = 0.0;
 #pragma unroll
-                    for (int i = 0; i < 6; ++i)
-                        acc += Bg[i * 24 + k] * ge[i];
-                    v[k] = acc;
-                }
+                        for (int i = 0; i < 6; ++i)
+                            acc += Bg[i * 24 + k] * ge[i];
+                        v[k] = acc;
+                    }
                 // reduce-scatter over the NGP lanes of the element
                 int kb = 0;
 #pragma unroll

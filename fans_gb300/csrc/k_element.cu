@@ -194,14 +194,21 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
     constexpr int NSTR = LARGE ? 9 : (C == 1 ? 3 : 6), NCOL = 8 * C, NE = NSTR > 6 ? NSTR : 6;
     static_assert(32 % NGP == 0 && NCOL % NGP == 0, "group layout");
     __shared__ double Bs[NGP * NSTR * NCOL];
+    __shared__ double Bbs[NGP * 24];
     for (int i = threadIdx.x; i < NGP * NSTR * NCOL; i += blockDim.x)
         Bs[i] = a.B[i];
+    constexpr bool STRUCT = C == 3; // mechanics: the 72-term kinematics when a.Bb is set
+    const bool     bb     = STRUCT && a.Bb;
+    if (bb)
+        for (int i = threadIdx.x; i < NGP * 24; i += blockDim.x)
+            Bbs[i] = a.Bb[i];
     __syncthreads();
     const int       nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
     const long long N  = (long long)nx * ny * nz;
     const long long T  = (N * NGP + 31) / 32 * 32;
     const int       gp = (int)(threadIdx.x % NGP);
     const double   *Bg = Bs + gp * NSTR * NCOL;
+    const double   *Bb = Bbs + gp * 24;
     double          se[MODE == ELEM_AVERAGES ? NSTR : 1], ss[MODE == ELEM_AVERAGES ? NSTR : 1], cnt = 0.0;
     if constexpr (MODE == ELEM_AVERAGES) {
 #pragma unroll
@@ -230,13 +237,31 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
                 for (int k = 0; k < NCOL; ++k)
                     ue[k] = 0.0;
             }
+            if constexpr (STRUCT) {
+                if (bb) {
+                    if constexpr (LARGE)
+                        defgrad_basic_b(Bb, ue, a.g0, e);
+                    else
+                        strain_basic_b(Bb, ue, a.g0, e);
+                } else {
 #pragma unroll
-            for (int i = 0; i < NSTR; ++i) {
-                double acc = 0.0;
+                    for (int i = 0; i < NSTR; ++i) {
+                        double acc = 0.0;
 #pragma unroll
-                for (int k = 0; k < NCOL; ++k)
-                    acc += Bg[i * NCOL + k] * ue[k];
-                e[i] = acc + a.g0[i];
+                        for (int k = 0; k < NCOL; ++k)
+                            acc += Bg[i * NCOL + k] * ue[k];
+                        e[i] = acc + a.g0[i];
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < NSTR; ++i) {
+                    double acc = 0.0;
+#pragma unroll
+                    for (int k = 0; k < NCOL; ++k)
+                        acc += Bg[i * NCOL + k] * ue[k];
+                    e[i] = acc + a.g0[i];
+                }
             }
         }
         const int law = valid ? a.law[ph] : -1;
@@ -296,14 +321,25 @@ __global__ void __launch_bounds__(kElThreads) k_element(ElementArgs a)
         }
         if constexpr (MODE == ELEM_RESIDUAL) {
             double v[NCOL];
-#pragma unroll
-            for (int k = 0; k < NCOL; ++k) {
-                double acc = 0.0;
-#pragma unroll
-                for (int i = 0; i < NSTR; ++i)
-                    acc += Bg[i * NCOL + k] * sig[i];
-                v[k] = acc;
+            bool   done = false;
+            if constexpr (STRUCT) {
+                if (bb) {
+                    if constexpr (LARGE)
+                        bt_piola_basic_b(Bb, sig, v);
+                    else
+                        bt_sigma_basic_b(Bb, sig, v);
+                    done = true;
+                }
             }
+            if (!done)
+#pragma unroll
+                for (int k = 0; k < NCOL; ++k) {
+                    double acc = 0.0;
+#pragma unroll
+                    for (int i = 0; i < NSTR; ++i)
+                        acc += Bg[i * NCOL + k] * sig[i];
+                    v[k] = acc;
+                }
             // reduce-scatter over the NGP lanes of the element
             int kb = 0;
 #pragma unroll

@@ -92,6 +92,7 @@ struct ElementArgs {
     const double  *u;     // SoA FP64
     const uint8_t *ms;
     const double  *B;     // ngp x nstr x 8C
+    const double  *Bb;    // ngp x 3 x 8 basic B (dN_q/dx_j), HEX8 / HEX8R mechanics; else null
     const double  *g0;    // nstr
     const int     *law;   // per phase
     const double  *Cph;   // per phase nstr x nstr (linear laws)
@@ -147,6 +148,7 @@ struct AdjArgs {
     const double  *cw;           // 6 doubles: w/(N n_gp), the seed of <sigma_N> (last step), or null
     const uint8_t *ms;
     const double  *B;            // ngp x 6 x 24
+    const double  *Bb;           // ngp x 3 x 8 basic B, or null (then the dense B)
     const int     *law;
     const double  *Cph;          // per phase 6 x 6 (linear elastic laws)
     const double  *prm;          // per phase, 8 law parameters
