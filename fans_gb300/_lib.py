@@ -21,7 +21,7 @@ LAW_SVK, LAW_NEOHOOKEAN = 9, 10
 SMALL_STRAIN, LARGE_STRAIN = 0, 1
 STRAIN_TYPES = {"small": SMALL_STRAIN, "large": LARGE_STRAIN}
 FP64, MIXED = 0, 1
-CG, FP = 0, 1
+CG, FP, NEWTON = 0, 1, 2
 L1, L2, LINF = 0, 1, 2
 ABSOLUTE, RELATIVE = 0, 1
 FIELD_U, FIELD_R, FIELD_STRAIN, FIELD_STRESS, FIELD_U_PREV = 0, 1, 2, 3, 4

@@ -103,6 +103,7 @@ struct fansgpu_ctx {
     // per-voxel stiffness scale and stored solutions for the stiffness sensitivity
     double             *vscale = nullptr, *zero_g0 = nullptr, *stored_u = nullptr;
     double             *vyield = nullptr; // per-voxel initial yield stress of J2PlasticityNew elements
+    double             *nwt    = nullptr; // Newton-Krylov scratch: tangent-CG residual and step, 2 n
     std::vector<double> stored_g0;
     std::vector<char>   stored_ok;
 
@@ -1404,8 +1405,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         return fail(nullptr, FANSGPU_EINVAL, "FE_type must be one of: 'HEX8', 'HEX8R', or 'BBAR'");
     if (desc->precision != FANSGPU_FP64 && desc->precision != FANSGPU_MIXED)
         return fail(nullptr, FANSGPU_EINVAL, "precision must be FANSGPU_FP64 or FANSGPU_MIXED");
-    if (desc->method != FANSGPU_CG && desc->method != FANSGPU_FP)
-        return fail(nullptr, FANSGPU_EINVAL, "method must be cg or fp");
+    if (desc->method != FANSGPU_CG && desc->method != FANSGPU_FP && desc->method != FANSGPU_NEWTON)
+        return fail(nullptr, FANSGPU_EINVAL, "method must be cg, fp or newton");
     if (desc->precision == FANSGPU_MIXED && desc->method != FANSGPU_CG)
         return fail(nullptr, FANSGPU_EUNSUPPORTED, "mixed precision is implemented for the CG method");
     if (desc->strain_type != FANSGPU_SMALL_STRAIN && desc->strain_type != FANSGPU_LARGE_STRAIN)
@@ -1558,7 +1559,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d, ctx->Bb_d,
                     ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc, ctx->pb_t, ctx->pb,
-                    ctx->vscale, ctx->zero_g0, ctx->stored_u, ctx->vyield, ctx->ctl, ctx->hist};
+                    ctx->vscale, ctx->zero_g0, ctx->stored_u, ctx->vyield, ctx->ctl, ctx->hist, ctx->nwt};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -1967,35 +1968,40 @@ AdjArgs adj_args(fansgpu_ctx *ctx, const double *u_n, const double *g0_n, const 
     return a;
 }
 
-// Linear CG (the flexible CG recurrences of solverCG.h:62-117 with the Green's
-// operator as preconditioner) for K_n^T lambda + f_n = 0 from lambda = 0, to a
-// relative L2 residual of rel_tol.  `a` carries the step's state, mu_n and the
-// seed; the context's CG vectors are its scratch.
-int adjoint_solve(fansgpu_ctx *ctx, AdjArgs a, double *lam, double rel_tol, int *iters)
+// Linear CG on the consistent tangent (the flexible CG recurrences of
+// solverCG.h:62-117 with the Green's operator as preconditioner): x from zero
+// until the residual res = K x + f has fallen by rel_tol (L2).  With res_given
+// the caller has put f in `res`; otherwise f is the adjoint load of `a`
+// (ADJ_RESIDUAL at x = 0: K_n^T lambda + f_n for the yield-stress adjoint).  `a`
+// carries the state the tangent is taken at; the context's s, d and Kd vectors
+// are the scratch.  Stopped by n_it, it returns ENOTCONV with x as far as it got.
+int tangent_cg(fansgpu_ctx *ctx, AdjArgs a, double *x, double *res, bool res_given, double rel_tol, int *iters)
 {
     const long long n = ctx->n;
     int             rc;
     *iters = 0;
-    FANS_CUDA_CHECK(cudaMemsetAsync(lam, 0, sizeof(double) * n, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->st));
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s, 0, sizeof(double) * n, ctx->st));
     FANS_CUDA_CHECK(cudaMemsetAsync(ctx->dd[0], 0, sizeof(double) * n, ctx->st));
     ctx->cur_d = 0;
     if ((rc = init_scalars(ctx)))
         return rc;
-    a.mode = ADJ_RESIDUAL;
-    a.x    = lam;
-    FANS_CUDA_CHECK(launch_adjoint(a, ctx->st));
-    FANS_CUDA_CHECK(launch_gather(ctx->rows, ctx->r, ctx->g, ctx->C, ctx->st));
-    FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, FANSGPU_L2, ctx->scal, 1, nullptr, ctx->red, SITE_NORM,
+    if (!res_given) {
+        a.mode = ADJ_RESIDUAL;
+        a.x    = x;
+        FANS_CUDA_CHECK(launch_adjoint(a, ctx->st));
+        FANS_CUDA_CHECK(launch_gather(ctx->rows, res, ctx->g, ctx->C, ctx->st));
+    }
+    FANS_CUDA_CHECK(launch_norm<double, float>(res, n, FANSGPU_L2, ctx->scal, 1, nullptr, ctx->red, SITE_NORM,
                                                ctx->st));
     if ((rc = sync_scalars(ctx)))
         return rc;
     const double err0 = ctx->scal_h->err;
     if (!std::isfinite(err0))
-        return fail(ctx, FANSGPU_ENAN, "yield-stress adjoint: non-finite adjoint load");
+        return fail(ctx, FANSGPU_ENAN, "tangent CG: non-finite load");
     double err = err0;
     while (err > rel_tol * err0 && *iters < ctx->tol.n_it) {
-        ConvArgs ca{ctx->r, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+        ConvArgs ca{res, ctx->s, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
         FANS_CUDA_CHECK(run_conv<double>(ctx, ctx->cp64, ca));
         double *dn = ctx->dd[ctx->cur_d ^ 1];
         FANS_CUDA_CHECK(cudaMemcpyAsync(dn, ctx->dd[ctx->cur_d], sizeof(double) * n, cudaMemcpyDeviceToDevice,
@@ -2008,18 +2014,18 @@ int adjoint_solve(fansgpu_ctx *ctx, AdjArgs a, double *lam, double rel_tol, int 
         FANS_CUDA_CHECK(launch_dot(dn, ctx->Kd, n, &ctx->scal->dAd, ctx->red, SITE_DOT, ctx->st));
         FANS_CUDA_CHECK(launch_set_alpha(ctx->scal, ctx->st));
         ctx->cur_d ^= 1;
-        UpdateArgs ua{n, ctx->r, ctx->Kd, lam, dn, ctx->s, FANSGPU_L2, 1, ctx->scal, ctx->red, SITE_UPDATE};
+        UpdateArgs ua{n, res, ctx->Kd, x, dn, ctx->s, FANSGPU_L2, 1, ctx->scal, ctx->red, SITE_UPDATE};
         FANS_CUDA_CHECK((launch_cg_update<double, double>(ua, ctx->st)));
         if ((rc = sync_scalars(ctx)))
             return rc;
         ++*iters;
         err = ctx->scal_h->err;
         if (ctx->scal_h->converged < 0 || !std::isfinite(err))
-            return fail(ctx, FANSGPU_ENAN, "yield-stress adjoint: non-finite residual at iteration %d", *iters);
+            return fail(ctx, FANSGPU_ENAN, "tangent CG: non-finite residual at iteration %d", *iters);
     }
     if (err > rel_tol * err0)
-        return fail(ctx, FANSGPU_ENOTCONV, "yield-stress adjoint: CG reached %d iterations at relative residual %g",
-                    *iters, err / err0);
+        return fail(ctx, FANSGPU_ENOTCONV, "tangent CG: %d iterations reached at relative residual %g", *iters,
+                    err / err0);
     return 0;
 }
 
@@ -2050,9 +2056,9 @@ int fansgpu_yield_stress_adjoint(fansgpu_ctx *ctx, int32_t n_steps, const double
         return rc;
     if (ctx->C != 3 || ctx->nstr != 6)
         return fail(ctx, FANSGPU_EUNSUPPORTED, "yield-stress adjoint: small-strain mechanics only");
-    if (ctx->mixed_active || ctx->vscale || ctx->desc.method != FANSGPU_CG)
+    if (ctx->mixed_active || ctx->vscale || ctx->desc.method == FANSGPU_FP)
         return fail(ctx, FANSGPU_EUNSUPPORTED,
-                    "yield-stress adjoint: strain control with the CG solver and no stiffness scale field only");
+                    "yield-stress adjoint: strain control with the CG or Newton solver, no stiffness scale field");
     bool any_j2 = false;
     for (int ph = 0; ph < ctx->nph; ++ph) {
         const int law = ctx->law[ph];
@@ -2139,8 +2145,10 @@ int fansgpu_yield_stress_adjoint(fansgpu_ctx *ctx, int32_t n_steps, const double
             a.mu_q            = b.mu + nep;
             a.cw              = m == n_steps ? b.cw : nullptr;
             int its           = 0;
-            if ((rc = adjoint_solve(ctx, a, b.lam, rel_tol, &its)))
-                return rc;
+            if ((rc = tangent_cg(ctx, a, b.lam, ctx->r, false, rel_tol, &its))) {
+                const std::string why = ctx->err_msg;
+                return fail(ctx, rc, "yield-stress adjoint, step %d: %s", m, why.c_str());
+            }
             if (iterations)
                 iterations[n_steps + m - 1] = its;
             a.mode = ADJ_STEP;
@@ -2152,6 +2160,93 @@ int fansgpu_yield_stress_adjoint(fansgpu_ctx *ctx, int32_t n_steps, const double
     FANS_CUDA_CHECK(cudaMemcpyAsync(grad, b.grad, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->st));
     FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->r, b.rsave, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+// Newton-Krylov (method FANSGPU_NEWTON, a GPU extension: FANS solves the same
+// discrete equations R(u) = 0 by nonlinear CG with LineSearchSecant,
+// solverCG.h:62-160).  Each outer step solves the consistent-tangent system
+// K(u) du = -R(u), K taken at the current strains and the committed internal
+// variables, by the Green's-preconditioned CG to a relative tolerance eta
+// (Eisenstat-Walker, choice 2: eta = 0.9 (|R_k| / |R_k-1|)^2 within
+// [1e-6, 0.1]), then sets u += lambda du with lambda halved (at most five times)
+// while the residual norm does not fall.  Linear elastic phases use their
+// stiffness; J2PlasticityNew the vector-Jacobian product of its return map
+// (j2_vjp with zero seeds on the internal variables).  The outer steps are the
+// solve's iterations and error history; the inner CG iterations go to *inner.
+int solve_newton(fansgpu_ctx *ctx, int *inner)
+{
+    const long long n = ctx->n;
+    int             rc;
+    *inner = 0;
+    if (ctx->C != 3 || ctx->nstr != 6 || ctx->mixed_active || ctx->vscale)
+        return fail(ctx, FANSGPU_EUNSUPPORTED,
+                    "Newton-Krylov: small-strain mechanics, strain control, no stiffness scale field");
+    for (int ph = 0; ph < ctx->nph; ++ph) {
+        const int law = ctx->law[ph];
+        if (law != FANSGPU_LAW_J2_LINEAR && law != FANSGPU_LAW_ELASTIC_ISO && law != FANSGPU_LAW_ELASTIC_TRI)
+            return fail(ctx, FANSGPU_EUNSUPPORTED,
+                        "Newton-Krylov: phase %d: only J2PlasticityNew and linear elastic laws have a tangent", ph);
+    }
+    if (!ctx->nwt && (rc = dalloc(ctx, &ctx->nwt, 2 * (size_t)n)))
+        return rc;
+    if ((rc = ensure_rows(ctx)))
+        return rc;
+    double *res = ctx->nwt, *du = ctx->nwt + n;
+    auto residual_norm = [&](int first, double *out) -> int {
+        int rr;
+        if ((rr = run_residual64(ctx, ctx->u, ctx->r)))
+            return rr;
+        int en = tk_mark(ctx);
+        FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, first, nullptr, ctx->red,
+                                                   SITE_NORM, ctx->st));
+        tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx));
+        if ((rr = sync_scalars(ctx)))
+            return rr;
+        *out = ctx->scal_h->err;
+        return 0;
+    };
+    if ((rc = init_scalars(ctx)))
+        return rc;
+    double err = 0.0;
+    if ((rc = residual_norm(1, &err)))
+        return rc;
+    ctx->iter = 0;
+    ctx->err_all.assign(1, err);
+    if (!std::isfinite(err))
+        return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm");
+    double err_rel = err_value(ctx, err);
+    if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
+        ctx->u_zero = false;
+    double eta = 0.1;
+    while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
+        // the tangent at the current u and the committed state; its right-hand side is -R(u)
+        const AdjArgs a = adj_args(ctx, ctx->u, ctx->g0_d, ctx->ep_t, ctx->q_t);
+        FANS_CUDA_CHECK(cudaMemcpyAsync(res, ctx->r, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+        int its = 0;
+        rc      = tangent_cg(ctx, a, du, res, true, eta, &its);
+        *inner += its;
+        if (rc && rc != FANSGPU_ENOTCONV) // an inner solve stopped by n_it still gives a usable step
+            return rc;
+        FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, du, 1.0, n, ctx->st));
+        double err_new = 0.0, lambda = 1.0;
+        if ((rc = residual_norm(0, &err_new)))
+            return rc;
+        for (int ls = 0; ls < 5 && !(err_new < err); ++ls) { // backtracking, NaN included
+            lambda *= 0.5;
+            FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, du, -lambda, n, ctx->st));
+            if ((rc = residual_norm(0, &err_new)))
+                return rc;
+        }
+        ctx->iter++;
+        ctx->err_all.push_back(err_new);
+        if (!std::isfinite(err_new))
+            return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at Newton step %d", ctx->iter);
+        const double ratio = err_new / err;
+        eta = std::min(0.1, std::max(1e-6, 0.9 * ratio * ratio));
+        err     = err_new;
+        err_rel = err_value(ctx, err);
+    }
     return 0;
 }
 
@@ -2191,6 +2286,8 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
     int refinements = 0;
     if (ctx->desc.method == FANSGPU_FP)
         rc = solve_fp64(ctx);
+    else if (ctx->desc.method == FANSGPU_NEWTON)
+        rc = solve_newton(ctx, &refinements);
     else if (!ctx->all_linear || ctx->mixed_active)
         rc = solve_cg_nl(ctx); // nonlinear laws and mixed BCs run the FP64 line-search path (solverCG.h:96)
     else if (ctx->desc.precision == FANSGPU_MIXED && !ctx->vscale)

@@ -33,7 +33,7 @@ class Context:
         d.howmany = int(howmany)
         d.fe_type = C.FE_TYPES[fe_type] if isinstance(fe_type, str) else int(fe_type)
         d.precision = {"fp64": C.FP64, "mixed": C.MIXED}[precision] if isinstance(precision, str) else int(precision)
-        d.method = {"cg": C.CG, "fp": C.FP}[method] if isinstance(method, str) else int(method)
+        d.method = {"cg": C.CG, "fp": C.FP, "newton": C.NEWTON}[method] if isinstance(method, str) else int(method)
         d.strain_type = C.STRAIN_TYPES[strain_type] if isinstance(strain_type, str) else int(strain_type)
         ptr = ctypes.c_void_p()
         rc = self.lib.fansgpu_create(ctypes.byref(d), ctypes.byref(ptr))

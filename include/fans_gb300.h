@@ -76,6 +76,12 @@ extern "C" {
 /* method (setup.h:76-85) */
 #define FANSGPU_CG 0
 #define FANSGPU_FP 1
+/* Newton-Krylov (new on the GPU path; FP64, strain control, J2PlasticityNew and
+ * linear elastic phases): outer Newton steps on R(u) = 0, each an inexact
+ * consistent-tangent solve by the Green's-preconditioned CG (Eisenstat-Walker
+ * tolerance) with backtracking.  fansgpu_stats.iterations counts Newton steps,
+ * fansgpu_stats.refinements the inner CG iterations. */
+#define FANSGPU_NEWTON 2
 
 /* error_parameters (solver.h:415-452) */
 #define FANSGPU_L1 0
@@ -110,7 +116,7 @@ typedef struct {
     int32_t howmany;     /* 1: thermal <1,3>; 3: mechanics (main.cpp:67-75) */
     int32_t fe_type;     /* FANSGPU_HEX8 / HEX8R / BBAR */
     int32_t precision;   /* FANSGPU_FP64 / FANSGPU_MIXED */
-    int32_t method;      /* FANSGPU_CG / FANSGPU_FP */
+    int32_t method;      /* FANSGPU_CG / FANSGPU_FP / FANSGPU_NEWTON */
     int32_t strain_type; /* FANSGPU_SMALL_STRAIN <3,6> (0, default) or FANSGPU_LARGE_STRAIN <3,9> */
 } fansgpu_desc;
 
