@@ -4,6 +4,7 @@ GPU (fansgpu_yield_stress_adjoint through the C ABI).
 1. The per-voxel yield-stress field equals the oracle with one J2 phase per
    voxel, and the GPU gradient equals the oracle's dense discrete adjoint
    (complex-step Gauss-point Jacobians, lstsq tangent solves) on the same path.
+   The forward path may run nonlinear CG or Newton-Krylov.
 2. The checkpoint interval changes nothing: every interval recomputes the same
    committed states from its checkpoints.
 3. At 16^3 the gradient equals central finite differences of the GPU forward
@@ -27,10 +28,10 @@ J2P = (68.6275, 26.3158, 0.25, 2.0)
 ELP = (222.222, 166.667)
 
 
-def yield_context(ms, sy, kapparef, tol=("Linfinity", "absolute", 1e-14, 20000)):
+def yield_context(ms, sy, kapparef, tol=("Linfinity", "absolute", 1e-14, 20000), method="cg"):
     from fans_gb300 import Context
 
-    ctx = Context(ms.shape, (1.0, 1.0, 1.0), 3, "HEX8", "fp64", "cg")
+    ctx = Context(ms.shape, (1.0, 1.0, 1.0), 3, "HEX8", "fp64", method)
     ctx.set_microstructure(np.asarray(ms, dtype=np.uint16))
     ctx.set_phase_material(0, O.LAW_J2, list(J2P))
     ctx.set_phase_material(1, O.LAW_ELASTIC_ISO, list(ELP))
@@ -53,7 +54,10 @@ def forward(ctx, path):
 KREF = 0.5 * (O.iso_elastic_C(*J2P[:2]) + O.iso_elastic_C(*ELP))
 
 
-def test_voxel_yield_field_and_adjoint_match_oracle():
+@pytest.mark.parametrize("method", ["cg", "newton"])
+def test_voxel_yield_field_and_adjoint_match_oracle(method):
+    """The forward path by nonlinear CG or by Newton-Krylov: the same converged
+    states, so the same gradient."""
     ms = random_ms((4, 4, 4), vf=0.3, seed=7)
     rng = np.random.default_rng(2)
     sy = 0.25 * (1.0 + 0.3 * rng.random(ms.shape))
@@ -61,7 +65,7 @@ def test_voxel_yield_field_and_adjoint_match_oracle():
     w = np.array([1.0, 0.3, -0.2, 0.5, 0.1, 0.0])
     Y = A.YieldPathProblem(ms, J2P, ELP, sy)
     st_o, g_o = Y.adjoint(path, w)
-    ctx = yield_context(ms, sy, Y.kapparef, ("L2", "absolute", 1e-12, 5000))
+    ctx = yield_context(ms, sy, Y.kapparef, ("L2", "absolute", 1e-12, 5000), method)
     out = ctx.yield_stress_adjoint(path, w, checkpoint_every=2, rel_tol=1e-12)
     assert rel(out["stress"], st_o) < 1e-9
     assert np.all(out["grad"][ms != 0] == 0.0)
