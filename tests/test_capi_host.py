@@ -34,6 +34,19 @@ def test_library_exports_every_header_symbol():
     assert b"sm_103a" in L.fansgpu_version()
 
 
+def test_header_constants_match_the_binding():
+    """Every #define FANSGPU_<NAME> value the ctypes binding also names (as <NAME>)
+    is the same number on both sides."""
+    from fans_gb300 import _lib
+
+    src = open(os.path.join(ROOT, "include", "fans_gb300.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define FANSGPU_([A-Z0-9_]+)\s+(-?\d+)", src)}
+    shared = [k for k in defs if hasattr(_lib, k)]
+    assert {"NEWTON", "VOXEL_YIELD_STRESS", "LAW_J2_LINEAR", "FIELD_U", "MIXED", "LARGE_STRAIN"} <= set(shared)
+    for k in shared:
+        assert getattr(_lib, k) == defs[k], k
+
+
 def test_create_without_device_fails_cleanly():
     from conftest import have_gpu
 
@@ -50,7 +63,8 @@ def test_create_argument_validation():
     from fans_gb300 import Context, FansGpuError
 
     for kw, code in [(dict(n=(7, 8, 8)), -6), (dict(n=(8, 8, 8), howmany=2), -1), (dict(n=(8, 8, 8), fe_type=5), -1),
-                     (dict(n=(8, 8, 8), precision="mixed", method="fp"), -6)]:
+                     (dict(n=(8, 8, 8), precision="mixed", method="fp"), -6),
+                     (dict(n=(8, 8, 8), precision="mixed", method="newton"), -6), (dict(n=(8, 8, 8), method=3), -1)]:
         n = kw.pop("n")
         with pytest.raises(FansGpuError) as ei:
             Context(n, (1, 1, 1), **({"howmany": 3} | kw))
