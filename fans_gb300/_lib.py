@@ -46,7 +46,7 @@ EXPORTS = [
     "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc", "fansgpu_set_refresh",
     "fansgpu_enable_mixed_bc", "fansgpu_disable_mixed_bc", "fansgpu_get_gradient", "fansgpu_set_voxel_field",
     "fansgpu_store_solution", "fansgpu_stiffness_gradient", "fansgpu_solve_batch", "fansgpu_yield_stress_adjoint",
-    "fansgpu_tuning",
+    "fansgpu_tuning", "fansgpu_set_wait_limit",
 ]
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
                 "residual64", "norm", "green_table", "strain_stress"]
@@ -135,6 +135,7 @@ def _declare(L):
     L.fansgpu_solve_batch.argtypes = [ctypes.POINTER(vp), ip, ctypes.POINTER(Stats), i32p]
     L.fansgpu_yield_stress_adjoint.argtypes = [vp, ip, dp, ip, dp, ctypes.c_double, dp, dp, i32p]
     L.fansgpu_tuning.argtypes = [vp, i32p]
+    L.fansgpu_set_wait_limit.argtypes = [vp, ip]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

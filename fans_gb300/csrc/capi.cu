@@ -22,7 +22,9 @@
 
 using namespace fansgpu;
 
-static std::string g_create_error;
+// Message of the last failing call made without a context, per calling thread
+// (fansgpu_last_error(NULL) reads the caller's own copy).
+static thread_local std::string g_create_error;
 
 // Controls of the device-resident inner loop of the mixed CG.
 struct LoopCtl {
@@ -99,11 +101,12 @@ struct fansgpu_ctx {
     int    *law_d = nullptr;
     double *prm_d = nullptr;
     double  alpha_warm = 0.1;
+    bool    newton_stalled = false; // the last Newton solve stopped without a decrease (u restored)
 
     // per-voxel stiffness scale and stored solutions for the stiffness sensitivity
     double             *vscale = nullptr, *zero_g0 = nullptr, *stored_u = nullptr;
     double             *vyield = nullptr; // per-voxel initial yield stress of J2PlasticityNew elements
-    double             *nwt    = nullptr; // Newton-Krylov scratch: tangent-CG residual and step, 2 n
+    double             *nwt    = nullptr; // Newton-Krylov scratch: tangent-CG residual, step, saved u: 3 n
     std::vector<double> stored_g0;
     std::vector<char>   stored_ok;
 
@@ -130,6 +133,7 @@ struct fansgpu_ctx {
     bool   tc_slower  = false; // the autotuner measured the CUDA-core operator faster on this grid
     int    tune       = 1;     // FANSGPU_TUNE: 1 FFT tiles (default), 3 + operator, 0 defaults, 2 forced
     int    tune_force[3] = {0, 0, 0}; // forced z / y / x tile variants
+    int    tc_wait_limit = 0;         // tensor-core operator's pipeline-wait bound in polls (0: default)
     bool   tuned      = false;
 };
 
@@ -757,6 +761,7 @@ StencilArgs mixed_operator_args(fansgpu_ctx *ctx, int cd)
     sa.scal     = ctx->scal;
     sa.red      = ctx->red;
     sa.red_site = SITE_STENCIL;
+    sa.wait_limit = ctx->tc_wait_limit;
     return sa;
 }
 
@@ -1631,6 +1636,17 @@ int fansgpu_reset(fansgpu_ctx *ctx)
     return 0;
 }
 
+int fansgpu_set_wait_limit(fansgpu_ctx *ctx, int32_t polls)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (polls < 0)
+        return fail(ctx, FANSGPU_EINVAL, "wait limit: polls >= 0 required (0 restores the default)");
+    ctx->tc_wait_limit = polls;
+    ctx->graphs_valid  = false; // captured operator launches carry the bound
+    return 0;
+}
+
 int fansgpu_set_refresh(fansgpu_ctx *ctx, double factor)
 {
     if (!ctx)
@@ -2188,11 +2204,11 @@ int solve_newton(fansgpu_ctx *ctx, int *inner)
             return fail(ctx, FANSGPU_EUNSUPPORTED,
                         "Newton-Krylov: phase %d: only J2PlasticityNew and linear elastic laws have a tangent", ph);
     }
-    if (!ctx->nwt && (rc = dalloc(ctx, &ctx->nwt, 2 * (size_t)n)))
+    if (!ctx->nwt && (rc = dalloc(ctx, &ctx->nwt, 3 * (size_t)n)))
         return rc;
     if ((rc = ensure_rows(ctx)))
         return rc;
-    double *res = ctx->nwt, *du = ctx->nwt + n;
+    double *res = ctx->nwt, *du = ctx->nwt + n, *u_save = ctx->nwt + 2 * n;
     auto residual_norm = [&](int first, double *out) -> int {
         int rr;
         if ((rr = run_residual64(ctx, ctx->u, ctx->r)))
@@ -2219,6 +2235,7 @@ int solve_newton(fansgpu_ctx *ctx, int *inner)
     if (ctx->tol.n_it > 0 && err_rel > ctx->tol.tolerance)
         ctx->u_zero = false;
     double eta = 0.1;
+    ctx->newton_stalled = false;
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         // the tangent at the current u and the committed state; its right-hand side is -R(u)
         const AdjArgs a = adj_args(ctx, ctx->u, ctx->g0_d, ctx->ep_t, ctx->q_t);
@@ -2228,6 +2245,7 @@ int solve_newton(fansgpu_ctx *ctx, int *inner)
         *inner += its;
         if (rc && rc != FANSGPU_ENOTCONV) // an inner solve stopped by n_it still gives a usable step
             return rc;
+        FANS_CUDA_CHECK(cudaMemcpyAsync(u_save, ctx->u, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
         FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, du, 1.0, n, ctx->st));
         double err_new = 0.0, lambda = 1.0;
         if ((rc = residual_norm(0, &err_new)))
@@ -2237,6 +2255,17 @@ int solve_newton(fansgpu_ctx *ctx, int *inner)
             FANS_CUDA_CHECK(launch_axpy<double>(ctx->u, du, -lambda, n, ctx->st));
             if ((rc = residual_norm(0, &err_new)))
                 return rc;
+        }
+        if (!(err_new < err)) {
+            // no decrease after the last halving: put u back (and with it r and the
+            // trial internal variables) and stop; the solve reports ENOTCONV
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->u, u_save, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
+            if ((rc = residual_norm(0, &err_new)))
+                return rc;
+            fail(ctx, FANSGPU_ENOTCONV, "Newton-Krylov: no decrease of the residual after 5 step halvings at step %d",
+                 ctx->iter + 1);
+            ctx->newton_stalled = true;
+            break;
         }
         ctx->iter++;
         ctx->err_all.push_back(err_new);

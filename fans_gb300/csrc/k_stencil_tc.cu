@@ -57,8 +57,20 @@ constexpr int COL_LO = 32, COL_A = 0, COL_D = 64;
 // dynamic shared memory requested: with the 1 KB reserved per block, 3 CTAs fit in an SM's 228 KB
 // and 4 do not (4 x 128 tensor-memory columns would fit, 4 x 288 threads' registers would not)
 constexpr int SMEM_REQ = 64 * 1024;
-constexpr unsigned kWaitLimit = 1u << 22; // bounded mbarrier waits (try_wait suspends between polls)
-enum { BAR_AFULL = 0, BAR_DFULL = 1, BAR_DFREE = 2, BAR_STAGED = 3, BAR_SFREE = 3 + R, NBAR = 3 + 2 * R };
+// Bounded mbarrier waits: try_wait polls (each suspends the thread for a while) before a wait
+// gives up; StencilArgs::wait_limit overrides it (a diagnostics control that lets a test make the
+// waits expire).  Draining the tensor pipe after an abort has its own, fixed bound.
+constexpr unsigned kWaitLimit  = 1u << 22;
+constexpr unsigned kDrainLimit = 1u << 22;
+enum {
+    BAR_AFULL  = 0,
+    BAR_DFULL  = 1,
+    BAR_DFREE  = 2,
+    BAR_STAGED = 3,
+    BAR_SFREE  = 3 + R,
+    BAR_DRAIN  = 3 + 2 * R, // the issuer's MMAs in flight after an abort
+    NBAR       = 4 + 2 * R
+};
 static_assert(NEL == 128 && EYN == 4 && EZN == 32, "one M-tile per element plane, one warp per element row");
 
 template <int C, int NPH>
@@ -151,10 +163,22 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Wait for the phase with the given parity; bounded, and released by the abort flag.
-__device__ __forceinline__ void mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag)
+// One poll of the phase with the given parity.
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 {
-    for (unsigned it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 " selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
+// Wait for the phase with the given parity; bounded (`limit` polls), and released by the abort flag.
+__device__ __forceinline__ void mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, unsigned limit)
+{
+    for (unsigned it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
                      " selp.u32 %0, 1, 0, p;\n}\n"
@@ -186,6 +210,7 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + Cfg::OFF_BAR + NBAR * 8 + 4);
     double       *red_smem  = reinterpret_cast<double *>(smem + Cfg::OFF_RED);
     auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+    const unsigned wlim = a.wait_limit > 0 ? (unsigned)a.wait_limit : kWaitLimit;
 
     const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
     const long long N = (long long)nx * ny * nz;
@@ -206,6 +231,7 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
             mbar_init(bar(BAR_STAGED + s), NGRP);
             mbar_init(bar(BAR_SFREE + s), NGRP);
         }
+        mbar_init(bar(BAR_DRAIN), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -294,12 +320,12 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
         for (int j = 0; j < J; ++j) {
             const int m = j + 1; // node plane to stage
             if (m >= R)                     // consumers are done with node plane m - R
-                mbar_wait(bar(BAR_SFREE + m % R), (uint32_t)(((m - R) / R) & 1), abort_flag);
+                mbar_wait(bar(BAR_SFREE + m % R), (uint32_t)(((m - R) / R) & 1), abort_flag, wlim);
             stage(m);
             fetch(m + RAWD - 1);            // into the raw slot node plane m-1 used
             named_bar(1, NGRP);     // node planes j and j+1 staged by all producers
             if (j >= 1)             // the MMAs of plane j-1 have read A
-                mbar_wait(bar(BAR_DFULL), (uint32_t)((j - 1) & 1), abort_flag);
+                mbar_wait(bar(BAR_DFULL), (uint32_t)((j - 1) & 1), abort_flag, wlim);
             __syncwarp(); // tcgen05.st is warp-aligned
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             // element row of plane j, split hi/lo, into this thread's lane of A
@@ -348,7 +374,7 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
         for (int j = 0; j < J; ++j) {
             const int X = xs - 1 + j, b = j & 1; // b: exchange parity
             const int ph_next = (NPH > 1 && j + 1 < J) ? (int)a.ms[(long long)wrap(X + 1, nx) * plane + el_yz] : 0;
-            mbar_wait(bar(BAR_DFULL), (uint32_t)(j & 1), abort_flag);
+            mbar_wait(bar(BAR_DFULL), (uint32_t)(j & 1), abort_flag, wlim);
             __syncwarp(); // tcgen05.ld is warp-aligned
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             float out[NCOL]; // this element's phase columns, 16 at a time
@@ -394,7 +420,7 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
                 xw[c * 32] = Z[C + c];
             named_bar(2, NGRP);
             if (X >= xs) {
-                mbar_wait(bar(BAR_STAGED + j % R), (uint32_t)((j / R) & 1), abort_flag); // node plane X
+                mbar_wait(bar(BAR_STAGED + j % R), (uint32_t)((j / R) & 1), abort_flag, wlim); // node plane X
                 if (out_ok) {
                     const long long gi = (long long)wrap(X, nx) * plane + oyz;
                     const float    *xr = Xch + (b * EYN + ey - 1) * C * 32 + ez;
@@ -417,9 +443,9 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
         const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Cfg::NW >> 3) << 17) | (8u << 24);
         const uint32_t wbase = smem_u32(smem + Cfg::OFF_W);
         for (int j = 0; j < J; ++j) {
-            mbar_wait(bar(BAR_AFULL), (uint32_t)(j & 1), abort_flag);
+            mbar_wait(bar(BAR_AFULL), (uint32_t)(j & 1), abort_flag, wlim);
             if (j >= 1) // consumers have read D of plane j-1
-                mbar_wait(bar(BAR_DFREE), (uint32_t)((j - 1) & 1), abort_flag);
+                mbar_wait(bar(BAR_DFREE), (uint32_t)((j - 1) & 1), abort_flag, wlim);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (!*abort_flag) {
                 const uint32_t d = tmem + COL_D, ah = tmem + COL_A, al = tmem + COL_A + COL_LO;
@@ -439,6 +465,15 @@ __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const floa
                              : "memory");
             } else {
                 mbar_arrive(bar(BAR_DFULL)); // keep the consumers' phases moving
+            }
+        }
+        if (*abort_flag) {
+            // the consumers may have stopped waiting for MMAs still in flight: wait (bounded) for
+            // every MMA this thread issued before tensor memory is released
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             bar(BAR_DRAIN))
+                         : "memory");
+            for (unsigned it = 0; it < kDrainLimit && !mbar_try(bar(BAR_DRAIN), 0u); ++it) {
             }
         }
     }

@@ -40,6 +40,7 @@ struct StencilArgs {
     CgScalars     *scal;
     GridRed        red;
     int            red_site;
+    int            wait_limit; // tensor-core operator: polls before a pipeline wait gives up (0: default)
 };
 template <typename T>
 cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st);

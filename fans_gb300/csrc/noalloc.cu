@@ -87,12 +87,17 @@ __global__ void __launch_bounds__(kThreads) k_norm_noalloc(const double *__restr
     }
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current (the first call on a device does this set-up).
+// Device address of the scratch array.  It is looked up on every call made
+// outside stream capture (cudaGetSymbolAddress is cheap), so a context that was
+// destroyed and made again (cudaDeviceReset, a new primary context) never sees
+// a stale address.  A call made while its stream is being captured cannot make
+// that lookup safely and uses the address the last uncaptured call on the same
+// device found: the first call on a device must therefore come before any
+// stream capture.
 std::mutex     g_mu;
 unsigned char *g_addr[256] = {nullptr};
 
-int scratch_address(unsigned char **addr)
+int scratch_address(cudaStream_t st, unsigned char **addr)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -101,17 +106,29 @@ int scratch_address(unsigned char **addr)
                              cudaGetErrorString(e));
     if (dev < 0 || dev >= 256)
         return fansgpu::fail(nullptr, FANSGPU_EUNSUPPORTED, "fansgpu_residual_norm_noalloc: device id %d", dev);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess)
+        return fansgpu::fail(nullptr, FANSGPU_ECUDA, "fansgpu_residual_norm_noalloc: stream query: %s",
+                             cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        e       = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return fansgpu::fail(nullptr, FANSGPU_ECUDA,
-                                 "fansgpu_residual_norm_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-                                 cudaGetErrorString(e));
-        g_addr[dev] = static_cast<unsigned char *>(p);
+    if (cap != cudaStreamCaptureStatusNone) {
+        if (!g_addr[dev])
+            return fansgpu::fail(nullptr, FANSGPU_ESTATE,
+                                 "fansgpu_residual_norm_noalloc: first call on device %d made during stream capture; "
+                                 "call it once before capturing",
+                                 dev);
+        *addr = g_addr[dev];
+        return 0;
     }
-    *addr = g_addr[dev];
+    void *p = nullptr;
+    e       = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return fansgpu::fail(nullptr, FANSGPU_ECUDA,
+                             "fansgpu_residual_norm_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
+                             cudaGetErrorString(e));
+    g_addr[dev] = static_cast<unsigned char *>(p);
+    *addr       = g_addr[dev];
     return 0;
 }
 
@@ -129,11 +146,11 @@ extern "C" int fansgpu_residual_norm_noalloc(const double *r_dev, int64_t n, int
                              "fansgpu_residual_norm_noalloc: n = %lld outside [0, %lld] (the static scratch holds "
                              "%d block partials of %lld values each)",
                              (long long)n, (long long)FANSGPU_NOALLOC_MAX_VALUES, kMaxBlocks, kChunk);
+    cudaStream_t   st      = static_cast<cudaStream_t>(stream);
     unsigned char *scratch = nullptr;
-    int            rc      = scratch_address(&scratch);
+    int            rc      = scratch_address(st, &scratch);
     if (rc)
         return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t  e;
     if (n == 0) {
         e = cudaMemsetAsync(out_dev, 0, sizeof(double), st);

@@ -168,6 +168,10 @@ class Context:
         """Mixed precision: FP32-residual reduction that triggers an FP64 refresh."""
         self._chk(self.lib.fansgpu_set_refresh(self.ctx, float(factor)))
 
+    def set_wait_limit(self, polls):
+        """Diagnostics: polls before a tensor-core pipeline wait gives up (0: default)."""
+        self._chk(self.lib.fansgpu_set_wait_limit(self.ctx, int(polls)))
+
     def tuning(self):
         """fansgpu_tuning: {"fp64": (z, y, x), "fp32": (z, y, x), "tensor_core": bool}."""
         out = np.zeros(7, dtype=np.int32)

@@ -344,11 +344,14 @@ int fansgpu_kernel_times(fansgpu_ctx *ctx, double *ms_total, int64_t *launches, 
  * receives ||r|| in `measure` (FANSGPU_L1 / L2 / LINF), ordered on `stream`
  * (a cudaStream_t, NULL = default stream).  The scratch is a static array of
  * 256 KiB + 256 B that every GPU loading the library holds until exit; n is
- * limited to FANSGPU_NOALLOC_MAX_VALUES (FANSGPU_EINVAL beyond).  The first
- * call on a device looks the array's device address up (cudaGetSymbolAddress)
- * and should come before any stream capture.  All calls on a GPU share the
- * array: calls that overlap on the GPU race and must be serialised.  Errors are
- * reported through fansgpu_last_error(NULL). */
+ * limited to FANSGPU_NOALLOC_MAX_VALUES (FANSGPU_EINVAL beyond).  Each call
+ * made outside stream capture looks the array's device address up
+ * (cudaGetSymbolAddress); a call made while `stream` is being captured reuses
+ * the address the last earlier call on that device found, so the first call on
+ * a device must come before any stream capture (FANSGPU_ESTATE otherwise).  All
+ * calls on a GPU share the array: calls that overlap on the GPU race and must
+ * be serialised.  Errors are reported through fansgpu_last_error(NULL), which
+ * is per calling thread. */
 #define FANSGPU_NOALLOC_MAX_VALUES 268435456LL
 int fansgpu_residual_norm_noalloc(const double *r_dev, int64_t n, int32_t measure, double *out_dev, void *stream);
 
@@ -356,6 +359,16 @@ int fansgpu_residual_norm_noalloc(const double *r_dev, int64_t n, int32_t measur
  * last FP64 true-residual refresh before the next one (default 1e-4; (0, 1)).
  * No reference counterpart (the reference runs in FP64 only). */
 int fansgpu_set_refresh(fansgpu_ctx *ctx, double factor);
+
+/* Diagnostics: the bound on each pipeline wait of the tensor-core operator
+ * (MIXED precision), in mbarrier polls; 0 restores the default (2^22 polls,
+ * far beyond any wait of a healthy launch).  A wait that runs out sets an
+ * abort flag that releases every other wait of its CTA; the CTA then waits for
+ * its own MMAs in flight, frees its tensor memory and returns, and the solve
+ * reports FANSGPU_ECUDA ("... wait timed out") with the context still usable.
+ * A small bound lets a test make the waits expire on purpose.  No reference
+ * counterpart (the reference has no device work). */
+int fansgpu_set_wait_limit(fansgpu_ctx *ctx, int32_t polls);
 
 /* Library version string. */
 const char *fansgpu_version(void);

@@ -13,8 +13,8 @@
   0.832542244829 and P33 = 74.757449712464 at F33 = 2 on CompressibleNeoHookean),
   which pins the oracle and the GPU path to numbers the reference computed.
 
-Run from the repository root with the reference checkout at REF (default
-/root/reference):  python tests/golden/make_fixtures.py [REF]
+Run from the repository root with a FANS checkout given as the argument or in
+the FANS_REFERENCE environment variable:  python tests/golden/make_fixtures.py REF
 """
 import hashlib
 import json
@@ -27,12 +27,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from fans_gb300 import h5  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FANS_REFERENCE", "")
 KEEP = ("microstructure", "problem_type", "strain_type", "materials", "FE_type", "method", "error_parameters",
         "n_it", "macroscale_loading", "results")
 
 
 def main():
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_fixtures.py REF  (or set FANS_REFERENCE): REF is a FANS checkout")
     src = os.path.join(REF, "test", "microstructures", "sphere32.h5")
     raw = open(src, "rb").read()
     ms = h5.read_microstructure(src, "/sphere/32x32x32/ms").astype(np.uint8)

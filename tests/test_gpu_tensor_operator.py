@@ -69,3 +69,34 @@ def test_tensor_operator_single_phase_and_hex8r():
         b = _solve(P, g0, simt=True)
         assert abs(a["st"]["iterations"] - b["st"]["iterations"]) <= 1
         assert rel(a["stress"], b["stress"]) < 1e-9
+
+
+def test_tensor_operator_wait_timeout_is_reported_and_recovered():
+    """Failure detection of the tensor-core pipeline without a GPU fault: with
+    the pipeline-wait bound cut to two polls (fansgpu_set_wait_limit), the
+    waits run out, every CTA sets its abort flag, waits for its own MMAs in
+    flight, frees its tensor memory and returns; the solve reports ECUDA with
+    "timed out" and the context stays usable.  With the default bound restored,
+    the same context (and a fresh one) solve to the same answer as before."""
+    from fans_gb300 import _lib
+
+    ms = random_ms((32, 32, 32), vf=0.3, seed=31)
+    P = oracle_problem(ms, 3, ELASTIC, "HEX8")
+    g0 = np.linspace(1.0, 0.4, 6)
+    ref = _solve(P, g0, simt=False)
+    ctx = gpu_context(P, precision="mixed")
+    ctx.set_tolerance("L2", "relative", 1e-8, 500)
+    ctx.set_gradient(g0)
+    assert ctx.tuning()["tensor_core"]
+    ctx.set_wait_limit(2)
+    with pytest.raises(_lib.FansGpuError) as ei:
+        ctx.solve()
+    assert ei.value.code == _lib.ECUDA and "timed out" in str(ei.value)
+    ctx.set_wait_limit(0)
+    ctx.reset()
+    st = ctx.solve()
+    assert st["converged"] and st["iterations"] == ref["st"]["iterations"]
+    assert rel(ctx.homogenized_stress(), ref["stress"]) < 1e-12
+    ctx.close()
+    again = _solve(P, g0, simt=False)
+    assert rel(again["stress"], ref["stress"]) < 1e-12

@@ -11,7 +11,9 @@ from fans_gb300 import h5
 from fans_gb300.reader import MixedBC, Reader
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_H5 = "/root/reference/test/microstructures/sphere32.h5"
+# a FANS checkout named by the FANS_REFERENCE environment variable (optional): its
+# test/microstructures/sphere32.h5 is the file the committed fixture was decoded from
+REF_H5 = os.path.join(os.environ.get("FANS_REFERENCE", ""), "test", "microstructures", "sphere32.h5")
 
 
 def test_sphere32_fixture_metadata():
@@ -23,7 +25,8 @@ def test_sphere32_fixture_metadata():
     assert ms.mean() == pytest.approx(0.2668, abs=1e-4)  # 26.7 % inclusion
 
 
-@pytest.mark.skipif(not os.path.exists(REF_H5), reason="reference checkout not present")
+@pytest.mark.skipif(not os.environ.get("FANS_REFERENCE") or not os.path.exists(REF_H5),
+                    reason="FANS_REFERENCE does not name a FANS checkout")
 def test_reader_decodes_chunked_deflate_fixture():
     f = h5.H5File(REF_H5)
     assert f.keys("/") == ["sphere"]
@@ -66,6 +69,38 @@ def test_writer_round_trip(tmp_path):
         w.dataset("/m/ms_xyz", ms, {"permute_order": "xyz"})
     assert np.array_equal(h5.read_microstructure(str(q), "/m/ms"), ms)
     assert np.array_equal(h5.read_microstructure(str(q), "/m/ms_xyz"), ms)
+
+
+def test_writer_output_read_by_h5py(tmp_path):
+    """An independent HDF5 implementation (h5py over libhdf5) reads what
+    fans_gb300.h5 writes: groups, the empty path element FANS's result paths
+    have, float64 / float32 / uint8 / int32 datasets, a replaced dataset and the
+    permute_order string attribute of Reader::WriteSlab (reader.h:314-329).
+    Skipped where h5py is not installed."""
+    h5py = pytest.importorskip("h5py")
+    rng = np.random.default_rng(1)
+    a = rng.random((5, 4, 3))
+    b = rng.integers(0, 255, (6, 7, 8), dtype=np.uint8)
+    c = rng.integers(-5, 5, (3, 2), dtype=np.int32)
+    p = tmp_path / "t.h5"
+    with h5.H5Writer(str(p)) as w:
+        w.dataset("/ms_results//load0/time_step0/stress", a, {"permute_order": "zyx"})
+        w.dataset("/g/b", b)
+        w.dataset("/g/b", b + 1)
+        w.dataset("/g/c", c)
+        w.dataset("/f32", np.float32([1.5, -2.0]))
+        for i in range(40):
+            w.dataset(f"/many/load{i}/v", np.arange(i + 1, dtype=np.float64))
+    with h5py.File(str(p), "r") as f:
+        d = f["/ms_results//load0/time_step0/stress"]
+        assert np.array_equal(d[...], a)
+        pa = d.attrs["permute_order"]
+        assert (pa.decode() if isinstance(pa, bytes) else str(pa)) == "zyx"
+        assert np.array_equal(f["/g/b"][...], b + 1) and f["/g/b"].dtype == np.uint8
+        assert np.array_equal(f["/g/c"][...], c)
+        assert f["/f32"].dtype == np.float32
+        assert sorted(f["/many"].keys()) == sorted(f"load{i}" for i in range(40))
+        assert np.array_equal(f["/many/load39/v"][...], np.arange(40.0))
 
 
 def test_reader_parses_reference_inputs():

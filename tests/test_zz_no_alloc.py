@@ -86,3 +86,36 @@ def _lib_max(lib):
 
     hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "fans_gb300.h")
     return int(re.search(r"FANSGPU_NOALLOC_MAX_VALUES\s+(\d+)LL", open(hdr).read()).group(1))
+
+
+def test_noalloc_norm_many_blocks_and_nan():
+    """A field of 8192 * 300 + 17 values spans 301 blocks (the last one ragged),
+    so the last block folds 301 partials in block order: L1, L2 and Linfinity
+    equal torch's FP64 norms to 1e-12, twice in a row; one NaN makes every
+    measure NaN (the maximum keeps NaN, as the solver's Linfinity does)."""
+    import torch
+
+    from fans_gb300 import _lib
+
+    lib = _lib.load()
+    n = 8192 * 300 + 17
+    g = torch.Generator(device="cpu").manual_seed(23)
+    x = torch.randn(n, dtype=torch.float64, generator=g).cuda()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    refs = {"L1": x.abs().sum().item(), "L2": x.norm().item(), "Linfinity": x.abs().max().item()}
+    for measure, ref in refs.items():
+        vals = []
+        for _ in range(2):
+            out.fill_(-1.0)
+            assert _call(lib, x.data_ptr(), n, _lib.MEASURES[measure], out.data_ptr(), stream) == 0
+            torch.cuda.synchronize()
+            vals.append(out.item())
+        assert vals[0] == vals[1]
+        assert abs(vals[0] - ref) <= 1e-12 * ref, (measure, vals[0], ref)
+    x[n // 2] = float("nan")
+    for measure in refs:
+        out.fill_(-1.0)
+        assert _call(lib, x.data_ptr(), n, _lib.MEASURES[measure], out.data_ptr(), stream) == 0
+        torch.cuda.synchronize()
+        assert np.isnan(out.item()), measure
