@@ -46,8 +46,9 @@ EXPORTS = [
     "fansgpu_kernel_times", "fansgpu_residual_norm_noalloc", "fansgpu_set_refresh",
     "fansgpu_enable_mixed_bc", "fansgpu_disable_mixed_bc", "fansgpu_get_gradient", "fansgpu_set_voxel_field",
     "fansgpu_store_solution", "fansgpu_stiffness_gradient", "fansgpu_solve_batch", "fansgpu_yield_stress_adjoint",
-    "fansgpu_tuning", "fansgpu_set_wait_limit",
+    "fansgpu_tuning", "fansgpu_set_wait_limit", "fansgpu_set_gradients", "fansgpu_select_rhs", "fansgpu_rhs_stats",
 ]
+MAX_RHS = 6
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
                 "residual64", "norm", "green_table", "strain_stress"]
 
@@ -55,7 +56,7 @@ KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv",
 class Desc(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32 * 3), ("L", ctypes.c_double * 3), ("howmany", ctypes.c_int32),
                 ("fe_type", ctypes.c_int32), ("precision", ctypes.c_int32), ("method", ctypes.c_int32),
-                ("strain_type", ctypes.c_int32)]
+                ("strain_type", ctypes.c_int32), ("n_rhs", ctypes.c_int32)]
 
 
 class Tol(ctypes.Structure):
@@ -136,6 +137,9 @@ def _declare(L):
     L.fansgpu_yield_stress_adjoint.argtypes = [vp, ip, dp, ip, dp, ctypes.c_double, dp, dp, i32p]
     L.fansgpu_tuning.argtypes = [vp, i32p]
     L.fansgpu_set_wait_limit.argtypes = [vp, ip]
+    L.fansgpu_set_gradients.argtypes = [vp, ip, dp]
+    L.fansgpu_select_rhs.argtypes = [vp, ip]
+    L.fansgpu_rhs_stats.argtypes = [vp, ip, ctypes.POINTER(Stats)]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

@@ -31,6 +31,11 @@ struct LoopCtl {
     double err0, last_true, tol, reliable;
     int    iter, n_it, relative, cap;
 };
+// The same for the multi-RHS loop: per right-hand side err0 and the last true residual.
+struct LoopCtlR {
+    double err0[kMaxRhs], last_true[kMaxRhs], tol, reliable;
+    int    iter, n_it, relative, cap, nrhs;
+};
 
 struct fansgpu_ctx {
     fansgpu_desc desc{};
@@ -59,6 +64,7 @@ struct fansgpu_ctx {
     float  *r32 = nullptr, *s32 = nullptr, *d32[2] = {nullptr, nullptr}, *Kd32 = nullptr, *e32 = nullptr;
     std::vector<double> K64h, f64h; // host copies of the per-phase tables (kernel-parameter path)
     float              *Kdf = nullptr, *fdf = nullptr; // double-float [hi | lo] tables (mixed refresh)
+    size_t              fdf_cap = 0;
     std::vector<float>  K32h;
     bool                u_zero = true; // v_u known to be zero (fresh context / reset): R(u) = F
     double *K64 = nullptr, *f64 = nullptr, *Cph = nullptr, *Bbar_d = nullptr, *g0_d = nullptr, *K0c = nullptr;
@@ -134,6 +140,25 @@ struct fansgpu_ctx {
     int    tune       = 1;     // FANSGPU_TUNE: 1 FFT tiles (default), 3 + operator, 0 defaults, 2 forced
     int    tune_force[3] = {0, 0, 0}; // forced z / y / x tile variants
     int    tc_wait_limit = 0;         // tensor-core operator's pipeline-wait bound in polls (0: default)
+
+    // several right-hand sides (desc.n_rhs): u, r and u_prev are per-RHS slices of u0, r0, up0
+    // (n values each) and point at the selected RHS `cur`; the FP32 fields of the mixed path and
+    // its spectrum hold nrhs slices (the single-RHS paths use slice 0 as scratch)
+    int                              nrhs = 1, cur = 0;
+    double                          *u0 = nullptr, *r0 = nullptr, *up0 = nullptr;
+    std::vector<std::vector<double>> rhs_g0, rhs_err;
+    std::vector<int>                 rhs_iter, rhs_ref;
+    std::vector<char>                rhs_uzero;
+    double                           rhs_ms = 0; // device time of the last solve (all RHS)
+    int                             *act = nullptr, *act_h = nullptr; // active flags of the multi-RHS loop
+    LoopCtlR                        *ctlr = nullptr, *ctlr_h = nullptr;
+    bool                             graphs_multi = false; // the captured graphs are the multi-RHS iteration
+
+    // basis tensor-core operator (k_stencil_tcb): exact basis blocks and per-phase coefficients
+    float *Wtb = nullptr, *coef_tb = nullptr;
+    int    tb_nb = 0;
+    bool   use_tcb = false;
+    bool   tc_legacy = false; // FANSGPU_STENCIL=tc: the per-phase 3xTF32 operator instead
     bool   tuned      = false;
 };
 
@@ -179,6 +204,7 @@ long long max_reduction_blocks(const Grid3 &g, int C)
     long long b = std::max<long long>(kMaxBlocks, stencil_blocks(g));
     b           = std::max<long long>(b, (long long)C * g.nx * g.ny); // z passes: at least one row per CTA
     b           = std::max<long long>(b, stencil_tc_blocks(g));
+    b           = std::max<long long>(b, (long long)kMaxRhs * kMaxBlocks); // multi-RHS update: one grid per RHS
     return b;
 }
 
@@ -232,6 +258,8 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
         kc /= 2;
     p.kc_x    = kc;
     p.use_reg = conv_reg_supported(g) ? 1 : 0;
+    p.nrhs    = 1;
+    p.active  = nullptr;
     if (!p.use_reg && cs * (2 * (size_t)p.C * g.nx * p.kc_x + g.nx) > 200 * 1024)
         return fail(ctx, FANSGPU_EUNSUPPORTED, "n_x=%d too large for the shared-memory x pass", g.nx);
     return 0;
@@ -459,6 +487,57 @@ int setup(fansgpu_ctx *ctx)
             FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Wtc, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, ctx->st));
             ctx->use_tc = true;
         }
+        // the basis operator: every phase an isotropic law of this problem, each basis block exact
+        ctx->use_tcb = false;
+        if (ctx->tc_allowed && !ctx->tc_legacy && !ctx->tc_slower && ctx->desc.precision == FANSGPU_MIXED &&
+            ctx->nstr == (C == 1 ? 3 : 6)) {
+            const int iso = C == 1 ? FANSGPU_LAW_THERMAL_ISO : FANSGPU_LAW_ELASTIC_ISO, nb = C == 1 ? 1 : 2;
+            bool      ok  = stencil_tcb_supported(ctx->g, C, nb, ctx->nph);
+            for (int ph = 0; ph < ctx->nph && ok; ++ph)
+                ok = ctx->law[ph] == iso;
+            // basis constitutive matrices: conduction I; elasticity 1 1^T (lambda) and 2 I (mu),
+            // so that C_ph = lambda 1 1^T + mu 2 I (LinearElastic.h:24-35)
+            std::vector<double> Kb((size_t)nb * NC * NC), Cb(nstr * nstr), q(nb);
+            for (int b = 0; b < nb && ok; ++b) {
+                std::fill(Cb.begin(), Cb.end(), 0.0);
+                for (int i = 0; i < nstr; ++i)
+                    for (int j = 0; j < nstr; ++j)
+                        Cb[i * nstr + j] = C == 1 ? (i == j ? 1.0 : 0.0)
+                                         : b == 0 ? (i < 3 && j < 3 ? 1.0 : 0.0)
+                                                  : (i == j ? 2.0 : 0.0);
+                fe::element_stiffness(C, ctx->ngp, ctx->B, Cb.data(), ctx->ve, Ke);
+                std::copy(Ke.begin(), Ke.end(), Kb.begin() + (size_t)b * NC * NC);
+            }
+            if (ok)
+                ok = stencil_tcb_quanta(C, Kb.data(), nb, q.data());
+            if (ok) {
+                std::vector<float> w(stencil_tcb_weights(C, nb)), cf((size_t)ctx->nph * nb);
+                stencil_tcb_pack_weights(C, nb, Kb.data(), q.data(), w.data());
+                for (int ph = 0; ph < ctx->nph; ++ph) {
+                    const std::vector<double> &pr = ctx->prm[ph];
+                    if (C == 1)
+                        cf[ph] = (float)(pr[0] * q[0]);
+                    else {
+                        cf[ph * 2 + 0] = (float)((pr[0] - 2.0 * pr[1] / 3.0) * q[0]); // lambda = K - 2G/3
+                        cf[ph * 2 + 1] = (float)(pr[1] * q[1]);                      // mu = G
+                    }
+                }
+                for (float *p : {ctx->Wtb, ctx->coef_tb})
+                    if (p)
+                        cudaFree(p);
+                ctx->Wtb = ctx->coef_tb = nullptr;
+                int rc5;
+                if ((rc5 = dalloc(ctx, &ctx->Wtb, w.size())) || (rc5 = dalloc(ctx, &ctx->coef_tb, cf.size())))
+                    return rc5;
+                FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Wtb, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice,
+                                                ctx->st));
+                FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->coef_tb, cf.data(), sizeof(float) * cf.size(),
+                                                cudaMemcpyHostToDevice, ctx->st));
+                FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st)); // w and cf are host temporaries
+                ctx->tb_nb   = nb;
+                ctx->use_tcb = true;
+            }
+        }
         {
             std::vector<float> kdf(2 * K64.size());
             for (size_t i = 0; i < K64.size(); ++i) {
@@ -525,12 +604,14 @@ int setup(fansgpu_ctx *ctx)
                 fdf[i]            = hi;
                 fdf[f.size() + i] = (float)(f[i] - (double)hi);
             }
-            if (ctx->fdf)
+            if (ctx->fdf && ctx->fdf_cap < fdf.size()) { // kept across gradients (one RHS after another)
                 cudaFree(ctx->fdf);
-            ctx->fdf = nullptr;
+                ctx->fdf = nullptr;
+            }
             int rc2;
-            if ((rc2 = dalloc(ctx, &ctx->fdf, fdf.size())))
+            if (!ctx->fdf && (rc2 = dalloc(ctx, &ctx->fdf, fdf.size())))
                 return rc2;
+            ctx->fdf_cap = std::max(ctx->fdf_cap, fdf.size());
             FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->fdf, fdf.data(), sizeof(float) * fdf.size(), cudaMemcpyHostToDevice, ctx->st));
         }
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->g0_d, ctx->g0.data(), sizeof(double) * nstr, cudaMemcpyHostToDevice, ctx->st));
@@ -643,6 +724,33 @@ int run_operator_elem(fansgpu_ctx *ctx, const double *x, double *y)
     FANS_CUDA_CHECK(launch_gather(ctx->rows, y, ctx->g, ctx->C, ctx->st));
     tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
     return 0;
+}
+
+// The selected right-hand side's host state (history, iteration count, u = 0 flag,
+// g0) lives in the context's single-RHS members; store_rhs saves it, load_rhs makes
+// RHS k the selected one (its field slices, its state; the force tables follow g0).
+void store_rhs(fansgpu_ctx *ctx)
+{
+    const int k       = ctx->cur;
+    ctx->rhs_err[k]   = ctx->err_all;
+    ctx->rhs_iter[k]  = ctx->iter;
+    ctx->rhs_uzero[k] = ctx->u_zero ? 1 : 0;
+    ctx->rhs_g0[k]    = ctx->g0;
+}
+
+void load_rhs(fansgpu_ctx *ctx, int k)
+{
+    ctx->cur     = k;
+    ctx->u       = ctx->u0 + (long long)k * ctx->n;
+    ctx->r       = ctx->r0 + (long long)k * ctx->n;
+    ctx->uprev   = ctx->up0 + (long long)k * ctx->n;
+    ctx->err_all = ctx->rhs_err[k];
+    ctx->iter    = ctx->rhs_iter[k];
+    ctx->u_zero  = ctx->rhs_uzero[k] != 0;
+    if (ctx->g0 != ctx->rhs_g0[k]) {
+        ctx->g0          = ctx->rhs_g0[k];
+        ctx->force_dirty = true;
+    }
 }
 
 int init_scalars(fansgpu_ctx *ctx)
@@ -786,6 +894,44 @@ cudaError_t enqueue_mixed_iteration(fansgpu_ctx *ctx, int cd)
     return e;
 }
 
+// The mixed path runs as a multi-RHS iteration (every right-hand side in each
+// kernel) where the basis tensor-core operator and the register FFT passes apply.
+bool multi_rhs_path(const fansgpu_ctx *ctx)
+{
+    return ctx->desc.precision == FANSGPU_MIXED && ctx->use_tcb && ctx->cp32.use_reg && ctx->all_linear &&
+           !ctx->vscale && !ctx->mixed_active;
+}
+
+// One inner iteration over all right-hand sides (inactive ones skipped on the
+// device): s_k = -G*r_k with delta_k/beta_k, d_k = s_k + beta_k d_k,old with K d_k
+// and alpha_k, then the FP32 update of r_k and e_k.
+cudaError_t enqueue_mixed_iteration_rhs(fansgpu_ctx *ctx, int cd)
+{
+    const long long n = ctx->n;
+    ConvPlan<float> p = ctx->cp32;
+    p.nrhs            = ctx->nrhs;
+    p.active          = ctx->act;
+    ConvArgs    ca{ctx->r32, ctx->s32, -1.0, 1, ctx->scal, ctx->red, SITE_CONV};
+    cudaError_t e = run_conv<float>(ctx, p, ca);
+    if (e != cudaSuccess)
+        return e;
+    StencilArgs sa = mixed_operator_args(ctx, cd);
+    sa.nrhs        = ctx->nrhs;
+    sa.rhs_stride  = n;
+    sa.active      = ctx->act;
+    int e0         = tk_mark(ctx);
+    e              = launch_stencil_tcb(sa, ctx->Wtb, ctx->coef_tb, ctx->tb_nb, ctx->st);
+    if (e != cudaSuccess)
+        return e;
+    tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
+    UpdateArgs ua{n, ctx->r32, ctx->Kd32, ctx->e32, ctx->d32[cd ^ 1], ctx->s32, ctx->tol.measure, 1, ctx->scal,
+                  ctx->red, SITE_UPDATE, ctx->nrhs, ctx->act};
+    int e2 = tk_mark(ctx);
+    e      = launch_cg_update<float, float>(ua, ctx->st);
+    tk_span(ctx, FANSGPU_K_UPDATE, e2, tk_mark(ctx));
+    return e;
+}
+
 // ---------------------------------------------------------------------------
 // Autotuning: the register FFT passes' tile variants (per precision) and, with
 // FANSGPU_TUNE=all, tensor-core against CUDA-core operator on the mixed path.
@@ -905,10 +1051,37 @@ __global__ void k_loop_check(LoopCtl *c, const CgScalars *scal, double *hist, cu
     }
 }
 
+// The multi-RHS counterpart of k_loop_check: records every active RHS's residual
+// estimate (history row k) and halts where the host would act for any of them.
+__global__ void k_loop_check_rhs(LoopCtlR *c, const CgScalars *scal, const int *act, double *hist,
+                                 cudaGraphConditionalHandle h_while, cudaGraphConditionalHandle h_if, int first)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    const int it   = ++c->iter;
+    bool      halt = it >= c->n_it || it + 1 >= c->cap;
+    for (int k = 0; k < c->nrhs; ++k) {
+        if (!act[k])
+            continue;
+        const double err = scal[k].err;
+        if (it < c->cap)
+            hist[(size_t)k * c->cap + it] = err;
+        const double est_rel = c->relative ? err / c->err0[k] : err;
+        halt = halt || scal[k].converged < 0 || !(err == err) || est_rel <= c->tol || err <= c->reliable * c->last_true[k];
+    }
+    if (first) {
+        cudaGraphSetConditional(h_if, halt ? 0u : 1u);
+        if (halt)
+            cudaGraphSetConditional(h_while, 0u);
+    } else {
+        cudaGraphSetConditional(h_while, halt ? 0u : 1u);
+    }
+}
+
 // The inner loop as one CUDA graph per starting parity of the d ping-pong:
 //   WHILE(h_while) { iteration(p); check; IF(h_if) { iteration(p ^ 1); check } }
 // The two iterations are captured once and added as child graphs.
-int build_loop_graphs(fansgpu_ctx *ctx)
+int build_loop_graphs(fansgpu_ctx *ctx, bool multi)
 {
     int rc;
     if (!ctx->ctl) {
@@ -922,7 +1095,7 @@ int build_loop_graphs(fansgpu_ctx *ctx)
         e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess)
             break;
-        const cudaError_t ce = enqueue_mixed_iteration(ctx, p);
+        const cudaError_t ce = multi ? enqueue_mixed_iteration_rhs(ctx, p) : enqueue_mixed_iteration(ctx, p);
         e                    = cudaStreamEndCapture(ctx->st, &it[p]);
         if (ce != cudaSuccess)
             e = ce;
@@ -957,19 +1130,23 @@ int build_loop_graphs(fansgpu_ctx *ctx)
             e    = cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault);
         }
         LoopCtl         *c  = ctx->ctl;
+        LoopCtlR        *cr = ctx->ctlr;
         const CgScalars *sc = ctx->scal;
+        const int       *ac = ctx->act;
         double          *h  = ctx->hist;
         int              f1 = 1, f0 = 0;
         void            *a1[] = {&c, &sc, &h, &hw, &hi, &f1};
         void            *a0[] = {&c, &sc, &h, &hw, &hi, &f0};
+        void            *q1[] = {&cr, &sc, &ac, &h, &hw, &hi, &f1};
+        void            *q0[] = {&cr, &sc, &ac, &h, &hw, &hi, &f0};
         cudaKernelNodeParams kp{};
-        kp.func     = (void *)k_loop_check;
+        kp.func     = multi ? (void *)k_loop_check_rhs : (void *)k_loop_check;
         kp.gridDim  = dim3(1);
         kp.blockDim = dim3(32);
         if (e == cudaSuccess)
             e = cudaGraphAddChildGraphNode(&n1, body, nullptr, 0, it[p]);
         if (e == cudaSuccess) {
-            kp.kernelParams = a1;
+            kp.kernelParams = multi ? q1 : a1;
             e               = cudaGraphAddKernelNode(&n2, body, &n1, 1, &kp);
         }
         if (e == cudaSuccess) {
@@ -984,7 +1161,7 @@ int build_loop_graphs(fansgpu_ctx *ctx)
             e  = cudaGraphAddChildGraphNode(&m1, ib, nullptr, 0, it[p ^ 1]);
         }
         if (e == cudaSuccess) {
-            kp.kernelParams = a0;
+            kp.kernelParams = multi ? q0 : a0;
             e               = cudaGraphAddKernelNode(&m2, ib, &m1, 1, &kp);
         }
         if (e == cudaSuccess)
@@ -998,6 +1175,7 @@ int build_loop_graphs(fansgpu_ctx *ctx)
     if (e != cudaSuccess)
         return fail(ctx, FANSGPU_ECUDA, "inner-loop graph: %s", cudaGetErrorString(e));
     ctx->graphs_valid = true;
+    ctx->graphs_multi = multi;
     return 0;
 }
 
@@ -1035,7 +1213,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         if (ctx->hist)
             cudaFree(ctx->hist);
         ctx->hist = nullptr;
-        if ((rc = dalloc(ctx, &ctx->hist, (size_t)ctx->tol.n_it + 2)))
+        if ((rc = dalloc(ctx, &ctx->hist, ((size_t)ctx->tol.n_it + 2) * kMaxRhs)))
             return rc;
         ctx->hist_cap     = ctx->tol.n_it + 2;
         ctx->graphs_valid = false; // the graphs hold the history pointer
@@ -1043,7 +1221,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     while (ctx->iter < ctx->tol.n_it && err_rel > ctx->tol.tolerance) {
         int done = 1; // iterations run by this pass
         if (ctx->use_graphs && !ctx->timing && ctx->iter > 0) { // the first iteration runs uncaptured
-            if (!ctx->graphs_valid && (rc = build_loop_graphs(ctx)))
+            if ((!ctx->graphs_valid || ctx->graphs_multi) && (rc = build_loop_graphs(ctx, false)))
                 return rc;
         }
         if (ctx->use_graphs && !ctx->timing && ctx->iter > 0 && !ctx->loop_on_device) {
@@ -1108,6 +1286,195 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     }
     // corrections since the last reliable update (n_it reached) belong to u too
     FANS_CUDA_CHECK(launch_fold(ctx->u, ctx->e32, n, ctx->st));
+    return 0;
+}
+
+// The reliable update of RHS k (the selected one after the call): fold its FP32
+// correction into u_k, its true residual R(u_k) in double-float, ||r_k|| into
+// scal[k] and the FP32 re-seed of r_k.  Host reads follow at the caller's sync.
+// (The per-RHS vectors hold the state here: the members are loaded from them.)
+int refresh_rhs(fansgpu_ctx *ctx, int k, bool fold, bool set_err0)
+{
+    const long long n = ctx->n;
+    int             rc;
+    load_rhs(ctx, k);
+    if ((rc = setup(ctx))) // the force tables of g0_k
+        return rc;
+    if (fold) {
+        FANS_CUDA_CHECK(launch_fold(ctx->u, ctx->e32 + (long long)k * n, n, ctx->st));
+        ctx->u_zero       = false;
+        ctx->rhs_uzero[k] = 0;
+    }
+    if ((rc = run_residual_df(ctx)))
+        return rc;
+    int en = tk_mark(ctx);
+    FANS_CUDA_CHECK(launch_norm_fast(ctx->r, n, ctx->tol.measure, ctx->scal + k, set_err0 ? 1 : 0,
+                                     ctx->r32 + (long long)k * n, ctx->red, SITE_NORM, ctx->st));
+    tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx));
+    return 0;
+}
+
+int sync_scalars_rhs(fansgpu_ctx *ctx)
+{
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->scal_h, ctx->scal, sizeof(CgScalars) * ctx->nrhs, cudaMemcpyDeviceToHost,
+                                    ctx->st));
+    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+    tk_flush(ctx);
+    return 0;
+}
+
+// Multi-RHS mixed-precision CG: solve_cg_mixed's recurrences run for every
+// right-hand side at once, each RHS with its own CG scalars, reliable updates and
+// convergence test (so each takes exactly the iterations and values its own
+// solve would).  An RHS leaves the iteration (its active flag drops, so every
+// kernel skips it) once its true residual meets the tolerance.  The inner loop
+// stays on the device between the points where any RHS needs the host.
+int solve_cg_mixed_rhs(fansgpu_ctx *ctx, int only)
+{
+    const long long n = ctx->n;
+    const int       R = ctx->nrhs, home = ctx->cur;
+    auto            mine = [&](int k) { return only < 0 || k == only; }; // the RHS this solve covers
+    int             rc;
+    store_rhs(ctx);
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->s32, 0, sizeof(float) * n * R, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->d32[0], 0, sizeof(float) * n * R, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->e32, 0, sizeof(float) * n * R, ctx->st));
+    ctx->cur_d = 0;
+    for (int k = 0; k < R; ++k) {
+        CgScalars s0{};
+        s0.delta       = 1.0; // solverCG.h:82
+        ctx->scal_h[k] = s0;
+        ctx->act_h[k]  = 0;
+        if (mine(k))
+            ctx->rhs_ref[k] = 0;
+    }
+    FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->scal, ctx->scal_h, sizeof(CgScalars) * R, cudaMemcpyHostToDevice, ctx->st));
+    for (int k = 0; k < R; ++k)
+        if (mine(k) && (rc = refresh_rhs(ctx, k, false, true))) // r_k = R(u_k) (compute_residual<2>, solverCG.h:76)
+            return rc;
+    if ((rc = sync_scalars_rhs(ctx)))
+        return rc;
+    std::vector<double> last_true(R), err_rel(R);
+    std::vector<char>   on(R, 0);
+    int                 n_on = 0;
+    for (int k = 0; k < R; ++k) {
+        if (!mine(k))
+            continue;
+        const double err = ctx->scal_h[k].err;
+        ctx->rhs_err[k].assign(1, err);
+        ctx->rhs_iter[k] = 0;
+        if (!std::isfinite(err))
+            return fail(ctx, FANSGPU_ENAN, "RHS %d: non-finite initial residual norm", k);
+        last_true[k] = err;
+        err_rel[k]   = ctx->tol.type == FANSGPU_ABSOLUTE ? err : 100.0; // solver.h:432-451 at iteration 0
+        on[k]        = ctx->tol.n_it > 0 && err_rel[k] > ctx->tol.tolerance;
+        if (on[k]) {
+            ctx->rhs_uzero[k] = 0; // u_k is updated from here on
+            ++n_on;
+        }
+        ctx->act_h[k] = on[k];
+    }
+    const bool graphs = ctx->use_graphs && !ctx->timing;
+    if (graphs && ctx->hist_cap < ctx->tol.n_it + 2) {
+        if (ctx->hist)
+            cudaFree(ctx->hist);
+        ctx->hist = nullptr;
+        if ((rc = dalloc(ctx, &ctx->hist, ((size_t)ctx->tol.n_it + 2) * kMaxRhs)))
+            return rc;
+        ctx->hist_cap     = ctx->tol.n_it + 2;
+        ctx->graphs_valid = false; // the graphs hold the history pointer
+    }
+    int it = 0; // iterations of the active right-hand sides (they advance together)
+    while (n_on > 0 && it < ctx->tol.n_it) {
+        FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->act, ctx->act_h, sizeof(int) * R, cudaMemcpyHostToDevice, ctx->st));
+        int done = 1;
+        if (graphs && it > 0 && (!ctx->graphs_valid || !ctx->graphs_multi) && (rc = build_loop_graphs(ctx, true)))
+            return rc;
+        if (graphs && it > 0 && !ctx->loop_on_device) {
+            FANS_CUDA_CHECK(cudaGraphLaunch(ctx->iter_exec[ctx->cur_d], ctx->st));
+            if ((rc = sync_scalars_rhs(ctx)))
+                return rc;
+        } else if (graphs && it > 0) {
+            LoopCtlR &c = *ctx->ctlr_h;
+            for (int k = 0; k < kMaxRhs; ++k) {
+                c.err0[k]      = k < R ? ctx->rhs_err[k][0] : 1.0;
+                c.last_true[k] = k < R ? last_true[k] : 0.0;
+            }
+            c.tol      = ctx->tol.tolerance;
+            c.reliable = ctx->reliable_delta;
+            c.iter     = it;
+            c.n_it     = ctx->tol.n_it;
+            c.relative = ctx->tol.type == FANSGPU_RELATIVE;
+            c.cap      = ctx->hist_cap;
+            c.nrhs     = R;
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->ctlr, ctx->ctlr_h, sizeof(LoopCtlR), cudaMemcpyHostToDevice, ctx->st));
+            FANS_CUDA_CHECK(cudaGraphLaunch(ctx->graph_exec[ctx->cur_d], ctx->st));
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->ctlr_h, ctx->ctlr, sizeof(LoopCtlR), cudaMemcpyDeviceToHost, ctx->st));
+            if ((rc = sync_scalars_rhs(ctx)))
+                return rc;
+            done = c.iter - it;
+            if (done < 1 || it + done > ctx->tol.n_it)
+                return fail(ctx, FANSGPU_ECUDA, "inner-loop graph ran %d iterations from %d", done, it);
+            if (done > 1) { // iterations the loop did not halt on only extend the histories
+                std::vector<double> h(done - 1);
+                for (int k = 0; k < R; ++k) {
+                    if (!on[k])
+                        continue;
+                    FANS_CUDA_CHECK(cudaMemcpyAsync(h.data(), ctx->hist + (size_t)k * ctx->hist_cap + it + 1,
+                                                    sizeof(double) * (done - 1), cudaMemcpyDeviceToHost, ctx->st));
+                    FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
+                    ctx->rhs_err[k].insert(ctx->rhs_err[k].end(), h.begin(), h.end());
+                }
+            }
+        } else {
+            FANS_CUDA_CHECK(enqueue_mixed_iteration_rhs(ctx, ctx->cur_d));
+            if ((rc = sync_scalars_rhs(ctx)))
+                return rc;
+        }
+        ctx->cur_d ^= done & 1;
+        it += done;
+        std::vector<int> due;
+        for (int k = 0; k < R; ++k) {
+            if (!on[k])
+                continue;
+            ctx->rhs_iter[k] = it;
+            const CgScalars &sc = ctx->scal_h[k];
+            if (sc.converged == -3)
+                return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out at iteration %d",
+                            it);
+            if (sc.converged < 0)
+                return fail(ctx, FANSGPU_ENAN, "RHS %d: non-finite residual norm at iteration %d", k, it);
+            const double est     = sc.err;
+            const double est_rel = ctx->tol.type == FANSGPU_ABSOLUTE ? est : est / ctx->rhs_err[k][0];
+            if (est_rel <= ctx->tol.tolerance || est <= ctx->reliable_delta * last_true[k])
+                due.push_back(k);
+            else
+                ctx->rhs_err[k].push_back(est);
+        }
+        // reliable updates of the RHS that asked for one; the others go on from their estimates
+        for (int k : due)
+            if ((rc = refresh_rhs(ctx, k, true, false)))
+                return rc;
+        if (!due.empty() && (rc = sync_scalars_rhs(ctx)))
+            return rc;
+        for (int k : due) {
+            ctx->rhs_ref[k]++;
+            last_true[k]     = ctx->scal_h[k].err;
+            ctx->rhs_err[k].push_back(last_true[k]);
+            const double rel = ctx->tol.type == FANSGPU_ABSOLUTE ? last_true[k] : last_true[k] / ctx->rhs_err[k][0];
+            if (!(rel > ctx->tol.tolerance)) { // converged (the true residual); NaN was caught by the norm
+                on[k]         = 0;
+                ctx->act_h[k] = 0;
+                --n_on;
+            }
+        }
+    }
+    // corrections since the last reliable update (n_it reached) belong to u too
+    FANS_CUDA_CHECK(launch_fold(ctx->u0, ctx->e32, n * R, ctx->st));
+    for (int k = 0; k < R; ++k)
+        if (mine(k) && ctx->rhs_iter[k] > 0)
+            ctx->rhs_uzero[k] = 0;
+    load_rhs(ctx, home);
     return 0;
 }
 
@@ -1421,11 +1788,18 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     for (int i = 0; i < 3; ++i)
         if (!(desc->L[i] > 0))
             return fail(nullptr, FANSGPU_EINVAL, "L must be positive");
+    const int nrhs = desc->n_rhs == 0 ? 1 : desc->n_rhs;
+    if (nrhs < 1 || nrhs > FANSGPU_MAX_RHS)
+        return fail(nullptr, FANSGPU_EINVAL, "n_rhs = %d: 1..%d right-hand sides", desc->n_rhs, FANSGPU_MAX_RHS);
+    if (nrhs > 1 && desc->method == FANSGPU_NEWTON)
+        return fail(nullptr, FANSGPU_EUNSUPPORTED, "Newton-Krylov solves one right-hand side (n_rhs = 1)");
 
     fansgpu_ctx *ctx = new fansgpu_ctx();
     ctx->desc        = *desc;
-    if (const char *ev = std::getenv("FANSGPU_STENCIL"))
+    if (const char *ev = std::getenv("FANSGPU_STENCIL")) { // "simt": CUDA-core operator; "tc": per-phase 3xTF32
         ctx->tc_allowed = std::strcmp(ev, "simt") != 0;
+        ctx->tc_legacy  = std::strcmp(ev, "tc") == 0;
+    }
     if (const char *ev = std::getenv("FANSGPU_TUNE")) { // "0": default tiles; "all": + operator; "zyx": forced
         if (std::strcmp(ev, "0") == 0)
             ctx->tune = 0;
@@ -1457,6 +1831,12 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
             ctx->Bbar[i] += ctx->B[gp * ns * NC + i] / ctx->ngp;
     ctx->g0.assign(ns, 0.0);
     ctx->kapparef.assign(ns * ns, 0.0);
+    ctx->nrhs = nrhs;
+    ctx->rhs_g0.assign(nrhs, std::vector<double>(ns, 0.0));
+    ctx->rhs_err.assign(nrhs, {});
+    ctx->rhs_iter.assign(nrhs, 0);
+    ctx->rhs_ref.assign(nrhs, 0);
+    ctx->rhs_uzero.assign(nrhs, 1);
 
     int rc = 0;
     auto bail = [&](int code) {
@@ -1474,33 +1854,42 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
     const long long F = (long long)ctx->g.nx * ctx->g.ny * nzh;
     const long long nspec = (long long)ctx->C * ctx->g.nx * ctx->g.ny * nzp;
     const bool      mixed = desc->precision == FANSGPU_MIXED;
-    if ((rc = dalloc(ctx, &ctx->d_ms, N)) || (rc = dalloc(ctx, &ctx->u, nn)) || (rc = dalloc(ctx, &ctx->r, nn)) ||
+    const long long nr = (long long)nrhs * nn; // per-RHS fields
+    if ((rc = dalloc(ctx, &ctx->d_ms, N)) || (rc = dalloc(ctx, &ctx->u0, nr)) || (rc = dalloc(ctx, &ctx->r0, nr)) ||
         (rc = dalloc(ctx, &ctx->s, nn)) || (rc = dalloc(ctx, &ctx->dd[0], nn)) ||
         (rc = dalloc(ctx, &ctx->dd[1], nn)) || (rc = dalloc(ctx, &ctx->Kd, nn)) ||
-        (rc = dalloc(ctx, &ctx->uprev, nn)) || (rc = dalloc(ctx, &ctx->spec64, nspec)) ||
+        (rc = dalloc(ctx, &ctx->up0, nr)) || (rc = dalloc(ctx, &ctx->spec64, nspec)) ||
         (rc = dalloc(ctx, &ctx->G64, F * NT)) || (rc = dalloc(ctx, &ctx->staging, N * std::max(ctx->C, ns))) ||
-        (rc = dalloc(ctx, &ctx->scal, 1)) || (rc = dalloc(ctx, &ctx->red.partials, (size_t)max_reduction_blocks(ctx->g, ctx->C) * kMaxRed)) ||
+        (rc = dalloc(ctx, &ctx->scal, kMaxRhs)) || (rc = dalloc(ctx, &ctx->act, kMaxRhs)) ||
+        (rc = dalloc(ctx, &ctx->ctlr, 1)) ||
+        (rc = dalloc(ctx, &ctx->red.partials, (size_t)max_reduction_blocks(ctx->g, ctx->C) * kMaxRed)) ||
         (rc = dalloc(ctx, &ctx->red.counter, kRedSites)) || (rc = dalloc(ctx, &ctx->red_out, 64)) ||
         (rc = dalloc(ctx, &ctx->K0c, NC * NC)) || (rc = dalloc(ctx, &ctx->Bbar_d, ns * NC)) ||
         (rc = dalloc(ctx, &ctx->Bgp_d, (size_t)ctx->ngp * ns * NC)) ||
         (rc = dalloc(ctx, &ctx->g0_d, ns)) || (rc = dalloc(ctx, &ctx->max_id, 1)) ||
         (rc = dalloc(ctx, &ctx->trig, 2 * (ctx->g.nx + ctx->g.ny + nzh))))
         return bail(rc);
+    ctx->u     = ctx->u0;
+    ctx->r     = ctx->r0;
+    ctx->uprev = ctx->up0;
     if (mixed) {
-        if ((rc = dalloc(ctx, &ctx->r32, nn)) || (rc = dalloc(ctx, &ctx->s32, nn)) ||
-            (rc = dalloc(ctx, &ctx->d32[0], nn)) || (rc = dalloc(ctx, &ctx->d32[1], nn)) ||
-            (rc = dalloc(ctx, &ctx->Kd32, nn)) || (rc = dalloc(ctx, &ctx->e32, nn)) || (rc = dalloc(ctx, &ctx->spec32, nspec)) ||
-            (rc = dalloc(ctx, &ctx->G32, F * NT)))
+        if ((rc = dalloc(ctx, &ctx->r32, nr)) || (rc = dalloc(ctx, &ctx->s32, nr)) ||
+            (rc = dalloc(ctx, &ctx->d32[0], nr)) || (rc = dalloc(ctx, &ctx->d32[1], nr)) ||
+            (rc = dalloc(ctx, &ctx->Kd32, nr)) || (rc = dalloc(ctx, &ctx->e32, nr)) ||
+            (rc = dalloc(ctx, &ctx->spec32, nspec * nrhs)) || (rc = dalloc(ctx, &ctx->G32, F * NT)))
             return bail(rc);
     }
-    if (cudaMallocHost((void **)&ctx->scal_h, sizeof(CgScalars)) != cudaSuccess) {
+    if (cudaMallocHost((void **)&ctx->scal_h, sizeof(CgScalars) * kMaxRhs) != cudaSuccess ||
+        cudaMallocHost((void **)&ctx->act_h, sizeof(int) * kMaxRhs) != cudaSuccess ||
+        cudaMallocHost((void **)&ctx->ctlr_h, sizeof(LoopCtlR)) != cudaSuccess) {
         fail(ctx, FANSGPU_ENOMEM, "pinned host allocation failed");
         return bail(FANSGPU_ENOMEM);
     }
     cudaMemsetAsync(ctx->red.counter, 0, sizeof(unsigned) * kRedSites, ctx->st);
-    cudaMemsetAsync(ctx->u, 0, sizeof(double) * nn, ctx->st);
-    cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * nn, ctx->st);
-    cudaMemsetAsync(ctx->r, 0, sizeof(double) * nn, ctx->st);
+    cudaMemsetAsync(ctx->u0, 0, sizeof(double) * nr, ctx->st);
+    cudaMemsetAsync(ctx->up0, 0, sizeof(double) * nr, ctx->st);
+    cudaMemsetAsync(ctx->r0, 0, sizeof(double) * nr, ctx->st);
+    cudaMemsetAsync(ctx->scal, 0, sizeof(CgScalars) * kMaxRhs, ctx->st);
     cudaMemcpyAsync(ctx->Bbar_d, ctx->Bbar.data(), sizeof(double) * ns * NC, cudaMemcpyHostToDevice, ctx->st);
     cudaMemcpyAsync(ctx->Bgp_d, ctx->B.data(), sizeof(double) * ctx->B.size(), cudaMemcpyHostToDevice, ctx->st);
     if (ctx->C == 3 && (desc->fe_type == FANSGPU_HEX8 || desc->fe_type == FANSGPU_HEX8R)) {
@@ -1558,8 +1947,8 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
         return 0;
     if (ctx->st)
         cudaStreamSynchronize(ctx->st);
-    void *ptrs[] = {ctx->d_ms, ctx->u,    ctx->r,      ctx->s,      ctx->dd[0],  ctx->dd[1],      ctx->Kd,
-                    ctx->uprev, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
+    void *ptrs[] = {ctx->d_ms, ctx->u0,   ctx->r0,     ctx->s,      ctx->dd[0],  ctx->dd[1],      ctx->Kd,
+                    ctx->up0,  ctx->act,  ctx->ctlr,   ctx->Wtb,    ctx->coef_tb, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d, ctx->Bb_d,
@@ -1570,6 +1959,10 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
             cudaFree(p);
     if (ctx->scal_h)
         cudaFreeHost(ctx->scal_h);
+    if (ctx->act_h)
+        cudaFreeHost(ctx->act_h);
+    if (ctx->ctlr_h)
+        cudaFreeHost(ctx->ctlr_h);
     if (ctx->ctl_h)
         cudaFreeHost(ctx->ctl_h);
     if (ctx->ev0)
@@ -1616,9 +2009,16 @@ int fansgpu_reset(fansgpu_ctx *ctx)
 {
     if (!ctx)
         return FANSGPU_EINVAL;
-    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->u, 0, sizeof(double) * ctx->n, ctx->st));
-    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->uprev, 0, sizeof(double) * ctx->n, ctx->st));
-    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->r, 0, sizeof(double) * ctx->n, ctx->st));
+    const size_t nr = sizeof(double) * ctx->n * ctx->nrhs; // every right-hand side
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->u0, 0, nr, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->up0, 0, nr, ctx->st));
+    FANS_CUDA_CHECK(cudaMemsetAsync(ctx->r0, 0, nr, ctx->st));
+    for (int k = 0; k < ctx->nrhs; ++k) {
+        ctx->rhs_err[k].clear();
+        ctx->rhs_iter[k]  = 0;
+        ctx->rhs_ref[k]   = 0;
+        ctx->rhs_uzero[k] = 1;
+    }
     if (ctx->ep_t) {
         const long long nep = 6LL * ctx->ngp * ctx->N, nq = (long long)ctx->ngp * ctx->N;
         FANS_CUDA_CHECK(cudaMemsetAsync(ctx->ep_t, 0, sizeof(double) * nep, ctx->st));
@@ -1666,7 +2066,8 @@ int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out)
         return rc;
     const ConvPlan<double> &a = ctx->cp64;
     const ConvPlan<float>  &b = ctx->cp32;
-    const int32_t v[7] = {a.var_z, a.var_y, a.var_x, b.var_z, b.var_y, b.var_x, ctx->use_tc ? 1 : 0};
+    const int32_t v[7] = {a.var_z, a.var_y, a.var_x, b.var_z, b.var_y, b.var_x,
+                         ctx->use_tcb ? 2 : ctx->use_tc ? 1 : 0};
     for (int k = 0; k < 7; ++k)
         out[k] = v[k];
     return 0;
@@ -1796,6 +2197,55 @@ int fansgpu_set_gradient(fansgpu_ctx *ctx, const double *g0)
             return fail(ctx, FANSGPU_EINVAL, "non-finite macroscale loading component %d", i);
     ctx->g0.assign(g0, g0 + ctx->nstr);
     ctx->force_dirty = true;
+    return 0;
+}
+
+int fansgpu_set_gradients(fansgpu_ctx *ctx, int32_t n, const double *g0)
+{
+    if (!ctx || !g0)
+        return ctx ? fail(ctx, FANSGPU_EINVAL, "null gradients") : FANSGPU_EINVAL;
+    if (n != ctx->nrhs)
+        return fail(ctx, FANSGPU_EINVAL, "set_gradients: %d gradients for %d right-hand sides", n, ctx->nrhs);
+    for (int i = 0; i < n * ctx->nstr; ++i)
+        if (!std::isfinite(g0[i]))
+            return fail(ctx, FANSGPU_EINVAL, "non-finite macroscale loading component %d of RHS %d", i % ctx->nstr,
+                        i / ctx->nstr);
+    store_rhs(ctx);
+    for (int k = 0; k < n; ++k)
+        ctx->rhs_g0[k].assign(g0 + (size_t)k * ctx->nstr, g0 + (size_t)(k + 1) * ctx->nstr);
+    load_rhs(ctx, ctx->cur);
+    return 0;
+}
+
+int fansgpu_select_rhs(fansgpu_ctx *ctx, int32_t k)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    if (k < 0 || k >= ctx->nrhs)
+        return fail(ctx, FANSGPU_EINVAL, "select_rhs: %d outside 0..%d", k, ctx->nrhs - 1);
+    store_rhs(ctx);
+    load_rhs(ctx, k);
+    return 0;
+}
+
+int fansgpu_rhs_stats(fansgpu_ctx *ctx, int32_t k, fansgpu_stats *st)
+{
+    if (!ctx || !st)
+        return FANSGPU_EINVAL;
+    if (k < 0 || k >= ctx->nrhs)
+        return fail(ctx, FANSGPU_EINVAL, "rhs_stats: %d outside 0..%d", k, ctx->nrhs - 1);
+    store_rhs(ctx);
+    const std::vector<double> &e = ctx->rhs_err[k];
+    if (e.empty())
+        return fail(ctx, FANSGPU_ESTATE, "rhs_stats: RHS %d has not been solved", k);
+    const double err  = e.back();
+    const double rel  = ctx->tol.type == FANSGPU_ABSOLUTE ? err : (ctx->rhs_iter[k] == 0 ? 100.0 : err / e[0]);
+    st->iterations    = ctx->rhs_iter[k];
+    st->converged     = rel <= ctx->tol.tolerance ? 1 : 0;
+    st->err0          = e[0];
+    st->err           = err;
+    st->refinements   = ctx->rhs_ref[k];
+    st->solve_ms      = ctx->rhs_ms;
     return 0;
 }
 
@@ -2304,23 +2754,23 @@ int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *t)
     return 0;
 }
 
-int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
+// Solver::solve of the selected right-hand side (solver.h:283-300).
+int solve_one(fansgpu_ctx *ctx, int *refinements)
 {
-    if (!ctx)
-        return FANSGPU_EINVAL;
-    int rc = setup(ctx);
-    if (rc)
-        return rc;
-    FANS_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->st));
-    int refinements = 0;
+    int rc;
+    *refinements = 0;
     if (ctx->desc.method == FANSGPU_FP)
         rc = solve_fp64(ctx);
     else if (ctx->desc.method == FANSGPU_NEWTON)
-        rc = solve_newton(ctx, &refinements);
+        rc = solve_newton(ctx, refinements);
     else if (!ctx->all_linear || ctx->mixed_active)
         rc = solve_cg_nl(ctx); // nonlinear laws and mixed BCs run the FP64 line-search path (solverCG.h:96)
-    else if (ctx->desc.precision == FANSGPU_MIXED && !ctx->vscale)
-        rc = solve_cg_mixed(ctx, &refinements);
+    else if (ctx->desc.precision == FANSGPU_MIXED && !ctx->vscale && multi_rhs_path(ctx)) {
+        rc = solve_cg_mixed_rhs(ctx, ctx->cur);
+        if (!rc)
+            *refinements = ctx->rhs_ref[ctx->cur];
+    } else if (ctx->desc.precision == FANSGPU_MIXED && !ctx->vscale)
+        rc = solve_cg_mixed(ctx, refinements);
     else
         rc = solve_cg64(ctx);
     if (rc)
@@ -2329,19 +2779,71 @@ int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
     if ((rc = commit_ivars(ctx)))
         return rc;
     ctx->u_zero = ctx->u_zero && ctx->iter == 0;
+    ctx->rhs_ref[ctx->cur] = *refinements;
+    store_rhs(ctx);
+    return 0;
+}
+
+int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats)
+{
+    if (!ctx)
+        return FANSGPU_EINVAL;
+    int rc = setup(ctx);
+    if (rc)
+        return rc;
+    const int R = ctx->nrhs;
+    if (R > 1 && (!ctx->all_linear || ctx->mixed_active))
+        return fail(ctx, FANSGPU_EUNSUPPORTED,
+                    "several right-hand sides need linear laws under strain control (internal variables and mixed "
+                    "boundary conditions belong to one load path)");
+    FANS_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->st));
+    int refinements = 0;
+    if (R == 1) {
+        rc = solve_one(ctx, &refinements);
+    } else if (multi_rhs_path(ctx)) {
+        rc = solve_cg_mixed_rhs(ctx, -1); // every RHS in each kernel
+    } else {
+        const int home = ctx->cur; // one after another
+        for (int k = 0; k < R && !rc; ++k) {
+            store_rhs(ctx);
+            load_rhs(ctx, k);
+            int rf = 0;
+            rc     = solve_one(ctx, &rf);
+        }
+        store_rhs(ctx);
+        load_rhs(ctx, home);
+    }
+    if (rc)
+        return rc;
     FANS_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->st));
     FANS_CUDA_CHECK(cudaEventSynchronize(ctx->ev1));
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    const double err     = ctx->err_all.back();
-    const double err_rel = err_value(ctx, err);
-    const bool   conv    = err_rel <= ctx->tol.tolerance;
+    ctx->rhs_ms = ms;
+    // aggregate over the right-hand sides: the worst relative error, all converged
+    store_rhs(ctx);
+    bool   conv = true;
+    int    iters = 0, refs = 0, worst = 0;
+    double worst_rel = -1.0;
+    for (int k = 0; k < R; ++k) {
+        const std::vector<double> &e = ctx->rhs_err[k];
+        if (e.empty())
+            return fail(ctx, FANSGPU_ECUDA, "RHS %d: no error history after the solve", k);
+        const double rel = ctx->tol.type == FANSGPU_ABSOLUTE ? e.back() : (ctx->rhs_iter[k] == 0 ? 100.0 : e.back() / e[0]);
+        conv             = conv && rel <= ctx->tol.tolerance;
+        iters            = std::max(iters, ctx->rhs_iter[k]);
+        refs += ctx->rhs_ref[k];
+        if (!(rel <= worst_rel)) {
+            worst_rel = rel;
+            worst     = k;
+        }
+    }
     if (stats) {
-        stats->iterations  = ctx->iter;
+        stats->iterations  = iters;
         stats->converged   = conv ? 1 : 0;
-        stats->err0        = ctx->err_all[0];
-        stats->err         = err;
-        stats->refinements = refinements;
+        stats->err0        = ctx->rhs_err[worst][0];
+        stats->err         = ctx->rhs_err[worst].back();
+        stats->refinements = refs;
         stats->solve_ms    = ms;
     }
     return conv ? 0 : FANSGPU_ENOTCONV;
@@ -2462,8 +2964,8 @@ int fansgpu_homogenized_tangent(fansgpu_ctx *ctx, double pert, double *out)
         if ((rc = fansgpu_set_gradient(ctx, g.data())))
             return rc;
         ctx->mixed_active = false; // solver.h:769
-        rc                = fansgpu_solve(ctx, nullptr);
-        if (rc && rc != FANSGPU_ENOTCONV)
+        int rf            = 0;
+        if ((rc = solve_one(ctx, &rf))) // the selected right-hand side only
             return rc;
         if ((rc = fansgpu_homogenized_stress(ctx, sig.data())))
             return rc;
@@ -2613,8 +3115,11 @@ int fansgpu_extrapolate_displacement(fansgpu_ctx *ctx)
 {
     if (!ctx)
         return FANSGPU_EINVAL;
-    FANS_CUDA_CHECK(launch_extrapolate(ctx->u, ctx->uprev, ctx->n, ctx->st));
+    // every right-hand side (their slices are contiguous)
+    FANS_CUDA_CHECK(launch_extrapolate(ctx->u0, ctx->up0, ctx->n * ctx->nrhs, ctx->st));
     ctx->u_zero = false;
+    for (int k = 0; k < ctx->nrhs; ++k)
+        ctx->rhs_uzero[k] = 0;
     FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st));
     return 0;
 }

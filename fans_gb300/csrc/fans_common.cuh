@@ -56,6 +56,7 @@ struct GridRed {
     unsigned int *counter;  // one counter per reduction site
 };
 constexpr int kMaxRed = 20; // large-strain averages reduce 2*9+1 values
+constexpr int kMaxRhs = 6;  // right-hand sides of one multi-RHS solve (the 6 Mandel load cases)
 
 // The device's opt-in maximum of shared memory per block (static + dynamic).
 inline int smem_optin_max()
@@ -165,6 +166,28 @@ __device__ __forceinline__ void grid_final(double (&v)[NV], const int (&ops)[NV]
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             double t = __ldcg(&partials[(size_t)b * kMaxRed + k]);
+            v[k]     = ops[k] == RED_MAX ? nan_max(v[k], t) : v[k] + t;
+        }
+    block_reduce<NV>(v, ops, smem);
+}
+
+// Deterministic final sum over the partials of blocks [b0, b0 + count) (called
+// by every thread of the last block; result valid in thread 0): the per-RHS
+// sums of a grid whose blockIdx.y is the right-hand side.  With b0 = 0 and
+// count = all blocks it is grid_final.
+template <int NV>
+__device__ __forceinline__ void grid_final_range(double (&v)[NV], const int (&ops)[NV], const double *partials,
+                                                 int b0, int count, double *smem)
+{
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        v[k] = 0.0;
+    const int per = (count + blockDim.x - 1) / blockDim.x;
+    const int s0 = threadIdx.x * per, s1 = min(count, s0 + per);
+    for (int b = s0; b < s1; ++b)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = __ldcg(&partials[(size_t)(b0 + b) * kMaxRed + k]);
             v[k]     = ops[k] == RED_MAX ? nan_max(v[k], t) : v[k] + t;
         }
     block_reduce<NV>(v, ops, smem);

@@ -32,7 +32,9 @@ __global__ void __launch_bounds__(KC * N1) k_y_reg(ConvPlan<T> p)
     constexpr int n = N1 * N2;
     __shared__ cplx<T> S[n * KC];
     const int t = threadIdx.x, l = t % KC, w = t / KC;
-    const int kz0 = blockIdx.x * KC, x = blockIdx.y, comp = blockIdx.z;
+    const int kz0 = blockIdx.x * KC, x = blockIdx.y, comp = blockIdx.z; // comp = rhs * C + c
+    if (p.active && !p.active[comp / p.C])
+        return;
     const bool valid = l < p.nzh - kz0;
     cplx<T> *base = p.spec + ((long long)comp * p.g.nx + x) * (long long)p.g.ny * p.nzp + kz0 + l;
     cplx<T>  v[N2];
@@ -101,82 +103,90 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
 
-    // forward FFT along x
-    cplx<T> v[N2];
-#pragma unroll
-    for (int j2 = 0; j2 < N2; ++j2)
-        v[j2] = valid ? gbase[(w + N1 * j2) * xstride] : cplx<T>{0, 0};
-    line_phase1<T, N1, N2, false>(v, w, p.tw_x);
-#pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2)
-        Fc[(k2 * N1 + w) * KC + l] = v[k2];
-    __syncthreads();
-    cplx<T> u[N1];
-    if (w < N2)
-#pragma unroll
-        for (int j1 = 0; j1 < N1; ++j1)
-            u[j1] = Fc[(w * N1 + j1) * KC + l];
-    __syncthreads();
-    if (w < N2) {
-        Dft<T, N1, false>::run(u);
-#pragma unroll
-        for (int k1 = 0; k1 < N1; ++k1)
-            Fc[(w + N2 * k1) * KC + l] = u[k1];
-    }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncthreads();
-
-    // Green's operator: C x C real symmetric per frequency (solver.h:400-406)
-    for (int i = t; i < n * KC; i += blockDim.x) {
-        const int kx = i / KC, ll = i % KC;
-        if (ll >= nk)
+    // the same Green's slice serves every right-hand side: RHS k's spectrum follows RHS k-1's
+    const long long rhs_spec = (long long)p.C * nx * ny * p.nzp;
+    for (int k = 0; k < p.nrhs; ++k) {
+        if (p.active && !p.active[k])
             continue;
-        const T *g = Gs + ((size_t)kx * KC + ll) * NT;
-        T        gm[NT];
+        cplx<T> *gb = gbase + k * rhs_spec;
+        // forward FFT along x
+        cplx<T> v[N2];
 #pragma unroll
-        for (int q = 0; q < NT; ++q)
-            gm[q] = g[q];
-        cplx<T> a[C], o[C];
+        for (int j2 = 0; j2 < N2; ++j2)
+            v[j2] = valid ? gb[(w + N1 * j2) * xstride] : cplx<T>{0, 0};
+        line_phase1<T, N1, N2, false>(v, w, p.tw_x);
 #pragma unroll
-        for (int c = 0; c < C; ++c)
-            a[c] = F[((size_t)c * n + kx) * KC + ll];
+        for (int k2 = 0; k2 < N2; ++k2)
+            Fc[(k2 * N1 + w) * KC + l] = v[k2];
+        __syncthreads();
+        cplx<T> u[N1];
+        if (w < N2)
 #pragma unroll
-        for (int r = 0; r < C; ++r) {
-            cplx<T> acc = {0, 0};
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                const int ia = r > c ? r : c, ib = r > c ? c : r;
-                const T   gv = gm[ia * (ia + 1) / 2 + ib];
-                acc.x += gv * a[c].x;
-                acc.y += gv * a[c].y;
-            }
-            o[r] = acc;
-        }
-#pragma unroll
-        for (int c = 0; c < C; ++c)
-            F[((size_t)c * n + kx) * KC + ll] = o[c];
-    }
-    __syncthreads();
-
-    // inverse FFT along x
-#pragma unroll
-    for (int j2 = 0; j2 < N2; ++j2)
-        v[j2] = Fc[(w + N1 * j2) * KC + l];
-    __syncthreads();
-    line_phase1<T, N1, N2, true>(v, w, p.tw_x);
-#pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2)
-        Fc[(k2 * N1 + w) * KC + l] = v[k2];
-    __syncthreads();
-    if (w < N2) {
-#pragma unroll
-        for (int j1 = 0; j1 < N1; ++j1)
-            u[j1] = Fc[(w * N1 + j1) * KC + l];
-        Dft<T, N1, true>::run(u);
-        if (valid)
+            for (int j1 = 0; j1 < N1; ++j1)
+                u[j1] = Fc[(w * N1 + j1) * KC + l];
+        __syncthreads();
+        if (w < N2) {
+            Dft<T, N1, false>::run(u);
 #pragma unroll
             for (int k1 = 0; k1 < N1; ++k1)
-                gbase[(w + N2 * k1) * xstride] = u[k1];
+                Fc[(w + N2 * k1) * KC + l] = u[k1];
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+
+        // Green's operator: C x C real symmetric per frequency (solver.h:400-406)
+        for (int i = t; i < n * KC; i += blockDim.x) {
+            const int kx = i / KC, ll = i % KC;
+            if (ll >= nk)
+                continue;
+            const T *g = Gs + ((size_t)kx * KC + ll) * NT;
+            T        gm[NT];
+#pragma unroll
+            for (int q = 0; q < NT; ++q)
+                gm[q] = g[q];
+            cplx<T> a[C], o[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                a[c] = F[((size_t)c * n + kx) * KC + ll];
+#pragma unroll
+            for (int r = 0; r < C; ++r) {
+                cplx<T> acc = {0, 0};
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const int ia = r > c ? r : c, ib = r > c ? c : r;
+                    const T   gv = gm[ia * (ia + 1) / 2 + ib];
+                    acc.x += gv * a[c].x;
+                    acc.y += gv * a[c].y;
+                }
+                o[r] = acc;
+            }
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                F[((size_t)c * n + kx) * KC + ll] = o[c];
+        }
+        __syncthreads();
+
+        // inverse FFT along x
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2)
+            v[j2] = Fc[(w + N1 * j2) * KC + l];
+        __syncthreads();
+        line_phase1<T, N1, N2, true>(v, w, p.tw_x);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2)
+            Fc[(k2 * N1 + w) * KC + l] = v[k2];
+        __syncthreads();
+        if (w < N2) {
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1)
+                u[j1] = Fc[(w * N1 + j1) * KC + l];
+            Dft<T, N1, true>::run(u);
+            if (valid)
+#pragma unroll
+                for (int k1 = 0; k1 < N1; ++k1)
+                    gb[(w + N2 * k1) * xstride] = u[k1];
+        }
+        __syncthreads(); // F is reused by the next right-hand side
     }
 }
 
@@ -190,9 +200,19 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
     __shared__ cplx<T> E[R * N2 * EP];
     __shared__ cplx<T> Z[R * M];
     const int       t = threadIdx.x, L = t / N1, w = t % N1;
-    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
-    const long long row   = (long long)blockIdx.x * R + L;
-    const bool      valid = row < nrows;
+    const long long rpr   = (long long)p.C * p.g.nx * p.g.ny; // rows per right-hand side
+    const long long nrows = rpr * p.nrhs;
+    const long long row0b = (long long)blockIdx.x * R;
+    if (p.active) { // return when every row of this block belongs to an inactive right-hand side
+        const long long last = min(row0b + R, nrows) - 1;
+        bool            any  = false;
+        for (long long q = row0b / rpr; q <= last / rpr; ++q)
+            any = any || p.active[q];
+        if (!any)
+            return;
+    }
+    const long long row   = row0b + L;
+    const bool      valid = row < nrows && (!p.active || p.active[row / rpr]);
     const cplx<T>  *rin   = reinterpret_cast<const cplx<T> *>(r) + row * M;
     cplx<T>         v[N2];
 #pragma unroll
@@ -218,7 +238,7 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
     const long long row0 = (long long)blockIdx.x * R;
     for (int i = t; i < R * (M + 1); i += blockDim.x) {
         const int Lr = i / (M + 1), k = i % (M + 1);
-        if (row0 + Lr >= nrows)
+        if (row0 + Lr >= nrows || (p.active && !p.active[(row0 + Lr) / rpr]))
             continue;
         cplx<T> zk = Z[Lr * M + (k == M ? 0 : k)];
         cplx<T> zm = Z[Lr * M + (k == 0 ? 0 : M - k)];
@@ -245,12 +265,23 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
     cplx<T>          *Xb = reinterpret_cast<cplx<T> *>(zsm); // [2][XS]
     cplx<T>          *Rb = Xb + 2 * XS;                      // [2][R*M] r rows
     cplx<T>          *Zp = Rb + 2 * R * M;                   // [R*M] packed half-length rows
-    __shared__ double red_smem[32];
+    __shared__ double red_smem[32 * kMaxRhs];
     const int       t = threadIdx.x, L = t / N1, w = t % N1;
-    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    const long long rpr   = (long long)p.C * p.g.nx * p.g.ny; // rows per right-hand side
+    const long long nrows = rpr * p.nrhs;
     const long long nblk  = (nrows + R - 1) / R;
+    // a block of rows is skipped when all its rows belong to inactive right-hand sides
+    auto live = [&](long long blk) {
+        if (!p.active)
+            return true;
+        const long long last = min(blk * R + R, nrows) - 1;
+        bool            any  = false;
+        for (long long q = blk * R / rpr; q <= last / rpr; ++q)
+            any = any || p.active[q];
+        return any;
+    };
     auto fetch = [&](long long blk, int b) {
-        if (blk < nblk) {
+        if (blk < nblk && live(blk)) {
             const long long row0 = blk * R;
             const int       nval = (int)(nrows - row0 < R ? nrows - row0 : R);
             cplx<T>        *X    = Xb + b * XS;
@@ -277,7 +308,10 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    T dot = (T)0;
+    T dotk[kMaxRhs]; // <r, s> per right-hand side, this thread's rows
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q)
+        dotk[q] = (T)0;
     fetch(blockIdx.x, 0);
     int it = 0;
     for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++it) {
@@ -285,6 +319,8 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
         fetch(blk + gridDim.x, b ^ 1);                       // the next block, into the other buffer
         asm volatile("cp.async.wait_group 1;" ::: "memory"); // this block's copies (this thread's) ...
         __syncthreads();                                     // ... and everyone else's
+        if (!live(blk))
+            continue; // uniform across the CTA: nothing was fetched for it
         cplx<T>        *X    = Xb + b * XS;
         const long long row0 = blk * R;
         for (int i = t; i < R * M; i += blockDim.x) {
@@ -312,7 +348,8 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
             E[(L * N2 + k2) * EP + w] = v[k2];
         __syncthreads();
         const long long row = row0 + L;
-        if (row < nrows && w < N2) {
+        const int       rk  = (int)(row / rpr);
+        if (row < nrows && w < N2 && (!p.active || p.active[rk])) {
             cplx<T> u[N1];
 #pragma unroll
             for (int j1 = 0; j1 < N1; ++j1)
@@ -321,6 +358,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
             cplx<T>       *sout = reinterpret_cast<cplx<T> *>(a.s) + row * M;
             const cplx<T> *rr   = Rb + b * R * M + L * M;
             const T        sg   = (T)a.sign;
+            T              dot  = (T)0;
 #pragma unroll
             for (int k1 = 0; k1 < N1; ++k1) {
                 const int m = w + N2 * k1;
@@ -331,23 +369,35 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
                     dot += rv.x * z.x + rv.y * z.y;
                 }
             }
+#pragma unroll
+            for (int q = 0; q < kMaxRhs; ++q)
+                if (q == rk)
+                    dotk[q] += dot;
         }
         __syncthreads(); // buffers b and Zp are free for the fetch two blocks on
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
     if (a.reduce) {
-        double    vv[1]  = {(double)dot};
-        const int ops[1] = {RED_SUM};
-        block_reduce<1>(vv, ops, red_smem);
-        if (grid_partial_commit<1>(vv, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
-            grid_final<1>(vv, ops, a.red.partials, gridDim.x, red_smem);
-            if (threadIdx.x == 0) {
-                CgScalars *s = a.scal;
-                s->delta0    = s->delta;
-                s->delta     = vv[0];
-                double beta  = (s->delta - s->deltamid) / s->delta0;
-                s->beta      = beta > 0.0 ? beta : 0.0;
-            }
+        double vv[kMaxRhs];
+        int    ops[kMaxRhs];
+#pragma unroll
+        for (int q = 0; q < kMaxRhs; ++q) {
+            vv[q]  = (double)dotk[q];
+            ops[q] = RED_SUM;
+        }
+        block_reduce<kMaxRhs>(vv, ops, red_smem);
+        if (grid_partial_commit<kMaxRhs>(vv, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
+            grid_final<kMaxRhs>(vv, ops, a.red.partials, gridDim.x, red_smem);
+            if (threadIdx.x == 0)
+                for (int q = 0; q < p.nrhs; ++q) {
+                    if (p.active && !p.active[q])
+                        continue;
+                    CgScalars *s = a.scal + q;
+                    s->delta0    = s->delta;
+                    s->delta     = vv[q];
+                    double beta  = (s->delta - s->deltamid) / s->delta0;
+                    s->beta      = beta > 0.0 ? beta : 0.0;
+                }
         }
     }
 }
@@ -356,7 +406,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
 template <typename T, int N1, int N2, bool INV, int KC>
 void go_y(const ConvPlan<T> &p, cudaStream_t st)
 {
-    dim3 g((p.nzh + KC - 1) / KC, p.g.nx, p.C);
+    dim3 g((p.nzh + KC - 1) / KC, p.g.nx, p.C * p.nrhs);
     k_y_reg<T, N1, N2, INV, KC><<<g, KC * N1, 0, st>>>(p);
 }
 
@@ -384,7 +434,7 @@ cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
 template <typename T, int N1, int N2, int R>
 void go_zf(const ConvPlan<T> &p, const T *r, cudaStream_t st)
 {
-    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    const long long nrows = (long long)p.C * p.g.nx * p.g.ny * p.nrhs;
     k_z_fwd_reg<T, N1, N2, R><<<(int)((nrows + R - 1) / R), R * N1, 0, st>>>(p, r);
 }
 
@@ -392,7 +442,7 @@ template <typename T, int N1, int N2, int R>
 cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
 {
     constexpr int   M     = N1 * N2;
-    const long long nrows = (long long)p.C * p.g.nx * p.g.ny;
+    const long long nrows = (long long)p.C * p.g.nx * p.g.ny * p.nrhs;
     const long long nblk  = (nrows + R - 1) / R;
     static int      nsm   = 0;
     if (!nsm) {

@@ -67,26 +67,32 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(UpdateArgs a)
 
 // FP32 inner-loop update with 16-byte accesses (n is a multiple of 8: even grid
 // dimensions); same arithmetic and FP64 partials as k_cg_update<float, float>.
+// Several right-hand sides: blockIdx.y = k works on RHS k's fields (offset k n)
+// with alpha_k, and the last block finishes ||r_k|| and <r_k, s_k> of every
+// active RHS from its blocks' partials in block order.
 __global__ void __launch_bounds__(kVecThreads) k_cg_update_f4(UpdateArgs a)
 {
     __shared__ double red_smem[32 * 2];
-    const float   alpha = (float)a.scal->alpha;
-    float4       *r  = reinterpret_cast<float4 *>(a.r);
-    const float4 *Kd = reinterpret_cast<const float4 *>(a.Kd);
-    float4       *u  = reinterpret_cast<float4 *>(a.u);
-    const float4 *d  = reinterpret_cast<const float4 *>(a.d);
-    const float4 *s  = reinterpret_cast<const float4 *>(a.s);
+    const int       k     = blockIdx.y;
+    const bool      on    = !a.active || a.active[k];
+    const long long off   = (long long)k * a.n / 4;
+    const float     alpha = on ? (float)a.scal[k].alpha : 0.f;
+    float4       *r  = reinterpret_cast<float4 *>(a.r) + off;
+    const float4 *Kd = reinterpret_cast<const float4 *>(a.Kd) + off;
+    float4       *u  = reinterpret_cast<float4 *>(a.u) + off;
+    const float4 *d  = reinterpret_cast<const float4 *>(a.d) + off;
+    const float4 *s  = reinterpret_cast<const float4 *>(a.s) + off;
     const int     measure = a.measure;
     const bool    mx = measure == 2;
-    const long long nv = a.n / 4;
+    const long long nv = on ? a.n / 4 : 0;
     double        nrm = 0.0, rs = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
         float4       rv = r[i];
-        const float4 k = Kd[i], sv = s[i];
-        rv.x -= alpha * k.x;
-        rv.y -= alpha * k.y;
-        rv.z -= alpha * k.z;
-        rv.w -= alpha * k.w;
+        const float4 kv = Kd[i], sv = s[i];
+        rv.x -= alpha * kv.x;
+        rv.y -= alpha * kv.y;
+        rv.z -= alpha * kv.z;
+        rv.w -= alpha * kv.w;
         r[i] = rv;
         if (a.do_u) {
             float4       uv = u[i];
@@ -110,13 +116,20 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update_f4(UpdateArgs a)
     double v[2]   = {nrm, rs};
     int    ops[2] = {mx ? RED_MAX : RED_SUM, RED_SUM};
     block_reduce<2>(v, ops, red_smem);
-    if (grid_partial_commit<2>(v, a.red.partials, a.red.counter + a.red_site, gridDim.x)) {
-        grid_final<2>(v, ops, a.red.partials, gridDim.x, red_smem);
-        if (threadIdx.x == 0) {
-            a.scal->err      = a.measure == 1 ? sqrt(v[0]) : v[0];
-            a.scal->deltamid = v[1];
-            if (!isfinite(a.scal->err))
-                a.scal->converged = -1;
+    const int gx = gridDim.x;
+    if (grid_partial_commit<2>(v, a.red.partials, a.red.counter + a.red_site, gx * gridDim.y)) {
+        for (int q = 0; q < (int)gridDim.y; ++q) {
+            if (a.active && !a.active[q])
+                continue;
+            grid_final_range<2>(v, ops, a.red.partials, q * gx, gx, red_smem);
+            if (threadIdx.x == 0) {
+                CgScalars *sc = a.scal + q;
+                sc->err       = a.measure == 1 ? sqrt(v[0]) : v[0];
+                sc->deltamid  = v[1];
+                if (!isfinite(sc->err))
+                    sc->converged = -1;
+            }
+            __syncthreads(); // red_smem is reused by the next right-hand side
         }
     }
 }
@@ -245,10 +258,13 @@ cudaError_t launch_ms_convert(const uint16_t *in, uint8_t *out, long long n, uns
 template <typename T, typename TU>
 cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st)
 {
+    const int nrhs = a.nrhs > 1 ? a.nrhs : 1;
     if (std::is_same<T, float>::value && std::is_same<TU, float>::value && a.n % 4 == 0)
-        k_cg_update_f4<<<grid_blocks_for(a.n / 4), kVecThreads, 0, st>>>(a);
-    else
+        k_cg_update_f4<<<dim3(grid_blocks_for(a.n / 4), nrhs), kVecThreads, 0, st>>>(a);
+    else if (nrhs == 1)
         k_cg_update<T, TU><<<grid_blocks_for(a.n), kVecThreads, 0, st>>>(a);
+    else
+        return cudaErrorInvalidValue; // several right-hand sides: the 16-byte FP32 update only
     return cudaGetLastError();
 }
 

@@ -41,6 +41,11 @@ struct StencilArgs {
     GridRed        red;
     int            red_site;
     int            wait_limit; // tensor-core operator: polls before a pipeline wait gives up (0: default)
+    // several right-hand sides (multi-RHS operator): RHS k's fields at offset k * rhs_stride,
+    // its scalars at scal[k]; active[k] == 0 skips it (null: all active)
+    int            nrhs;
+    long long      rhs_stride;
+    const int     *active;
 };
 template <typename T>
 cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st);
@@ -84,6 +89,17 @@ size_t      stencil_tc_weights(int C, int nph); // floats of the packed W (hi + 
 void        stencil_tc_pack_weights(int C, int nph, const float *K32, float *out);
 cudaError_t launch_stencil_tc(const StencilArgs &a, const float *W, int nph, cudaStream_t st);
 long long   stencil_tc_blocks(const Grid3 &g);
+
+// Multi-RHS tensor-core CG operator with the element stiffness in an exact basis
+// (K_ph = sum_b coef[ph][b] W_b, W_b = K_b / q_b integers exact in tf32; 2 products):
+// stencil_tcb_quanta finds q_b (false if a basis matrix is not exact), the packed W
+// holds the nb basis blocks, coef is nph x nb FP32 (law coefficient x q_b).  a.nrhs
+// right-hand sides (<= kMaxRhs) in one launch, alpha_k per RHS.
+bool        stencil_tcb_quanta(int C, const double *Kb, int nb, double *q);
+bool        stencil_tcb_supported(const Grid3 &g, int C, int nb, int nph);
+size_t      stencil_tcb_weights(int C, int nb);
+void        stencil_tcb_pack_weights(int C, int nb, const double *Kb, const double *q, float *out);
+cudaError_t launch_stencil_tcb(const StencilArgs &a, const float *W, const float *coef, int nb, cudaStream_t st);
 
 // -------------------------------------------------------- element kernels ---
 enum ElemMode { ELEM_RESIDUAL = 0, ELEM_AVERAGES = 1 };
@@ -190,6 +206,10 @@ struct ConvPlan {
     int            kc_y, kc_x;     // kz columns per CTA in the y / x passes
     int            use_reg;        // register-resident passes (conv_reg_supported)
     int            var_z, var_y, var_x; // register passes: tile variant (0 default, 1 the alternative)
+    // register passes over several right-hand sides: RHS k's rows follow RHS k-1's (r, s and spec
+    // of nrhs consecutive fields; the Green's table is shared); active[k] == 0 skips RHS k
+    int            nrhs;
+    const int     *active;
 };
 
 // s = sign * IFFT(G . FFT(r)); with reduce, <r, s> -> scal (delta0, delta,
@@ -243,6 +263,8 @@ struct UpdateArgs {
     CgScalars *scal;
     GridRed    red;
     int        red_site;
+    int        nrhs;       // FP32 16-byte update: nrhs consecutive fields of n values (0 or 1: one)
+    const int *active;     // active[k] == 0 skips RHS k (null: all active)
 };
 template <typename T, typename TU>
 cudaError_t launch_cg_update(const UpdateArgs &a, cudaStream_t st);

@@ -25,7 +25,7 @@ class Context:
     """One GPU solver context (fansgpu_create .. fansgpu_destroy)."""
 
     def __init__(self, n, L=(1.0, 1.0, 1.0), howmany=3, fe_type="HEX8", precision="fp64", method="cg",
-                 strain_type="small"):
+                 strain_type="small", n_rhs=1):
         self.lib = C.load()
         d = C.Desc()
         d.n[:] = [int(v) for v in n]
@@ -35,6 +35,7 @@ class Context:
         d.precision = {"fp64": C.FP64, "mixed": C.MIXED}[precision] if isinstance(precision, str) else int(precision)
         d.method = {"cg": C.CG, "fp": C.FP, "newton": C.NEWTON}[method] if isinstance(method, str) else int(method)
         d.strain_type = C.STRAIN_TYPES[strain_type] if isinstance(strain_type, str) else int(strain_type)
+        d.n_rhs = int(n_rhs)
         ptr = ctypes.c_void_p()
         rc = self.lib.fansgpu_create(ctypes.byref(d), ctypes.byref(ptr))
         if rc != C.OK:
@@ -46,6 +47,7 @@ class Context:
         self.n_str = 9 if self.large_strain else (3 if howmany == 1 else 6)
         self.n_gp = 1 if d.fe_type == C.FE_TYPES["HEX8R"] else 8
         self.N = self.n[0] * self.n[1] * self.n[2]
+        self.n_rhs = max(1, int(n_rhs))
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -97,6 +99,29 @@ class Context:
         self._chk(self.lib.fansgpu_solve(self.ctx, ctypes.byref(st)), allow=(C.ENOTCONV,))
         return {"iterations": st.iterations, "converged": bool(st.converged), "err0": st.err0, "err": st.err,
                 "refinements": st.refinements, "solve_ms": st.solve_ms}
+
+    # -- several right-hand sides (fansgpu_set_gradients / select_rhs / rhs_stats) ----
+    def set_gradients(self, g0s):
+        g = np.ascontiguousarray(g0s, dtype=float).reshape(-1, self.n_str)
+        self._chk(self.lib.fansgpu_set_gradients(self.ctx, g.shape[0], _ptr(g)))
+
+    def select_rhs(self, k):
+        self._chk(self.lib.fansgpu_select_rhs(self.ctx, int(k)))
+
+    def rhs_stats(self, k):
+        st = C.Stats()
+        self._chk(self.lib.fansgpu_rhs_stats(self.ctx, int(k), ctypes.byref(st)))
+        return {"iterations": st.iterations, "converged": bool(st.converged), "err0": st.err0, "err": st.err,
+                "refinements": st.refinements, "solve_ms": st.solve_ms}
+
+    def homogenized_stresses(self):
+        """<sigma> of every right-hand side (n_rhs x n_str); RHS 0 is selected afterwards."""
+        out = np.zeros((self.n_rhs, self.n_str))
+        for k in range(self.n_rhs):
+            self.select_rhs(k)
+            out[k] = self.homogenized_stress()
+        self.select_rhs(0)
+        return out
 
     def homogenized_stress(self):
         out = np.zeros(self.n_str)

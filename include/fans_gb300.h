@@ -118,7 +118,13 @@ typedef struct {
     int32_t precision;   /* FANSGPU_FP64 / FANSGPU_MIXED */
     int32_t method;      /* FANSGPU_CG / FANSGPU_FP / FANSGPU_NEWTON */
     int32_t strain_type; /* FANSGPU_SMALL_STRAIN <3,6> (0, default) or FANSGPU_LARGE_STRAIN <3,9> */
+    int32_t n_rhs;       /* right-hand sides (load cases) held and solved together: 1..FANSGPU_MAX_RHS
+                            (0 means 1).  FANS runs its load cases one Solver after another
+                            (main.cpp:14-41) and its linear tangent as n_str solves (solver.h:759-776);
+                            here they share one solve (see fansgpu_set_gradients) */
 } fansgpu_desc;
+
+#define FANSGPU_MAX_RHS 6
 
 #define FANSGPU_SMALL_STRAIN 0
 #define FANSGPU_LARGE_STRAIN 1 /* n_str = 9: g0 and strains are the deformation gradient F (row-major),
@@ -252,6 +258,33 @@ int fansgpu_set_tolerance(fansgpu_ctx *ctx, const fansgpu_tol *tol);
  * variables (solver.h:299).  stats may be NULL.  Returns FANSGPU_ENOTCONV when
  * n_it was reached (the state is still valid, as in the reference). */
 int fansgpu_solve(fansgpu_ctx *ctx, fansgpu_stats *stats);
+
+/* Several right-hand sides (fansgpu_desc.n_rhs > 1; new on the GPU path): the
+ * context holds one displacement, residual and solver state per RHS.  Each RHS
+ * is one FANS load case with its own macroscopic gradient -- the n_str unit
+ * gradients of the linear homogenized tangent (solver.h:759-776), or the load
+ * cases of an input file (main.cpp:14-41).
+ *   fansgpu_set_gradients: g0 of every RHS (n_rhs x n_str, row-major; n must
+ *     equal n_rhs).
+ *   fansgpu_solve: solves every RHS.  Linear laws only (internal variables are
+ *     per solve), strain control, CG or FP.  With MIXED precision on the
+ *     tensor-core path all RHS run as one multi-RHS CG: every kernel of an
+ *     iteration covers all of them (the Green's table is read once per
+ *     iteration for all RHS), each RHS keeps its own CG scalars, reliable
+ *     updates and convergence test, and leaves the iteration once converged;
+ *     the per-RHS results equal those of separate solves.  Otherwise the RHS are
+ *     solved one after another.  stats (may be NULL) gets the aggregate: the
+ *     largest iteration count, converged = all converged, err0 / err of the
+ *     RHS with the largest relative error, refinements summed.
+ *   fansgpu_select_rhs: the RHS that fansgpu_set_gradient, _homogenized_stress,
+ *     _homogenized_tangent, _postprocess_averages, _get_field / _set_field,
+ *     _get_error_history, _store_solution, _residual, _apply_operator and
+ *     _convolve act on (default 0).  fansgpu_reset and
+ *     fansgpu_extrapolate_displacement act on every RHS.
+ *   fansgpu_rhs_stats: the last solve's statistics of RHS k. */
+int fansgpu_set_gradients(fansgpu_ctx *ctx, int32_t n, const double *g0);
+int fansgpu_select_rhs(fansgpu_ctx *ctx, int32_t k);
+int fansgpu_rhs_stats(fansgpu_ctx *ctx, int32_t k, fansgpu_stats *stats);
 
 /* Independent solves of several contexts at once (batched micro problems, e.g.
  * one per macroscopic integration point): each context's fansgpu_solve runs on

@@ -136,3 +136,38 @@ def test_sphere_generator_counts():
     ms2, c2 = spheres(32, 4, 0.2, seed=0)
     assert np.array_equal(ms, ms2)
     assert 0.17 < ms.mean() < 0.23
+
+
+def test_struct_layouts_match_a_c_compiler(tmp_path):
+    """fansgpu_desc / fansgpu_tol / fansgpu_stats as gcc lays them out from
+    include/fans_gb300.h (sizes and every field offset) equal the ctypes mirror
+    the Python binding passes."""
+    import shutil
+    import subprocess
+
+    from fans_gb300 import _lib
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("gcc not available")
+    structs = {"fansgpu_desc": _lib.Desc, "fansgpu_tol": _lib.Tol, "fansgpu_stats": _lib.Stats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fans_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            parts = ln.split()
+            got[tuple(parts[:-1])] = int(parts[-1])
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

@@ -53,7 +53,7 @@ def test_cpp_binding_solves_like_the_oracle(tmp_path):
     loads = [np.array([1.0, 0, 0, 0, 0, 0]), np.array([0.3, -0.2, 0.1, 0.05, -0.04, 0.02])]
     lines = ["16 16 16", "HEX8 fp64 cg L2 relative 1e-12 2000", str(P.nphase)]
     for ph in range(P.nphase):
-        lines.append(f"{int(P.law[ph])} 2 {P.param[ph, 0]!r} {P.param[ph, 1]!r}")
+        lines.append(f"{int(P.law[ph])} 2 {float(P.param[ph, 0])!r} {float(P.param[ph, 1])!r}")
     lines.append(" ".join(repr(float(v)) for v in np.asarray(P.kapparef).ravel()))
     lines.append(str(len(loads)))
     lines += [" ".join(repr(float(v)) for v in g) for g in loads]

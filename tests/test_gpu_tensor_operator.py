@@ -21,9 +21,12 @@ from helpers import ELASTIC, THERMAL, gpu_context, oracle_problem, random_ms, re
 pytestmark = pytest.mark.gpu
 
 
-def _solve(P, g0, simt):
+def _solve(P, g0, simt, mode=None):
+    """mode: "tcb" (default operator: exact-basis tensor cores where it applies),
+    "tc" (per-phase 3xTF32 tensor-core operator) or "simt" (CUDA cores)."""
+    mode = mode or ("simt" if simt else "tc")
     old = os.environ.get("FANSGPU_STENCIL")
-    os.environ["FANSGPU_STENCIL"] = "simt" if simt else "tc"
+    os.environ["FANSGPU_STENCIL"] = "" if mode == "tcb" else mode
     try:
         ctx = gpu_context(P, precision="mixed")
     finally:
@@ -53,6 +56,31 @@ def test_tensor_operator_matches_cuda_core_operator(c, groups, shape):
     assert a["st"]["converged"] and b["st"]["converged"]
     assert abs(a["st"]["iterations"] - b["st"]["iterations"]) <= 1
     assert rel(a["stress"], b["stress"]) < 1e-9
+    assert rel(a["u"], b["u"]) < 1e-6
+    P.set_gradient(g0)
+    P.solve(measure="L2", type="relative", tol=1e-8, n_it=500)
+    assert rel(a["stress"], P.homogenized_stress()) < 1e-7
+
+
+@pytest.mark.parametrize("c,groups,shape", [(3, ELASTIC, (32, 32, 32)), (3, ELASTIC, (40, 16, 48)),
+                                            (3, ELASTIC, (80, 40, 64)), (1, THERMAL, (24, 32, 32)),
+                                            (1, THERMAL, (16, 48, 32))])
+def test_basis_operator_matches_cuda_core_and_per_phase_operators(c, groups, shape):
+    """The exact-basis tensor-core operator (the default where every phase is an
+    isotropic law and the register FFT applies; ragged tiles in x, y and z here)
+    against the CUDA-core and the per-phase 3xTF32 operators: same iterations
+    (within 1), stresses to 1e-9, the oracle to 1e-7."""
+    ms = random_ms(shape, vf=0.3, seed=22)
+    P = oracle_problem(ms, c, groups, "HEX8")
+    g0 = np.linspace(0.7, -0.3, P.nstr)
+    a = _solve(P, g0, False, "tcb")
+    b = _solve(P, g0, True)
+    t = _solve(P, g0, False, "tc")
+    for o in (a, b, t):
+        assert o["st"]["converged"]
+    assert abs(a["st"]["iterations"] - b["st"]["iterations"]) <= 1
+    assert abs(a["st"]["iterations"] - t["st"]["iterations"]) <= 1
+    assert rel(a["stress"], b["stress"]) < 1e-9 and rel(a["stress"], t["stress"]) < 1e-9
     assert rel(a["u"], b["u"]) < 1e-6
     P.set_gradient(g0)
     P.solve(measure="L2", type="relative", tol=1e-8, n_it=500)
