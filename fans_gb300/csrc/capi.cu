@@ -2693,6 +2693,14 @@ int solve_newton(fansgpu_ctx *ctx, int *inner)
         int its = 0;
         rc      = tangent_cg(ctx, a, du, res, true, eta, &its);
         *inner += its;
+        if (rc == FANSGPU_ENAN) {
+            // the tangent solve broke down (e.g. a right-hand side at round-off level): no step
+            // is taken, u and r stay those of the last accepted step, and the solve reports ENOTCONV
+            fail(ctx, FANSGPU_ENOTCONV, "Newton-Krylov: the tangent solve broke down at step %d; u kept",
+                 ctx->iter + 1);
+            ctx->newton_stalled = true;
+            break;
+        }
         if (rc && rc != FANSGPU_ENOTCONV) // an inner solve stopped by n_it still gives a usable step
             return rc;
         FANS_CUDA_CHECK(cudaMemcpyAsync(u_save, ctx->u, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->st));
@@ -2759,6 +2767,8 @@ int solve_one(fansgpu_ctx *ctx, int *refinements)
 {
     int rc;
     *refinements = 0;
+    if ((rc = setup(ctx))) // the force tables follow this RHS's g0
+        return rc;
     if (ctx->desc.method == FANSGPU_FP)
         rc = solve_fp64(ctx);
     else if (ctx->desc.method == FANSGPU_NEWTON)

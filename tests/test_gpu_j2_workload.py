@@ -7,13 +7,20 @@ reference's test_J2Plasticity.json does: with extrapolateDisplacement the
 elastic steps start almost converged, and a relative tolerance would then ask
 for a residual below round-off.
 
-The oracle cannot run 20 nonlinear steps at 128^3 inside a test, so:
-* the same workload down-sampled to 32^3 is compared with the oracle step by
-  step (stress averages 1e-7, committed plastic strains 1e-6 of their maximum);
-* at 128^3 eight steps of 0.001 (eps_11 to 0.008): the first step is
-  elastic (equal to the elastic solve), the tangent drops once the matrix
-  yields and stays positive (hardening), and plastic strain appears in the
-  matrix only."""
+The oracle cannot run 20 nonlinear steps at 128^3 inside a test (about 16
+minutes on 8 host cores), so its curve is a committed fixture,
+tests/golden/j2_128_curve.json, made by tests/golden/make_workload_fixtures.py
+with the same solver settings.  The GPU path -- nonlinear CG with
+LineSearchSecant and Newton-Krylov -- runs the full 20-step workload and meets
+that curve step by step to 1e-7 relative (the solves stop at Linfinity 1e-10,
+and the secant line search's discrete decisions let converged states differ at
+that level).  Also:
+* the same workload down-sampled to 32^3 is compared with the oracle run live,
+  step by step (stress averages 1e-7, committed plastic strains 1e-6 of their
+  maximum);
+* on the 128^3 curve the first step is elastic (equal to the elastic solve),
+  the tangent drops once the matrix yields and stays positive (hardening), and
+  plastic strain appears in the matrix only."""
 import numpy as np
 import pytest
 
@@ -66,25 +73,50 @@ def test_j2_workload_downsampled_matches_oracle():
     ctx.close()
 
 
-def test_j2_workload_128_curve_properties():
-    ms = _ms(128)
-    assert abs(ms.mean() - 0.25) < 0.02
+def _fixture():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "j2_128_curve.json")) as f:
+        return json.load(f)
+
+
+def _ctx128(ms, method):
     from fans_gb300 import Context
 
     P = oracle_problem(ms[:4, :4, :4], 3, J2, "HEX8")  # the reference-stiffness rule only
-
-    ctx = Context((128, 128, 128), (1.0, 1.0, 1.0), 3, "HEX8", "fp64", "cg")
+    ctx = Context((128, 128, 128), (1.0, 1.0, 1.0), 3, "HEX8", "fp64", method)
     ctx.set_microstructure(ms)
     ctx.set_phase_material(0, O.LAW_J2, [68.6275, 26.3158, 0.25, 2.0])
     ctx.set_phase_material(1, O.LAW_ELASTIC_ISO, [222.222, 166.667])
     ctx.set_reference(P.kapparef)
     ctx.set_tolerance("Linfinity", "absolute", 1e-10, 2000)
-    sig = _path(ctx, 8, de=0.001)
-    ep = ctx.get_field(5).reshape(-1, 6)
-    # plastic strain only in the matrix, and it is there at the end of the path
-    assert np.abs(ep[ms.reshape(-1) == 1]).max() == 0.0
-    assert np.abs(ep[ms.reshape(-1) == 0]).max() > 0.0
+    return ctx
+
+
+@pytest.mark.parametrize("method", ["cg", "newton"])
+def test_j2_workload_128_matches_oracle_curve(method):
+    fx = _fixture()
+    ms = _ms(128)
+    assert abs(ms.mean() - fx["vf"]) < 1e-12  # the fixture's microstructure
+    ctx = _ctx128(ms, method)
+    sig = _path(ctx, 20)
+    ref = np.array(fx["stress"])
+    for k in range(20):
+        assert rel(sig[k], ref[k]) < 1e-7, (method, k, sig[k], ref[k])
+    if method == "cg":
+        ep = ctx.get_field(5).reshape(-1, 6)
+        # plastic strain only in the matrix, and it is there at the end of the path
+        assert np.abs(ep[ms.reshape(-1) == 1]).max() == 0.0
+        assert np.abs(ep[ms.reshape(-1) == 0]).max() > 0.0
     ctx.close()
+    print(f"J2 128^3 {method}: sigma_11 at eps_11 = 0.01: {sig[-1, 0]:.10f} (oracle {ref[-1, 0]:.10f})")
+
+
+def test_j2_workload_128_curve_properties():
+    ms = _ms(128)
+    sig = np.array(_fixture()["stress"])
+    from fans_gb300 import Context
 
     # the elastic reference: the same microstructure with an elastic matrix
     el = Context((128, 128, 128), (1.0, 1.0, 1.0), 3, "HEX8", "fp64", "cg")
@@ -94,13 +126,13 @@ def test_j2_workload_128_curve_properties():
     el.set_reference(O.OracleProblem(ms[:4, :4, :4], (1, 1, 1), 3, ELASTIC, "HEX8").kapparef)
     el.set_tolerance("L2", "relative", 1e-10, 2000)
     g = np.zeros(6)
-    g[0] = 0.001
+    g[0] = 0.0005
     el.set_gradient(g)
     assert el.solve()["converged"]
     s_el = el.homogenized_stress()
     el.close()
     # the first step is elastic (J2 and the elastic solve agree), later ones soften and harden
     assert rel(sig[0], s_el) < 1e-6
-    tangent = np.diff(sig[:, 0]) / 0.001
+    tangent = np.diff(sig[:, 0]) / 0.0005
     assert tangent[-1] < 0.8 * tangent[0]  # the matrix has yielded
     assert (tangent > 0).all()  # linear isotropic hardening keeps the tangent positive

@@ -108,9 +108,9 @@ def test_newton_stall_restores_u_and_reports_not_converged():
     """A Newton step that does not lower the residual after five halvings is
     undone: u (and with it r and the trial internal variables) goes back to the
     state before the step and the solve stops with ENOTCONV instead of running
-    to n_it.  Forced by asking for an absolute Linfinity tolerance of 0 from a
-    state already converged to round-off, where no step can keep lowering the
-    residual."""
+    to n_it; so does a step whose tangent solve breaks down.  Forced by asking
+    for an absolute Linfinity tolerance of 0 from a state already converged to
+    round-off, where no step can keep lowering the residual."""
     from fans_gb300 import _lib
 
     P = oracle_problem(_ms(16), 3, J2, "HEX8")
@@ -126,7 +126,8 @@ def test_newton_stall_restores_u_and_reports_not_converged():
     assert not st["converged"] and st["iterations"] < 200, st
     hist = nt.error_history()
     assert len(hist) == st["iterations"] + 1 and hist[-1] == st["err"] and st["err"] <= hist[0]
-    assert "no decrease" in _lib.load().fansgpu_last_error(nt.ctx).decode()
+    msg = _lib.load().fansgpu_last_error(nt.ctx).decode()
+    assert "no decrease" in msg or "broke down" in msg, msg
     # the state is the last accepted one: its residual norm is the reported error
     r = nt.get_field(_lib.FIELD_R)
     assert np.abs(r).max() == pytest.approx(st["err"], rel=1e-12, abs=0)
