@@ -203,16 +203,16 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
     const long long rpr   = (long long)p.C * p.g.nx * p.g.ny; // rows per right-hand side
     const long long nrows = rpr * p.nrhs;
     const long long row0b = (long long)blockIdx.x * R;
-    if (p.active) { // return when every row of this block belongs to an inactive right-hand side
-        const long long last = min(row0b + R, nrows) - 1;
-        bool            any  = false;
-        for (long long q = row0b / rpr; q <= last / rpr; ++q)
-            any = any || p.active[q];
-        if (!any)
-            return;
-    }
+    // A block's rows belong to at most two right-hand sides (R <= 64 rows per block, and
+    // the register plans need n_x, n_y >= 16, so every RHS has >= 256 rows): RHS k0 below
+    // row bnd, k0 + 1 from there.
+    const int       k0  = p.active ? (int)(row0b / rpr) : 0;
+    const long long bnd = p.active ? (k0 + 1) * rpr : nrows;
+    auto            on  = [&](long long rw) { return !p.active || p.active[k0 + (rw >= bnd ? 1 : 0)]; };
+    if (p.active && !on(row0b) && !on(min(row0b + R, nrows) - 1))
+        return; // every row of this block belongs to an inactive right-hand side
     const long long row   = row0b + L;
-    const bool      valid = row < nrows && (!p.active || p.active[row / rpr]);
+    const bool      valid = row < nrows && on(row);
     const cplx<T>  *rin   = reinterpret_cast<const cplx<T> *>(r) + row * M;
     cplx<T>         v[N2];
 #pragma unroll
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
     const long long row0 = (long long)blockIdx.x * R;
     for (int i = t; i < R * (M + 1); i += blockDim.x) {
         const int Lr = i / (M + 1), k = i % (M + 1);
-        if (row0 + Lr >= nrows || (p.active && !p.active[(row0 + Lr) / rpr]))
+        if (row0 + Lr >= nrows || !on(row0 + Lr))
             continue;
         cplx<T> zk = Z[Lr * M + (k == M ? 0 : k)];
         cplx<T> zm = Z[Lr * M + (k == 0 ? 0 : M - k)];
@@ -270,15 +270,14 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
     const long long rpr   = (long long)p.C * p.g.nx * p.g.ny; // rows per right-hand side
     const long long nrows = rpr * p.nrhs;
     const long long nblk  = (nrows + R - 1) / R;
-    // a block of rows is skipped when all its rows belong to inactive right-hand sides
+    // a block's rows belong to at most two right-hand sides (as in k_z_fwd_reg); a block is
+    // skipped when all its rows belong to inactive ones
     auto live = [&](long long blk) {
         if (!p.active)
             return true;
+        const int       k0   = (int)(blk * R / rpr);
         const long long last = min(blk * R + R, nrows) - 1;
-        bool            any  = false;
-        for (long long q = blk * R / rpr; q <= last / rpr; ++q)
-            any = any || p.active[q];
-        return any;
+        return p.active[k0] || (last >= (k0 + 1) * rpr && p.active[k0 + 1]);
     };
     auto fetch = [&](long long blk, int b) {
         if (blk < nblk && live(blk)) {
@@ -348,7 +347,8 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
             E[(L * N2 + k2) * EP + w] = v[k2];
         __syncthreads();
         const long long row = row0 + L;
-        const int       rk  = (int)(row / rpr);
+        const int       rk0 = p.active || p.nrhs > 1 ? (int)(row0 / rpr) : 0;
+        const int       rk  = rk0 + (row >= (rk0 + 1) * rpr ? 1 : 0);
         if (row < nrows && w < N2 && (!p.active || p.active[rk])) {
             cplx<T> u[N1];
 #pragma unroll

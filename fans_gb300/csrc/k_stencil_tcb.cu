@@ -86,7 +86,8 @@ struct TbCfg {
     static constexpr int OFF_X    = al(OFF_RAW + RAWD * 2 * C * NPL * 4); // [2][EYN][C][32]
     static constexpr int OFF_BAR  = al(OFF_X + 2 * EYN * C * 32 * 4);     // NBAR mbarriers, tmem slot, abort flag
     static constexpr int OFF_ACT  = OFF_BAR + NBAR * 8 + 8;              // active RHS list + count
-    static constexpr int OFF_SEG  = al(OFF_ACT + (kMaxRhs + 1) * 4);      // [4 warps][kMaxRhs] double
+    static constexpr int OFF_BETA = OFF_ACT + (kMaxRhs + 1) * 4;         // beta of each active RHS (float)
+    static constexpr int OFF_SEG  = al(OFF_BETA + kMaxRhs * 4);           // [4 warps][kMaxRhs] double
     static constexpr int OFF_RED  = al(OFF_SEG + 4 * kMaxRhs * 8);        // [32][kMaxRhs] double
     static constexpr int SMEM     = OFF_RED + 32 * kMaxRhs * 8;
     static_assert(NW <= TCOLS - COL_D && NCOL <= COL_LO && COL_LO + NCOL <= COL_D, "tensor-memory map");
@@ -194,6 +195,7 @@ __global__ void __launch_bounds__(TPB, 3)
     uint32_t     *tmem_slot  = reinterpret_cast<uint32_t *>(smem + Cfg::OFF_BAR + NBAR * 8);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + Cfg::OFF_BAR + NBAR * 8 + 4);
     int          *s_act      = reinterpret_cast<int *>(smem + Cfg::OFF_ACT); // [kMaxRhs] RHS ids, then the count
+    float        *s_beta     = reinterpret_cast<float *>(smem + Cfg::OFF_BETA); // beta of segment kk
     double       *seg_red    = reinterpret_cast<double *>(smem + Cfg::OFF_SEG);
     double       *red_smem   = reinterpret_cast<double *>(smem + Cfg::OFF_RED);
     auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
@@ -218,8 +220,10 @@ __global__ void __launch_bounds__(TPB, 3)
     if (tid == 0) {
         int n = 0;
         for (int k = 0; k < a.nrhs; ++k)
-            if (!a.active || a.active[k])
+            if (!a.active || a.active[k]) {
+                s_beta[n]  = (float)a.scal[k].beta;
                 s_act[n++] = k;
+            }
         s_act[kMaxRhs] = n;
         mbar_init(bar(BAR_AFULL), NGRP);
         mbar_init(bar(BAR_DFULL), 1);
@@ -305,7 +309,7 @@ __global__ void __launch_bounds__(TPB, 3)
             const int       X       = xs - 1 + sm;
             const bool      owned_x = X >= xs && X < xe;
             const long long off     = (long long)rk * rstr + (long long)wrapi(X, nx) * plane;
-            const float     beta    = (float)a.scal[rk].beta;
+            const float     beta    = s_beta[sk];
             const float    *raw     = Raw + (sg % RAWD) * 2 * C * NPL;
             float          *slot    = Dp + (sg % R) * C * NPL;
 #pragma unroll
@@ -384,7 +388,7 @@ __global__ void __launch_bounds__(TPB, 3)
 #pragma unroll
         for (int i = 0; i < 4 * C; ++i)
             carry[i] = 0.f;
-        double dot = 0.0; // <d_k, K d_k> of this thread's nodes in the current segment
+        float dot = 0.f; // <d_k, K d_k> of this thread's nodes in the current segment (FP64 from the warp sum on)
         int ph_next = nU > 0 ? a.ms[(long long)wrapi(xs - 1, nx) * plane + el_yz] : 0;
         int kk = 0, j = 0; // segment and element plane of unit U
         for (int U = 0; U < nU; ++U, j = (j + 1 == J) ? 0 : j + 1, kk += (j == 0)) {
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(TPB, 3)
                         yout[c * N + gi] = vo;
                         dl += dp[c * NPL] * vo;
                     }
-                    dot += (double)dl;
+                    dot += dl;
                 }
             }
             mbar_arrive(bar(BAR_SFREE + g0 % R));
@@ -460,12 +464,13 @@ __global__ void __launch_bounds__(TPB, 3)
                 // end of the segment: release its last node plane (read only by the producers,
                 // whose A build of this unit the MMAs have consumed) and fold <d, K d>
                 mbar_arrive(bar(BAR_SFREE + (g0 + 1) % R));
+                double dd = (double)dot;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1)
-                    dot += __shfl_down_sync(0xffffffffu, dot, o);
+                    dd += __shfl_down_sync(0xffffffffu, dd, o);
                 if (lane == 0)
-                    seg_red[ey * kMaxRhs + s_act[kk]] = dot;
-                dot = 0.0;
+                    seg_red[ey * kMaxRhs + s_act[kk]] = dd;
+                dot = 0.f;
             }
         }
     } else if (lane == 0) {
