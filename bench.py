@@ -195,6 +195,16 @@ def max_over_ranks(value, dist=None, device="cpu"):
     return float(t.item())
 
 
+def fp64_rate():
+    import ctypes
+
+    from fans_gb300 import _lib
+
+    v = ctypes.c_double(0.0)
+    rc = _lib.load().fansgpu_fp64_fma_rate(ctypes.byref(v))
+    return v.value if rc == 0 else None
+
+
 def build_problem(n, seed=0):
     from fans_gb300.microstructure import spheres
 
@@ -536,10 +546,22 @@ def main():
         ctx64.solve()  # builds the Green's table; 3 iterations as warm-up
         ctx64.set_tolerance("L2", "relative", args.tol, 2000)
         st64: list = []
+        ctx64.set_timing(True)  # per-launch events: the FP64 path runs no graphs, so the step time is unchanged
         t64, C64 = timed_steps(ctx64, 1, lambda: homogenize(ctx64, kref, st64))
+        k64 = ctx64.kernel_times()
         fp64 = {"ms_per_step": round(t64, 1), "iterations": [s["iterations"] for s in st64],
                 "ceff_rel_diff_mixed_vs_fp64": float(np.linalg.norm(Ceff - C64) / np.linalg.norm(C64)),
-                "speedup_mixed_vs_fp64": round(t64 / ms_step, 2)}
+                "speedup_mixed_vs_fp64": round(t64 / ms_step, 2),
+                "kernels_ms": {k: round(v[0], 1) for k, v in k64.items() if v[1]}}
+        # the FP64 operator is bound by the FP64 pipe: its DFMA rate against the measured one
+        rate = fp64_rate()
+        sl = k64.get("stencil", (0.0, 0))
+        if rate and sl[1]:
+            dfma = 64 * 3 * 3 * n ** 3  # 8 elements x (8 nodes x 3 comps) x 3 rows per node
+            achieved = dfma * sl[1] / (sl[0] * 1e-3)
+            fp64["operator_roofline"] = {"bound": "fp64", "achieved_dfma_per_s": achieved, "peak_dfma_per_s": rate,
+                                         "frac": round(achieved / rate, 3), "avg_launch_ms": round(sl[0] / sl[1], 3),
+                                         "peak_kind": "measured (fansgpu_fp64_fma_rate)"}
         ctx64.close()
 
     cpu = None

@@ -47,6 +47,7 @@ EXPORTS = [
     "fansgpu_enable_mixed_bc", "fansgpu_disable_mixed_bc", "fansgpu_get_gradient", "fansgpu_set_voxel_field",
     "fansgpu_store_solution", "fansgpu_stiffness_gradient", "fansgpu_solve_batch", "fansgpu_yield_stress_adjoint",
     "fansgpu_tuning", "fansgpu_set_wait_limit", "fansgpu_set_gradients", "fansgpu_select_rhs", "fansgpu_rhs_stats",
+    "fansgpu_fp64_fma_rate",
 ]
 MAX_RHS = 6
 KERNEL_NAMES = ["stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update",
@@ -140,6 +141,7 @@ def _declare(L):
     L.fansgpu_set_gradients.argtypes = [vp, ip, dp]
     L.fansgpu_select_rhs.argtypes = [vp, ip]
     L.fansgpu_rhs_stats.argtypes = [vp, ip, ctypes.POINTER(Stats)]
+    L.fansgpu_fp64_fma_rate.argtypes = [dp]
     for name in EXPORTS:
         if name not in ("fansgpu_last_error", "fansgpu_version"):
             getattr(L, name).restype = ctypes.c_int

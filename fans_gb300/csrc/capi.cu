@@ -140,6 +140,8 @@ struct fansgpu_ctx {
     int    tune       = 1;     // FANSGPU_TUNE: 1 FFT tiles (default), 3 + operator, 0 defaults, 2 forced
     int    tune_force[3] = {0, 0, 0}; // forced z / y / x tile variants
     int    tc_wait_limit = 0;         // tensor-core operator's pipeline-wait bound in polls (0: default)
+    int    tc_backoff_ns = 0;         // basis operator: consumers' pause between polls (FANSGPU_TC_BACKOFF)
+    bool   fp64_df = true;            // FP64 CG: operator in double-float (FANSGPU_FP64_OPERATOR=dfma: FP64 pipe)
 
     // several right-hand sides (desc.n_rhs): u, r and u_prev are per-RHS slices of u0, r0, up0
     // (n values each) and point at the selected RHS `cur`; the FP32 fields of the mixed path and
@@ -783,7 +785,8 @@ int solve_cg64(fansgpu_ctx *ctx)
     if ((rc = init_scalars(ctx)))
         return rc;
     // r = R(u) (compute_residual<2>, solverCG.h:76)
-    if ((rc = run_residual64(ctx, ctx->u, ctx->r)))
+    const bool df = ctx->fp64_df && ctx->all_linear && !ctx->vscale; // FP64-accurate operator off the FP64 pipe
+    if ((rc = df ? run_residual_df(ctx) : run_residual64(ctx, ctx->u, ctx->r)))
         return rc;
     { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
@@ -827,6 +830,14 @@ int solve_cg64(fansgpu_ctx *ctx)
                 return rc;
             FANS_CUDA_CHECK(launch_dot(dn, ctx->Kd, n, &ctx->scal->dAd, ctx->red, SITE_DOT, ctx->st));
             FANS_CUDA_CHECK(launch_set_alpha(ctx->scal, ctx->st));
+        } else if (df) {
+            // d = s + beta d_old, K d in double-float on the FP32 pipes (GB300's FP64 rate is about
+            // 1/60 of its FP32 rate), <d, K d> and alpha in FP64
+            sa.Kph = ctx->Kdf;
+            sa.fph = nullptr;
+            int e0 = tk_mark(ctx);
+            FANS_CUDA_CHECK(launch_residual_df(sa, ctx->st));
+            tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
         } else {
             int e0 = tk_mark(ctx);
             FANS_CUDA_CHECK(launch_stencil<double>(sa, ctx->st));
@@ -870,6 +881,7 @@ StencilArgs mixed_operator_args(fansgpu_ctx *ctx, int cd)
     sa.red      = ctx->red;
     sa.red_site = SITE_STENCIL;
     sa.wait_limit = ctx->tc_wait_limit;
+    sa.wait_sleep_ns = ctx->tc_backoff_ns;
     return sa;
 }
 
@@ -1811,6 +1823,10 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
                 ctx->tune_force[k] = ev[k] - '0';
         }
     }
+    if (const char *ev = std::getenv("FANSGPU_FP64_OPERATOR")) // "dfma": the FP64 CG operator on the FP64 pipe
+        ctx->fp64_df = std::strcmp(ev, "dfma") != 0;
+    if (const char *ev = std::getenv("FANSGPU_TC_BACKOFF")) // ns between the operator consumers' polls
+        ctx->tc_backoff_ns = std::max(0, std::min(100000, std::atoi(ev)));
     if (const char *ev = std::getenv("FANSGPU_GRAPHS")) { // "0": no graphs; "iter": one graph per iteration
         ctx->use_graphs     = std::strcmp(ev, "0") != 0;
         ctx->loop_on_device = std::strcmp(ev, "iter") != 0;

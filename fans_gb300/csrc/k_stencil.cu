@@ -513,20 +513,32 @@ __global__ void __launch_bounds__(kStencilThreads) k_residual_df(StencilArgs a)
         int gx = pmod(x0 - 1 + ex, nx), gy = pmod(y0 - 1 + ey, ny), gz = pmod(z0 - 1 + ez, nz);
         mss[i] = a.ms[((long long)gx * ny + gy) * nz + gz];
     }
-    const double *u = reinterpret_cast<const double *>(a.x);
+    // x = u, or with fuse_d the CG direction d = s + beta d_old in FP64 (written to d_new
+    // for the nodes this CTA owns)
+    const double *u    = reinterpret_cast<const double *>(a.x);
+    const double *dold = reinterpret_cast<const double *>(a.d_old);
+    double       *dnew = reinterpret_cast<double *>(a.d_new);
+    const double  beta = a.fuse_d ? a.scal->beta : 0.0;
     for (int i = tid; i < HXYZ; i += blockDim.x) {
         int hz = i % HZ, hy = (i / HZ) % HY, hx = i / (HZ * HY);
         int gx = pmod(x0 - 1 + hx, nx), gy = pmod(y0 - 1 + hy, ny), gz = pmod(z0 - 1 + hz, nz);
         long long gi = ((long long)gx * ny + gy) * nz + gz;
+        const bool own = a.fuse_d && hx >= 1 && hx <= TX && hy >= 1 && hy <= TY && hz >= 1 && hz <= TZ &&
+                         x0 - 1 + hx < nx && y0 - 1 + hy < ny && z0 - 1 + hz < nz;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            const double v  = u[c * N + gi];
-            const float  hi = (float)v;
+            double v = u[c * N + gi];
+            if (a.fuse_d)
+                v = v + beta * dold[c * N + gi];
+            if (own)
+                dnew[c * N + gi] = v;
+            const float hi = (float)v;
             xh[c * HXYZ + i] = hi;
             xl[c * HXYZ + i] = (float)(v - (double)hi);
         }
     }
     __syncthreads();
+    double dot = 0.0; // <x, y> of this thread's nodes (reduce)
 
     const float *fg = reinterpret_cast<const float *>(a.fph); // [hi | lo], nph * NC each
     const int  tz = tid % TZ, ty = tid / TZ;
@@ -599,8 +611,26 @@ __global__ void __launch_bounds__(kStencilThreads) k_residual_df(StencilArgs a)
         const long long gi   = ((long long)gx * ny + gy) * nz + gz;
         double         *yout = reinterpret_cast<double *>(a.y);
 #pragma unroll
-        for (int c = 0; c < C; ++c)
-            yout[c * N + gi] = (double)Sh[c] + (double)Sl[c];
+        for (int c = 0; c < C; ++c) {
+            const double yv = (double)Sh[c] + (double)Sl[c];
+            yout[c * N + gi] = yv;
+            if (a.reduce)
+                dot += ((double)ch[c] + (double)cl[c]) * yv;
+        }
+    }
+    if (a.reduce) { // <d, K d> and alpha = delta / <d, K d> (solverCG.h:101)
+        __shared__ double red_smem[32];
+        double    v[1]   = {dot};
+        const int ops[1] = {RED_SUM};
+        block_reduce<1>(v, ops, red_smem);
+        const int nb = gridDim.x * gridDim.y * gridDim.z;
+        if (grid_partial_commit<1>(v, a.red.partials, a.red.counter + a.red_site, nb)) {
+            grid_final<1>(v, ops, a.red.partials, nb, red_smem);
+            if (threadIdx.x == 0) {
+                a.scal->dAd   = v[0];
+                a.scal->alpha = a.scal->delta / v[0];
+            }
+        }
     }
 }
 

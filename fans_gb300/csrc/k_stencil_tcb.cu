@@ -175,6 +175,19 @@ __device__ __forceinline__ void mbar_wait(uint32_t bar, uint32_t parity, volatil
     *abort_flag = 1;
 }
 
+// The same with a pause of `ns` nanoseconds between polls: for waits off the critical path,
+// so that the waiting warps leave their issue slots to the warps doing the work.
+__device__ __forceinline__ void mbar_wait_sleep(uint32_t bar, uint32_t parity, volatile int *abort_flag, unsigned limit,
+                                                unsigned ns)
+{
+    for (unsigned it = 0; it < limit; ++it) {
+        if (mbar_try(bar, parity) || *abort_flag)
+            return;
+        __nanosleep(ns);
+    }
+    *abort_flag = 1;
+}
+
 __device__ __forceinline__ void named_bar(int id, int nthreads)
 {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
@@ -401,7 +414,10 @@ __global__ void __launch_bounds__(TPB, 3)
 #pragma unroll
             for (int bb = 0; bb < NB; ++bb)
                 cf[bb] = coef[ph * NB + bb];
-            mbar_wait(bar(BAR_DFULL), (uint32_t)(U & 1), abort_flag, wlim);
+            if (a.wait_sleep_ns > 0)
+                mbar_wait_sleep(bar(BAR_DFULL), (uint32_t)(U & 1), abort_flag, wlim, (unsigned)a.wait_sleep_ns);
+            else
+                mbar_wait(bar(BAR_DFULL), (uint32_t)(U & 1), abort_flag, wlim);
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             float out[NCOL]; // K_ph u_e = sum_b cf_b D_b

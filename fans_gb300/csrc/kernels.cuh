@@ -41,6 +41,7 @@ struct StencilArgs {
     GridRed        red;
     int            red_site;
     int            wait_limit; // tensor-core operator: polls before a pipeline wait gives up (0: default)
+    int            wait_sleep_ns; // basis operator: consumers sleep this long between polls of D (0: spin)
     // several right-hand sides (multi-RHS operator): RHS k's fields at offset k * rhs_stride,
     // its scalars at scal[k]; active[k] == 0 skips it (null: all active)
     int            nrhs;

@@ -403,6 +403,12 @@ int fansgpu_set_refresh(fansgpu_ctx *ctx, double factor);
  * counterpart (the reference has no device work). */
 int fansgpu_set_wait_limit(fansgpu_ctx *ctx, int32_t polls);
 
+/* Diagnostics: the device's FP64 FMA rate (FMAs per second), measured by a
+ * short kernel of independent FMA chains on every SM of the current device.
+ * The FP64 solve path is bound by this rate, not by HBM; bench.py reports the
+ * FP64 operator's fraction of it.  No reference counterpart. */
+int fansgpu_fp64_fma_rate(double *dfma_per_s);
+
 /* Library version string. */
 const char *fansgpu_version(void);
 
