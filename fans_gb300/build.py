@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfans_gb300.so")
-SOURCES = ["k_stencil.cu", "k_stencil_tc.cu", "k_stencil_tcb.cu", "k_fft.cu", "k_fft_reg.cu", "k_vec.cu", "k_element.cu", "k_adjoint.cu", "capi.cu",
+SOURCES = ["k_stencil.cu", "k_stencil_tc.cu", "k_stencil_tcb.cu", "k_stencil_tcx.cu", "k_fft.cu", "k_fft_reg.cu", "k_vec.cu", "k_element.cu", "k_adjoint.cu", "capi.cu",
            "noalloc.cu", "k_diag.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]

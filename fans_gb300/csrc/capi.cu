@@ -160,6 +160,10 @@ struct fansgpu_ctx {
     float *Wtb = nullptr, *coef_tb = nullptr;
     int    tb_nb = 0;
     bool   use_tcb = false;
+    // FP64-accurate basis operator on the tensor cores (k_stencil_tcx): double-float coefficients
+    float *coef_tx  = nullptr;
+    bool   use_tcx  = false;
+    bool   exact_tc = true; // FANSGPU_EXACT=df: the CUDA-core double-float kernel instead
     bool   tc_legacy = false; // FANSGPU_STENCIL=tc: the per-phase 3xTF32 operator instead
     bool   tuned      = false;
 };
@@ -489,10 +493,11 @@ int setup(fansgpu_ctx *ctx)
             FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Wtc, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, ctx->st));
             ctx->use_tc = true;
         }
-        // the basis operator: every phase an isotropic law of this problem, each basis block exact
+        // the basis operators: every phase an isotropic law of this problem, each basis block exact.
+        // k_stencil_tcb (FP32, mixed path) and k_stencil_tcx (FP64-accurate: true residual, FP64 CG)
         ctx->use_tcb = false;
-        if (ctx->tc_allowed && !ctx->tc_legacy && !ctx->tc_slower && ctx->desc.precision == FANSGPU_MIXED &&
-            ctx->nstr == (C == 1 ? 3 : 6)) {
+        ctx->use_tcx = false;
+        if (ctx->nstr == (C == 1 ? 3 : 6)) {
             const int iso = C == 1 ? FANSGPU_LAW_THERMAL_ISO : FANSGPU_LAW_ELASTIC_ISO, nb = C == 1 ? 1 : 2;
             bool      ok  = stencil_tcb_supported(ctx->g, C, nb, ctx->nph);
             for (int ph = 0; ph < ctx->nph && ok; ++ph)
@@ -513,31 +518,38 @@ int setup(fansgpu_ctx *ctx)
             if (ok)
                 ok = stencil_tcb_quanta(C, Kb.data(), nb, q.data());
             if (ok) {
-                std::vector<float> w(stencil_tcb_weights(C, nb)), cf((size_t)ctx->nph * nb);
+                std::vector<float> w(stencil_tcb_weights(C, nb)), cf((size_t)ctx->nph * nb),
+                    cfd((size_t)ctx->nph * nb * 2);
                 stencil_tcb_pack_weights(C, nb, Kb.data(), q.data(), w.data());
                 for (int ph = 0; ph < ctx->nph; ++ph) {
                     const std::vector<double> &pr = ctx->prm[ph];
-                    if (C == 1)
-                        cf[ph] = (float)(pr[0] * q[0]);
-                    else {
-                        cf[ph * 2 + 0] = (float)((pr[0] - 2.0 * pr[1] / 3.0) * q[0]); // lambda = K - 2G/3
-                        cf[ph * 2 + 1] = (float)(pr[1] * q[1]);                      // mu = G
+                    for (int b = 0; b < nb; ++b) {
+                        // lambda = K - 2G/3, mu = G (LinearElastic.h:24); conductivity as given
+                        const double c = C == 1 ? pr[0] * q[0] : (b == 0 ? (pr[0] - 2.0 * pr[1] / 3.0) * q[0] : pr[1] * q[1]);
+                        cf[ph * nb + b]            = (float)c;
+                        cfd[(ph * nb + b) * 2]     = (float)c; // double-float pair
+                        cfd[(ph * nb + b) * 2 + 1] = (float)(c - (double)(float)c);
                     }
                 }
-                for (float *p : {ctx->Wtb, ctx->coef_tb})
+                for (float *p : {ctx->Wtb, ctx->coef_tb, ctx->coef_tx})
                     if (p)
                         cudaFree(p);
-                ctx->Wtb = ctx->coef_tb = nullptr;
+                ctx->Wtb = ctx->coef_tb = ctx->coef_tx = nullptr;
                 int rc5;
-                if ((rc5 = dalloc(ctx, &ctx->Wtb, w.size())) || (rc5 = dalloc(ctx, &ctx->coef_tb, cf.size())))
+                if ((rc5 = dalloc(ctx, &ctx->Wtb, w.size())) || (rc5 = dalloc(ctx, &ctx->coef_tb, cf.size())) ||
+                    (rc5 = dalloc(ctx, &ctx->coef_tx, cfd.size())))
                     return rc5;
                 FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->Wtb, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice,
                                                 ctx->st));
                 FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->coef_tb, cf.data(), sizeof(float) * cf.size(),
                                                 cudaMemcpyHostToDevice, ctx->st));
-                FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st)); // w and cf are host temporaries
+                FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->coef_tx, cfd.data(), sizeof(float) * cfd.size(),
+                                                cudaMemcpyHostToDevice, ctx->st));
+                FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st)); // host temporaries
                 ctx->tb_nb   = nb;
-                ctx->use_tcb = true;
+                ctx->use_tcb = ctx->tc_allowed && !ctx->tc_legacy && !ctx->tc_slower &&
+                               ctx->desc.precision == FANSGPU_MIXED;
+                ctx->use_tcx = ctx->exact_tc && stencil_tcx_supported(ctx->g, C, nb, ctx->nph);
             }
         }
         {
@@ -653,6 +665,21 @@ int run_residual_df(fansgpu_ctx *ctx)
 {
     if (ctx->u_zero)
         return run_stencil<double>(ctx, ctx->u, ctx->r, true); // r = F, no arithmetic on u
+    if (ctx->use_tcx) { // the same, with the products on the tensor cores
+        StencilArgs a{};
+        a.g          = ctx->g;
+        a.C          = ctx->C;
+        a.x          = ctx->u;
+        a.y          = ctx->r;
+        a.ms         = ctx->d_ms;
+        a.nph        = ctx->nph;
+        a.scal       = ctx->scal + ctx->cur;
+        a.wait_limit = ctx->tc_wait_limit;
+        int e0       = tk_mark(ctx);
+        FANS_CUDA_CHECK(launch_stencil_tcx(a, ctx->Wtb, ctx->coef_tx, ctx->fdf, ctx->tb_nb, ctx->st));
+        tk_span(ctx, FANSGPU_K_RESIDUAL, e0, tk_mark(ctx));
+        return 0;
+    }
     StencilArgs a{};
     a.g        = ctx->g;
     a.C        = ctx->C;
@@ -830,6 +857,12 @@ int solve_cg64(fansgpu_ctx *ctx)
                 return rc;
             FANS_CUDA_CHECK(launch_dot(dn, ctx->Kd, n, &ctx->scal->dAd, ctx->red, SITE_DOT, ctx->st));
             FANS_CUDA_CHECK(launch_set_alpha(ctx->scal, ctx->st));
+        } else if (df && ctx->use_tcx) {
+            // d = s + beta d_old, K d FP64-accurate with the products on the tensor cores, <d, K d>, alpha
+            sa.wait_limit = ctx->tc_wait_limit;
+            int e0        = tk_mark(ctx);
+            FANS_CUDA_CHECK(launch_stencil_tcx(sa, ctx->Wtb, ctx->coef_tx, nullptr, ctx->tb_nb, ctx->st));
+            tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
         } else if (df) {
             // d = s + beta d_old, K d in double-float on the FP32 pipes (GB300's FP64 rate is about
             // 1/60 of its FP32 rate), <d, K d> and alpha in FP64
@@ -853,6 +886,9 @@ int solve_cg64(fansgpu_ctx *ctx)
             return rc;
         ctx->iter++;
         ctx->err_all.push_back(ctx->scal_h->err);
+        if (ctx->scal_h->converged == -3)
+            return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out at iteration %d",
+                        ctx->iter);
         if (ctx->scal_h->converged < 0)
             return fail(ctx, FANSGPU_ENAN, "non-finite residual norm at iteration %d", ctx->iter);
         err_rel = err_value(ctx, ctx->scal_h->err);
@@ -1287,6 +1323,8 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     tk_span(ctx, FANSGPU_K_NORM, en, tk_mark(ctx)); }
             if ((rc = sync_scalars(ctx)))
                 return rc;
+            if (ctx->scal_h->converged == -3)
+                return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out (true residual)");
             (*refinements)++;
             last_true = ctx->scal_h->err;
             ctx->err_all.push_back(last_true);
@@ -1372,6 +1410,8 @@ int solve_cg_mixed_rhs(fansgpu_ctx *ctx, int only)
     for (int k = 0; k < R; ++k) {
         if (!mine(k))
             continue;
+        if (ctx->scal_h[k].converged == -3)
+            return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out (true residual)");
         const double err = ctx->scal_h[k].err;
         ctx->rhs_err[k].assign(1, err);
         ctx->rhs_iter[k] = 0;
@@ -1470,6 +1510,8 @@ int solve_cg_mixed_rhs(fansgpu_ctx *ctx, int only)
         if (!due.empty() && (rc = sync_scalars_rhs(ctx)))
             return rc;
         for (int k : due) {
+            if (ctx->scal_h[k].converged == -3)
+                return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out (true residual)");
             ctx->rhs_ref[k]++;
             last_true[k]     = ctx->scal_h[k].err;
             ctx->rhs_err[k].push_back(last_true[k]);
@@ -1823,6 +1865,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
                 ctx->tune_force[k] = ev[k] - '0';
         }
     }
+    if (const char *ev = std::getenv("FANSGPU_EXACT")) // "df": FP64-accurate products on the CUDA cores
+        ctx->exact_tc = std::strcmp(ev, "df") != 0;
     if (const char *ev = std::getenv("FANSGPU_FP64_OPERATOR")) // "dfma": the FP64 CG operator on the FP64 pipe
         ctx->fp64_df = std::strcmp(ev, "dfma") != 0;
     if (const char *ev = std::getenv("FANSGPU_TC_BACKOFF")) // ns between the operator consumers' polls
@@ -1964,7 +2008,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
     if (ctx->st)
         cudaStreamSynchronize(ctx->st);
     void *ptrs[] = {ctx->d_ms, ctx->u0,   ctx->r0,     ctx->s,      ctx->dd[0],  ctx->dd[1],      ctx->Kd,
-                    ctx->up0,  ctx->act,  ctx->ctlr,   ctx->Wtb,    ctx->coef_tb, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
+                    ctx->up0,  ctx->act,  ctx->ctlr,   ctx->Wtb,    ctx->coef_tb, ctx->coef_tx, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
                     ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d, ctx->Bb_d,

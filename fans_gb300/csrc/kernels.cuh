@@ -102,6 +102,14 @@ size_t      stencil_tcb_weights(int C, int nb);
 void        stencil_tcb_pack_weights(int C, int nb, const double *Kb, const double *q, float *out);
 cudaError_t launch_stencil_tcb(const StencilArgs &a, const float *W, const float *coef, int nb, cudaStream_t st);
 
+// FP64-accurate y = K x (+ F) on the tensor cores (the exact basis W of the operator above, the
+// element rows as three exact fixed-point tf32 slices, double-float epilogue): a.x FP64 (or with
+// fuse_d d = s + beta d_old, written to d_new), a.y FP64, optional <x, y> -> scal (dAd, alpha).
+// coef_df: nph x nb (hi, lo) FP32 pairs; f_df: [hi | lo] nph x 8C element forces, or null.
+bool        stencil_tcx_supported(const Grid3 &g, int C, int nb, int nph);
+cudaError_t launch_stencil_tcx(const StencilArgs &a, const float *W, const float *coef_df, const float *f_df, int nb,
+                               cudaStream_t st);
+
 // -------------------------------------------------------- element kernels ---
 enum ElemMode { ELEM_RESIDUAL = 0, ELEM_AVERAGES = 1 };
 struct ElementArgs {
