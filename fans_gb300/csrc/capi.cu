@@ -661,7 +661,8 @@ int run_stencil(fansgpu_ctx *ctx, const T *x, T *y, bool with_f)
 }
 
 // r = R(u) = K u + F with FP64 accuracy from FP32 arithmetic (mixed-path refresh).
-int run_residual_df(fansgpu_ctx *ctx)
+// A tensor-core wait timeout is reported in scal->converged (-3).
+int run_residual_df(fansgpu_ctx *ctx, CgScalars *scal)
 {
     if (ctx->u_zero)
         return run_stencil<double>(ctx, ctx->u, ctx->r, true); // r = F, no arithmetic on u
@@ -673,7 +674,7 @@ int run_residual_df(fansgpu_ctx *ctx)
         a.y          = ctx->r;
         a.ms         = ctx->d_ms;
         a.nph        = ctx->nph;
-        a.scal       = ctx->scal + ctx->cur;
+        a.scal       = scal;
         a.wait_limit = ctx->tc_wait_limit;
         int e0       = tk_mark(ctx);
         FANS_CUDA_CHECK(launch_stencil_tcx(a, ctx->Wtb, ctx->coef_tx, ctx->fdf, ctx->tb_nb, ctx->st));
@@ -813,7 +814,7 @@ int solve_cg64(fansgpu_ctx *ctx)
         return rc;
     // r = R(u) (compute_residual<2>, solverCG.h:76)
     const bool df = ctx->fp64_df && ctx->all_linear && !ctx->vscale; // FP64-accurate operator off the FP64 pipe
-    if ((rc = df ? run_residual_df(ctx) : run_residual64(ctx, ctx->u, ctx->r)))
+    if ((rc = df ? run_residual_df(ctx, ctx->scal) : run_residual64(ctx, ctx->u, ctx->r)))
         return rc;
     { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm<double, float>(ctx->r, n, ctx->tol.measure, ctx->scal, 1, nullptr, ctx->red,
@@ -823,6 +824,8 @@ int solve_cg64(fansgpu_ctx *ctx)
         return rc;
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
+    if (ctx->scal_h->converged == -3)
+        return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out (initial residual)");
     if (!std::isfinite(ctx->scal_h->err))
         return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm (e.g. det F <= 0 in CompressibleNeoHookean)");
     double err_rel = err_value(ctx, ctx->scal_h->err);
@@ -1242,7 +1245,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
     ctx->cur_d = 0;
     if ((rc = init_scalars(ctx)))
         return rc;
-    if ((rc = run_residual_df(ctx)))
+    if ((rc = run_residual_df(ctx, ctx->scal)))
         return rc;
     { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm_fast(ctx->r, n, ctx->tol.measure, ctx->scal, 1, ctx->r32, ctx->red,
@@ -1252,6 +1255,8 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
         return rc;
     ctx->iter = 0;
     ctx->err_all.assign(1, ctx->scal_h->err);
+    if (ctx->scal_h->converged == -3)
+        return fail(ctx, FANSGPU_ECUDA, "tensor-core operator: MMA completion wait timed out (initial residual)");
     if (!std::isfinite(ctx->scal_h->err))
         return fail(ctx, FANSGPU_ENAN, "non-finite initial residual norm (e.g. det F <= 0 in CompressibleNeoHookean)");
     *refinements      = 0;
@@ -1315,7 +1320,7 @@ int solve_cg_mixed(fansgpu_ctx *ctx, int *refinements)
             // FP64, re-seed the FP32 residual
             FANS_CUDA_CHECK(launch_fold(ctx->u, ctx->e32, n, ctx->st));
             ctx->u_zero = false;
-            if ((rc = run_residual_df(ctx)))
+            if ((rc = run_residual_df(ctx, ctx->scal)))
                 return rc;
             { int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm_fast(ctx->r, n, ctx->tol.measure, ctx->scal, 0, ctx->r32,
@@ -1355,7 +1360,7 @@ int refresh_rhs(fansgpu_ctx *ctx, int k, bool fold, bool set_err0)
         ctx->u_zero       = false;
         ctx->rhs_uzero[k] = 0;
     }
-    if ((rc = run_residual_df(ctx)))
+    if ((rc = run_residual_df(ctx, ctx->scal + k)))
         return rc;
     int en = tk_mark(ctx);
     FANS_CUDA_CHECK(launch_norm_fast(ctx->r, n, ctx->tol.measure, ctx->scal + k, set_err0 ? 1 : 0,
@@ -2126,9 +2131,11 @@ int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out)
         return rc;
     const ConvPlan<double> &a = ctx->cp64;
     const ConvPlan<float>  &b = ctx->cp32;
-    const int32_t v[7] = {a.var_z, a.var_y, a.var_x, b.var_z, b.var_y, b.var_x,
-                         ctx->use_tcb ? 2 : ctx->use_tc ? 1 : 0};
-    for (int k = 0; k < 7; ++k)
+    // the FP64-accurate operator: of the FP64 CG iterations, else of the mixed path's true residual
+    const bool fp64_pipe = ctx->desc.precision != FANSGPU_MIXED && !(ctx->fp64_df && ctx->all_linear && !ctx->vscale);
+    const int32_t v[8] = {a.var_z, a.var_y, a.var_x, b.var_z, b.var_y, b.var_x,
+                         ctx->use_tcb ? 2 : ctx->use_tc ? 1 : 0, fp64_pipe ? 0 : ctx->use_tcx ? 2 : 1};
+    for (int k = 0; k < 8; ++k)
         out[k] = v[k];
     return 0;
 }

@@ -58,8 +58,8 @@ enum {
     BAR_STAGED = 3,
     BAR_SFREE  = 3 + R,
     BAR_DRAIN  = 3 + 2 * R,
-    BAR_INV    = 4 + 2 * R, // the element scales of a plane written (producers -> consumers)
-    NBAR       = 5 + 2 * R
+    BAR_INV    = 4 + 2 * R, // + (plane & 1): the element scales of a plane written (producers -> consumers)
+    NBAR       = 6 + 2 * R
 };
 
 template <int C, int NB>
@@ -232,6 +232,7 @@ __global__ void __maxnreg__(112)
         }
         mbar_init(bar(BAR_DRAIN), 1);
         mbar_init(bar(BAR_INV), NGRP);
+        mbar_init(bar(BAR_INV + 1), NGRP);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -388,7 +389,7 @@ __global__ void __maxnreg__(112)
             }
             // the MMAs read A through the async proxy
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(bar(BAR_INV));
+            mbar_arrive(bar(BAR_INV + (j & 1)));
             mbar_arrive(bar(BAR_AFULL));
         }
     } else if (warp < 8) {
@@ -422,7 +423,10 @@ __global__ void __maxnreg__(112)
             mbar_wait(bar(BAR_DFULL), (uint32_t)(j & 1), abort_flag, wlim);
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            mbar_wait(bar(BAR_INV), (uint32_t)(j & 1), abort_flag, wlim);
+            // one barrier per scale buffer: the producers can complete plane j+1's
+            // arrival before this wait, but not plane j+2's (that needs this
+            // plane's DFREE), so the parity of a buffer's barrier never aliases
+            mbar_wait(bar(BAR_INV + b), (uint32_t)((j >> 1) & 1), abort_flag, wlim);
             const float inv = Inv[b * NEL + ey * 32 + ez];
             float       oh[NCOL], ol[NCOL]; // K_ph u_e (+ f_ph) in double-float
 #pragma unroll

@@ -198,11 +198,13 @@ class Context:
         self._chk(self.lib.fansgpu_set_wait_limit(self.ctx, int(polls)))
 
     def tuning(self):
-        """fansgpu_tuning: {"fp64": (z, y, x), "fp32": (z, y, x), "tensor_core": bool}."""
-        out = np.zeros(7, dtype=np.int32)
+        """fansgpu_tuning: {"fp64": (z, y, x), "fp32": (z, y, x), "tensor_core": bool,
+        "operator": "cuda" | "tc" | "tc_basis", "exact_operator": "fp64" | "df" | "tc_slices"}."""
+        out = np.zeros(8, dtype=np.int32)
         self._chk(self.lib.fansgpu_tuning(self.ctx, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
         return {"fp64": tuple(int(v) for v in out[:3]), "fp32": tuple(int(v) for v in out[3:6]),
-                "tensor_core": bool(out[6])}
+                "tensor_core": bool(out[6]), "operator": ("cuda", "tc", "tc_basis")[int(out[6])],
+                "exact_operator": ("fp64", "df", "tc_slices")[int(out[7])]}
 
     def set_timing(self, on=True):
         self._chk(self.lib.fansgpu_set_timing(self.ctx, int(bool(on))))

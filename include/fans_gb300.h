@@ -203,11 +203,14 @@ int fansgpu_enable_mixed_bc(fansgpu_ctx *ctx, int32_t n_e, const int32_t *idx_e,
 #define FANSGPU_VOXEL_YIELD_STRESS 1
 int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *values);
 
-/* The tile shapes the context's first setup chose (autotuned unless
- * FANSGPU_TUNE=0 or forced): out[0..2] = FP64 z, y, x pass variants, out[3..5]
- * the FP32 ones (0 = default tile, 1 = the smaller one), out[6] = 1 when the
- * mixed path runs the tensor-core operator.  New on the GPU path (FANS's FFTW
- * plans are chosen by FFTW_MEASURE, solver.h:221-222). */
+/* The tile shapes and operators the context's first setup chose (autotuned
+ * unless FANSGPU_TUNE=0 or forced), out[8]: out[0..2] = FP64 z, y, x pass
+ * variants, out[3..5] the FP32 ones (0 = default tile, 1 = the smaller one),
+ * out[6] = the mixed path's CG operator (0 CUDA cores, 1 per-phase tensor-core,
+ * 2 exact-basis tensor-core), out[7] = the FP64-accurate operator (the FP64 CG
+ * operator, and the mixed path's true residual: 0 FP64 pipe, 1 double-float on
+ * the CUDA cores, 2 exact fixed-point slices on the tensor cores).  New on the
+ * GPU path (FANS's FFTW plans are chosen by FFTW_MEASURE, solver.h:221-222). */
 int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out);
 
 /* Adjoint of the homogenized stiffness w.r.t. the per-voxel scale.  After

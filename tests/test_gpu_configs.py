@@ -70,3 +70,38 @@ def test_elastic_128_fp64_and_mixed_match_oracle():
     assert np.linalg.norm(C_mix - C_ref) / np.linalg.norm(C_ref) < 1e-6
     print(f"elastic 128^3: |C_fp64 - C_oracle| {rel(C64, C_ref):.2e}, "
           f"|C_mixed - C_oracle| / |C_oracle| {np.linalg.norm(C_mix - C_ref) / np.linalg.norm(C_ref):.2e}")
+
+
+def test_elastic_256_multi_rhs_matches_oracle_fixture():
+    """The headline workload (256^3, seed 0, r 6, vf 0.30, six unit loads, rel. L2
+    1e-8) as one multi-RHS mixed-precision solve: C_eff within 1e-6 of the FP64
+    oracle's complete solve (tests/golden/elastic256_ceff.json, made by
+    tests/golden/make_workload_fixtures.py), each load case within +-1 of the
+    oracle's iteration count."""
+    import json
+    import os
+
+    from fans_gb300 import Context
+    from fans_gb300.microstructure import spheres
+
+    fx = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "elastic256_ceff.json")))
+    ms, _ = spheres(256, 6, 0.30, 0)
+    assert abs(ms.mean() - fx["vf"]) < 1e-12
+    P = oracle_problem(ms[:4, :4, :4].astype(np.uint16), 3, ELASTIC, "HEX8")  # the reference-stiffness rule only
+    ctx = Context((256, 256, 256), (1.0, 1.0, 1.0), 3, "HEX8", "mixed", "cg", n_rhs=6)
+    ctx.set_microstructure(ms)
+    for ph in range(2):
+        ctx.set_phase_material(ph, int(P.law[ph]), P.param[ph, :2])
+    ctx.set_reference(P.kapparef)
+    ctx.set_tolerance("L2", "relative", 1e-8, 2000)
+    ctx.set_gradients(np.eye(6))
+    assert ctx.solve()["converged"]
+    its = [ctx.rhs_stats(k)["iterations"] for k in range(6)]
+    C = ctx.homogenized_stresses().T
+    ctx.close()
+    Cf = np.array(fx["C_eff_columns"])
+    C, Cf = 0.5 * (C + C.T), 0.5 * (Cf + Cf.T)
+    err = np.linalg.norm(C - Cf) / np.linalg.norm(Cf)
+    assert err < 1e-6, err
+    assert all(abs(a - b) <= 1 for a, b in zip(its, fx["iterations"])), (its, fx["iterations"])
+    print(f"elastic 256^3 multi-RHS: |C - C_oracle| / |C_oracle| = {err:.2e}, iterations {its}")
