@@ -499,7 +499,7 @@ int setup(fansgpu_ctx *ctx)
         ctx->use_tcx = false;
         if (ctx->nstr == (C == 1 ? 3 : 6)) {
             const int iso = C == 1 ? FANSGPU_LAW_THERMAL_ISO : FANSGPU_LAW_ELASTIC_ISO, nb = C == 1 ? 1 : 2;
-            bool      ok  = stencil_tcb_supported(ctx->g, C, nb, ctx->nph);
+            bool      ok  = ctx->nph >= 1 && ctx->nph <= 256;
             for (int ph = 0; ph < ctx->nph && ok; ++ph)
                 ok = ctx->law[ph] == iso;
             // basis constitutive matrices: conduction I; elasticity 1 1^T (lambda) and 2 I (mu),
@@ -548,7 +548,7 @@ int setup(fansgpu_ctx *ctx)
                 FANS_CUDA_CHECK(cudaStreamSynchronize(ctx->st)); // host temporaries
                 ctx->tb_nb   = nb;
                 ctx->use_tcb = ctx->tc_allowed && !ctx->tc_legacy && !ctx->tc_slower &&
-                               ctx->desc.precision == FANSGPU_MIXED;
+                               ctx->desc.precision == FANSGPU_MIXED && stencil_tcb_supported(ctx->g, C, nb, ctx->nph);
                 ctx->use_tcx = ctx->exact_tc && stencil_tcx_supported(ctx->g, C, nb, ctx->nph);
             }
         }

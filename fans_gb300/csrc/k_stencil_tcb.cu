@@ -25,8 +25,10 @@
 //
 // Tiling, roles and hand-over follow the single-RHS tensor-core operator
 // (k_stencil_tc.cu): a CTA owns a 3 (y) x 31 (z) node column, one element plane
-// of which is one M-tile; producers stage node planes (cp.async three planes
-// ahead) and build A in tensor memory, one thread issues the MMAs, consumers
+// of which is one M-tile; producers stage node planes (16-byte cp.async chunks of
+// z-aligned node rows, three planes ahead; d = s + beta d_old four nodes at a
+// time with packed FP32x2 arithmetic) and build A in tensor memory, one thread
+// issues the MMAs, consumers
 // read D and sum element rows into nodes without atomics (register carry in x,
 // a warp shuffle in z, an exchange buffer in y).  Every mbarrier wait is bounded;
 // an expired wait sets an abort flag that releases the others, the issuer waits
@@ -35,6 +37,7 @@
 #include "kernels.cuh"
 
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 
 namespace fansgpu {
@@ -42,15 +45,18 @@ namespace fansgpu {
 namespace {
 
 constexpr int BY = 3, BZ = 31;
-constexpr int PY = BY + 2, PZ = BZ + 2;
+constexpr int PY = BY + 2; // node rows of a column plane (halo included)
 constexpr int EYN = BY + 1, EZN = BZ + 1;
 constexpr int NEL = EYN * EZN; // 128 elements = one M-tile
 constexpr int NGRP = 128;
 constexpr int TPB  = 2 * NGRP + 32;
-constexpr int NPL  = PY * PZ; // 165 nodes per plane incl. halo
 constexpr int XL   = 64;
 constexpr int R    = 4; // node-plane slots
 constexpr int RAWD = 4; // raw (s, d_old) planes in flight
+// A node plane of the column is held as PY rows of ZR floats: the nodes from the 16-byte
+// aligned z = za on (at most ZMAIN of them), then the periodic neighbours z = nz-4..nz-1
+// (columns ZMAIN..ZMAIN+3) and z = 0..3 (ZMAIN+4..ZMAIN+7); rows move as 16-byte chunks.
+constexpr int ZMAIN = 40, ZR = 48, CPRMAX = ZMAIN / 4 + 2;
 constexpr int TCOLS = 128, COL_LO = 32, COL_A = 0, COL_D = 64;
 constexpr int SMEM_REQ = 64 * 1024; // three CTAs per SM
 constexpr unsigned kWaitLimit  = 1u << 22;
@@ -77,13 +83,14 @@ struct TbCfg {
     static constexpr int NW      = (NROW + 15) / 16 * 16;
     static constexpr int KSTEPS  = NCOL / 8;
     static constexpr int W_BYTES = NW * NCOL * 4;
-    static constexpr int NPF     = (C * NPL + NGRP - 1) / NGRP;
+    static constexpr int ROWF    = C * PY * ZR;                        // floats of one node plane
+    static constexpr int NCH     = (C * PY * CPRMAX + NGRP - 1) / NGRP; // 16-byte chunks per producer
     static constexpr int al(int b) { return (b + 127) / 128 * 128; }
     static constexpr int OFF_W    = 0;
     static constexpr int OFF_COEF = al(OFF_W + W_BYTES);                 // [kMaxPh][NB] float
-    static constexpr int OFF_D    = al(OFF_COEF + kMaxPh * NB * 4);      // [R][C][NPL]
-    static constexpr int OFF_RAW  = al(OFF_D + R * C * NPL * 4);         // [RAWD][s, d_old][C][NPL]
-    static constexpr int OFF_X    = al(OFF_RAW + RAWD * 2 * C * NPL * 4); // [2][EYN][C][32]
+    static constexpr int OFF_D    = al(OFF_COEF + kMaxPh * NB * 4);      // [R][C][PY][ZR]
+    static constexpr int OFF_RAW  = al(OFF_D + R * ROWF * 4);            // [RAWD][s, d_old][C][PY][ZR]
+    static constexpr int OFF_X    = al(OFF_RAW + RAWD * 2 * ROWF * 4);   // [2][EYN][C][32]
     static constexpr int OFF_BAR  = al(OFF_X + 2 * EYN * C * 32 * 4);     // NBAR mbarriers, tmem slot, abort flag
     static constexpr int OFF_ACT  = OFF_BAR + NBAR * 8 + 8;              // active RHS list + count
     static constexpr int OFF_BETA = OFF_ACT + (kMaxRhs + 1) * 4;         // beta of each active RHS (float)
@@ -198,7 +205,7 @@ __global__ void __launch_bounds__(TPB, 3)
     k_stencil_tcb(StencilArgs a, const float *__restrict__ Wg, const float *__restrict__ coefg)
 {
     using Cfg = TbCfg<C, NB>;
-    constexpr int NCOL = Cfg::NCOL, NPF = Cfg::NPF;
+    constexpr int NCOL = Cfg::NCOL, NCH = Cfg::NCH, ROWF = Cfg::ROWF;
     extern __shared__ __align__(16) unsigned char smem[];
     float        *Dp         = reinterpret_cast<float *>(smem + Cfg::OFF_D);
     float        *Xch        = reinterpret_cast<float *>(smem + Cfg::OFF_X);
@@ -269,40 +276,67 @@ __global__ void __launch_bounds__(TPB, 3)
         const float *dold = reinterpret_cast<const float *>(a.d_old);
         float       *dnew = reinterpret_cast<float *>(a.d_new);
         const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-        long long goff[NPF];
-        int       loff[NPF];
-        unsigned  owned_mask = 0, valid_mask = 0;
+        // the column's node rows in z: from za (16-byte aligned) on, zlen nodes, plus the wrap chunks
+        const int  za   = z0 == 0 ? 0 : ((z0 - 1) & ~3);
+        const int  zlen = min(ZMAIN, nz - za);
+        const bool wlo = z0 == 0, whi = z0 + BZ >= nz;
+        const int  cpr  = zlen / 4 + (wlo ? 1 : 0) + (whi ? 1 : 0); // chunks per row
+        // node z of the column -> its row column (rows past nz only feed elements outside the grid)
+        auto zcol = [&](int z) { return z < 0 ? ZMAIN + 3 : (z >= nz ? ZMAIN + 4 + min(z - nz, 3) : z - za); };
+        // this thread's 16-byte chunks of a node plane (row (c, hy), 4 nodes): global offset of
+        // the row chunk, offset in a plane's rows, and which of its 4 nodes this CTA owns
+        long long goff[NCH];
+        int       soff[NCH];
+        unsigned  omask[NCH];
+        unsigned  valid_mask = 0;
 #pragma unroll
-        for (int k = 0; k < NPF; ++k) {
-            const int idx = tid + k * NGRP;
-            goff[k] = 0;
-            loff[k] = 0;
-            if (idx < C * NPL) {
-                const int c = idx / NPL, rem = idx % NPL, hy = rem / PZ, hz = rem % PZ;
-                const int y = y0 - 1 + hy, z = z0 - 1 + hz;
-                goff[k] = c * N + (long long)pmod(y, ny) * nz + pmod(z, nz);
-                loff[k] = c * NPL + rem;
+        for (int k = 0; k < NCH; ++k) {
+            const int q = tid + k * NGRP;
+            goff[k]  = 0;
+            soff[k]  = 0;
+            omask[k] = 0;
+            if (q < C * PY * cpr) {
+                const int row = q / cpr, h = q % cpr, c = row / PY, hy = row % PY;
+                const int y   = y0 - 1 + hy;
+                int zsrc, col;
+                if (h < zlen / 4) {
+                    zsrc = za + 4 * h;
+                    col  = 4 * h;
+                } else if (wlo && h == zlen / 4) {
+                    zsrc = nz - 4;
+                    col  = ZMAIN;
+                } else {
+                    zsrc = 0;
+                    col  = ZMAIN + 4;
+                }
+                goff[k] = c * N + (long long)pmod(y, ny) * nz + zsrc;
+                soff[k] = (c * PY + hy) * ZR + col;
                 valid_mask |= 1u << k;
-                if (hy >= 1 && hy <= BY && hz >= 1 && hz <= BZ && y < ny && z < nz)
-                    owned_mask |= 1u << k;
+                if (col < ZMAIN && hy >= 1 && hy <= BY && y < ny)
+                    for (int i = 0; i < 4; ++i) {
+                        const int z = zsrc + i;
+                        if (z >= z0 && z < z0 + BZ && z < nz)
+                            omask[k] |= 1u << i;
+                    }
             }
         }
         // node plane g = (segment kk, plane m) with g = kk (J+1) + m: s and d_old of its RHS
         // copied into raw slot g % RAWD, RAWD-1 planes ahead of their use.  fetch and stage
-        // walk the node planes in order, each with its own (kk, m) counter.
+        // walk the node planes in order, each with its own (kk, m) counter.  A thread stages
+        // exactly the chunks it fetched, so its own cp.async wait orders them.
         int fk = 0, fm = 0, fg = 0; // next node plane to fetch
         auto fetch_next = [&]() {
             if (fg < nG) {
                 const long long off = (long long)s_act[fk] * rstr + (long long)wrapi(xs - 1 + fm, nx) * plane;
-                float          *raw = Raw + (fg % RAWD) * 2 * C * NPL;
+                const uint32_t  raw = smem_u32(Raw + (fg % RAWD) * 2 * ROWF);
 #pragma unroll
-                for (int k = 0; k < NPF; ++k)
+                for (int k = 0; k < NCH; ++k)
                     if (valid_mask & (1u << k)) {
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(raw + loff[k])),
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(raw + 4u * (uint32_t)soff[k]),
                                      "l"(sin + off + goff[k])
                                      : "memory");
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                                         smem_u32(raw + C * NPL + loff[k])),
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                                         raw + 4u * (uint32_t)(ROWF + soff[k])),
                                      "l"(dold + off + goff[k])
                                      : "memory");
                     }
@@ -323,15 +357,29 @@ __global__ void __launch_bounds__(TPB, 3)
             const bool      owned_x = X >= xs && X < xe;
             const long long off     = (long long)rk * rstr + (long long)wrapi(X, nx) * plane;
             const float     beta    = s_beta[sk];
-            const float    *raw     = Raw + (sg % RAWD) * 2 * C * NPL;
-            float          *slot    = Dp + (sg % R) * C * NPL;
+            const float2    b2      = make_float2(beta, beta);
+            const float    *raw     = Raw + (sg % RAWD) * 2 * ROWF;
+            float          *slot    = Dp + (sg % R) * ROWF;
 #pragma unroll
-            for (int k = 0; k < NPF; ++k)
+            for (int k = 0; k < NCH; ++k)
                 if (valid_mask & (1u << k)) {
-                    const float v = raw[loff[k]] + beta * raw[C * NPL + loff[k]];
-                    slot[loff[k]] = v;
-                    if (owned_x && (owned_mask & (1u << k)))
-                        dnew[off + goff[k]] = v;
+                    const float4 sv = *reinterpret_cast<const float4 *>(raw + soff[k]);
+                    const float4 dv = *reinterpret_cast<const float4 *>(raw + ROWF + soff[k]);
+                    const float2 v0 = __ffma2_rn(b2, make_float2(dv.x, dv.y), make_float2(sv.x, sv.y));
+                    const float2 v1 = __ffma2_rn(b2, make_float2(dv.z, dv.w), make_float2(sv.z, sv.w));
+                    const float4 v  = make_float4(v0.x, v0.y, v1.x, v1.y);
+                    *reinterpret_cast<float4 *>(slot + soff[k]) = v;
+                    if (owned_x && omask[k]) {
+                        float *dst = dnew + off + goff[k];
+                        if (omask[k] == 0xFu) {
+                            *reinterpret_cast<float4 *>(dst) = v;
+                        } else {
+                            if (omask[k] & 1u) dst[0] = v.x;
+                            if (omask[k] & 2u) dst[1] = v.y;
+                            if (omask[k] & 4u) dst[2] = v.z;
+                            if (omask[k] & 8u) dst[3] = v.w;
+                        }
+                    }
                 }
             mbar_arrive(bar(BAR_STAGED + sg % R));
             ++sg;
@@ -346,6 +394,11 @@ __global__ void __launch_bounds__(TPB, 3)
             stage_next(); // node plane 0
             fetch_next();
         }
+        // this element's nodes (ey + qb, ez + qc) in a plane's rows
+        int noff[4];
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq)
+            noff[qq] = (ey + (qq >> 1)) * ZR + zcol(z0 - 1 + ez + (qq & 1));
         int kk = 0, j = 0; // segment and element plane of unit U
         for (int U = 0; U < nU; ++U, j = (j + 1 == J) ? 0 : j + 1, kk += (j == 0)) {
             const int g0 = kk * (J + 1) + j; // near-x node plane of element plane j
@@ -360,24 +413,31 @@ __global__ void __launch_bounds__(TPB, 3)
                 mbar_wait(bar(BAR_DFULL), (uint32_t)((U - 1) & 1), abort_flag, wlim);
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const float *P0 = Dp + (g0 % R) * C * NPL, *P1 = Dp + ((g0 + 1) % R) * C * NPL;
-            float u0[C], v[NCOL];
+            const float *P0 = Dp + (g0 % R) * ROWF, *P1 = Dp + ((g0 + 1) % R) * ROWF;
+            float u0[C], w[NCOL];
 #pragma unroll
             for (int c = 0; c < C; ++c)
-                u0[c] = P0[c * NPL + ey * PZ + ez];
+                u0[c] = P0[c * PY * ZR + noff[0]];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int qa = q & 1, qb = (q >> 1) & 1, qc = (q >> 2) & 1;
                 const float *P = qa ? P1 : P0;
 #pragma unroll
                 for (int c = 0; c < C; ++c)
-                    v[q * C + c] = P[c * NPL + (ey + qb) * PZ + ez + qc] - u0[c];
+                    w[q * C + c] = P[c * PY * ZR + noff[qb * 2 + qc]];
             }
+            // differences to the first node, then hi (tf32 truncation) and lo = v - hi, two
+            // values per packed FP32x2 instruction
             float h[NCOL], l[NCOL];
+            const float2 m1 = make_float2(-1.f, -1.f);
 #pragma unroll
-            for (int k = 0; k < NCOL; ++k) {
-                h[k] = to_tf32(v[k]);
-                l[k] = v[k] - h[k];
+            for (int k = 0; k < NCOL; k += 2) {
+                const float2 v2 = __ffma2_rn(make_float2(u0[k % C], u0[(k + 1) % C]), m1, make_float2(w[k], w[k + 1]));
+                h[k]            = to_tf32(v2.x);
+                h[k + 1]        = to_tf32(v2.y);
+                const float2 l2 = __ffma2_rn(make_float2(h[k], h[k + 1]), m1, v2);
+                l[k]            = l2.x;
+                l[k + 1]        = l2.y;
             }
 #pragma unroll
             for (int k0 = 0; k0 < NCOL; k0 += 8) {
@@ -395,7 +455,9 @@ __global__ void __launch_bounds__(TPB, 3)
         float          *yout  = reinterpret_cast<float *>(a.y);
         const uint32_t  lane_base = tmem + ((uint32_t)(ey * 32) << 16);
         const bool      out_ok = ey >= 1 && ez >= 1 && y0 - 1 + ey < ny && z0 - 1 + ez < nz;
-        const int       onode  = ey * PZ + ez;
+        // this thread's node (ey, ez) in a plane's rows (16-byte aligned z from za on)
+        const int       za     = z0 == 0 ? 0 : ((z0 - 1) & ~3);
+        const int       onode  = ey * ZR + (z0 - 1 + ez - za);
         const long long oyz    = out_ok ? (long long)(y0 - 1 + ey) * nz + (z0 - 1 + ez) : 0;
         float carry[4 * C];
 #pragma unroll
@@ -420,20 +482,22 @@ __global__ void __launch_bounds__(TPB, 3)
                 mbar_wait(bar(BAR_DFULL), (uint32_t)(U & 1), abort_flag, wlim);
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float out[NCOL]; // K_ph u_e = sum_b cf_b D_b
+            float out[NCOL]; // K_ph u_e = sum_b cf_b D_b, two rows per packed FP32x2 instruction
 #pragma unroll
             for (int c0 = 0; c0 < Cfg::NW; c0 += 16) {
                 float vv[16];
                 tmem_ld16(lane_base + (uint32_t)(COL_D + c0), vv);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int jj = 0; jj < 16; ++jj) {
+                for (int jj = 0; jj < 16; jj += 2) { // NCOL is even: a pair never straddles two blocks
                     const int col = c0 + jj, bb = col / NCOL, r = col % NCOL;
                     if (col < Cfg::NROW) {
-                        if (bb == 0)
-                            out[r] = cf[0] * vv[jj];
-                        else
-                            out[r] = fmaf(cf[bb < NB ? bb : 0], vv[jj], out[r]);
+                        const float  c1 = cf[bb < NB ? bb : 0];
+                        const float2 v2 = make_float2(vv[jj], vv[jj + 1]);
+                        const float2 o2 = bb == 0 ? __fmul2_rn(make_float2(c1, c1), v2)
+                                                  : __ffma2_rn(make_float2(c1, c1), v2, make_float2(out[r], out[r + 1]));
+                        out[r]     = o2.x;
+                        out[r + 1] = o2.y;
                     }
                 }
             }
@@ -464,13 +528,13 @@ __global__ void __launch_bounds__(TPB, 3)
                 if (out_ok) {
                     const long long gi = (long long)s_act[kk] * rstr + (long long)wrapi(X, nx) * plane + oyz;
                     const float    *xr = Xch + (b * EYN + ey - 1) * C * 32 + ez;
-                    const float    *dp = Dp + (g0 % R) * C * NPL + onode;
+                    const float    *dp = Dp + (g0 % R) * ROWF + onode;
                     float           dl = 0.f;
 #pragma unroll
                     for (int c = 0; c < C; ++c) {
                         const float vo = Z[c] + xr[c * 32];
                         yout[c * N + gi] = vo;
-                        dl += dp[c * NPL] * vo;
+                        dl += dp[c * PY * ZR] * vo;
                     }
                     dot += dl;
                 }
@@ -622,14 +686,16 @@ void stencil_tcb_pack_weights(int C, int nb, const double *Kb, const double *q, 
 
 bool stencil_tcb_supported(const Grid3 &g, int C, int nb, int nph)
 {
+    // node rows move as 16-byte chunks: nz a multiple of 4 (every grid of the register FFT passes)
     return (C == 3 || C == 1) && nb >= 1 && nb <= 2 && nph >= 1 && nph <= kMaxPh && g.nx >= 2 && g.ny >= 2 &&
-           g.nz >= 2;
+           g.nz >= 4 && g.nz % 4 == 0;
 }
 
 cudaError_t launch_stencil_tcb(const StencilArgs &a, const float *W, const float *coef, int nb, cudaStream_t st)
 {
-    if (a.nrhs < 1 || a.nrhs > kMaxRhs)
-        return cudaErrorInvalidValue;
+    if (a.nrhs < 1 || a.nrhs > kMaxRhs || a.g.nz % 4 != 0 || a.rhs_stride % 4 != 0 || (uintptr_t)a.x % 16 != 0 ||
+        (uintptr_t)a.d_old % 16 != 0 || (uintptr_t)a.d_new % 16 != 0)
+        return cudaErrorInvalidValue; // 16-byte node-row chunks
     dim3 grid((a.g.nx + XL - 1) / XL, (a.g.ny + BY - 1) / BY, (a.g.nz + BZ - 1) / BZ);
 #define FANSGPU_TCB(C_, B_)                                                                                      \
     do {                                                                                                       \
