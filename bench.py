@@ -528,7 +528,9 @@ def main():
     dom = max((k for k in ktimes if ktimes[k][1] > 0 and abytes(k) is not None), key=lambda k: ktimes[k][0])
     avg_ms = ktimes[dom][0] / ktimes[dom][1]
     achieved = abytes(dom) / (avg_ms * 1e-3) / 1e9
-    traffic = traffic_table().get((dom, n, args.rhs))
+    traffic = traffic_table().get((dom, n, args.rhs))  # ncu bytes of a launch with every RHS active
+    if traffic is not None and dom in ITER_KERNELS:
+        traffic = round(traffic * r_avg / args.rhs)     # the average launch of the step
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 3), "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": int(abytes(dom)), "avg_launch_ms": round(avg_ms, 4),

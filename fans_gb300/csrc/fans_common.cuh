@@ -85,6 +85,17 @@ inline cudaError_t allow_max_dyn_smem(F *fn)
                                 smem_optin_max() - (int)fa.sharedSizeBytes);
 }
 
+// The same, and the largest shared-memory carveout, for kernels that need more than half
+// of an SM's shared memory per CTA to keep two CTAs resident.
+template <typename F>
+inline cudaError_t allow_max_dyn_smem_carveout(F *fn)
+{
+    cudaError_t e = allow_max_dyn_smem(fn);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute((const void *)fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
+}
+
 // Maxima that keep NaN (fmax returns the other operand), so that a non-finite
 // residual reaches the host through the Linfinity norm as well.
 __device__ __forceinline__ double nan_max(double a, double b) { return (a > b || a != a) ? a : b; }

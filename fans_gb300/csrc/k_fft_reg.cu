@@ -114,6 +114,17 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
 #pragma unroll
         for (int j2 = 0; j2 < N2; ++j2)
             v[j2] = valid ? gb[(w + N1 * j2) * xstride] : cplx<T>{0, 0};
+        {   // the next active RHS's column into L2 while this one is transformed
+            int kn = k + 1;
+            while (kn < p.nrhs && p.active && !p.active[kn])
+                ++kn;
+            if (kn < p.nrhs && valid) {
+                const cplx<T> *gn = gbase + kn * rhs_spec;
+#pragma unroll
+                for (int j2 = 0; j2 < N2; ++j2)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(gn + (w + N1 * j2) * xstride));
+            }
+        }
         line_phase1<T, N1, N2, false>(v, w, p.tw_x);
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2)

@@ -181,8 +181,10 @@ __device__ __forceinline__ void named_bar(int id, int nthreads)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// 96 registers: two CTAs of nine warps per SM need five warps' registers on one scheduler
+// (5 x 32 x 96 <= 16384); at 104-112 only one CTA was resident and the kernel ran 1.6x slower.
 template <int C, int NB>
-__global__ void __maxnreg__(112)
+__global__ void __maxnreg__(96)
     k_stencil_tcx(StencilArgs a, const float *__restrict__ Wg, const float *__restrict__ coefg,
                   const float *__restrict__ fg)
 {
@@ -594,7 +596,7 @@ cudaError_t launch_stencil_tcx(const StencilArgs &a, const float *W, const float
     dim3 grid((a.g.nx + XL - 1) / XL, (a.g.ny + BY - 1) / BY, (a.g.nz + BZ - 1) / BZ);
 #define FANSGPU_TCX(C_, B_)                                                                                      \
     do {                                                                                                       \
-        cudaError_t e = allow_max_dyn_smem(k_stencil_tcx<C_, B_>);                                             \
+        cudaError_t e = allow_max_dyn_smem_carveout(k_stencil_tcx<C_, B_>);                                             \
         if (e != cudaSuccess)                                                                                  \
             return e;                                                                                          \
         k_stencil_tcx<C_, B_><<<grid, TPB, SMEM_REQ, st>>>(a, W, coef_df, f_df);                                \
