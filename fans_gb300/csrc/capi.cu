@@ -997,7 +997,7 @@ struct TuneChoice {
     int tc_slower;
 };
 std::mutex                             g_tune_mu;
-std::map<std::array<int, 6>, TuneChoice> g_tune_cache;
+std::map<std::array<int, 7>, TuneChoice> g_tune_cache;
 
 float time_mixed_operator(fansgpu_ctx *ctx, bool tc)
 {
@@ -1049,8 +1049,10 @@ int autotune(fansgpu_ctx *ctx)
         apply(c);
         return 0;
     }
-    const std::array<int, 6> key{ctx->g.nx, ctx->g.ny, ctx->g.nz, ctx->C, ctx->desc.precision,
-                                 (ctx->use_tc ? 1 : 0) + 2 * (ctx->tune == 3)};
+    // the multi-RHS iteration runs every FFT pass over all right-hand sides: time the variants so
+    const int rhs_tuned = multi_rhs_path(ctx) ? ctx->nrhs : 1;
+    const std::array<int, 7> key{ctx->g.nx, ctx->g.ny, ctx->g.nz, ctx->C, ctx->desc.precision,
+                                 (ctx->use_tc ? 1 : 0) + 2 * (ctx->tune == 3), rhs_tuned};
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto                        it = g_tune_cache.find(key);
     if (it == g_tune_cache.end()) {
@@ -1060,10 +1062,13 @@ int autotune(fansgpu_ctx *ctx)
         c.v64[1] = ctx->cp64.var_y;
         c.v64[2] = ctx->cp64.var_x;
         if (mixed) {
-            FANS_CUDA_CHECK(tune_convolution_reg<float>(ctx->cp32, ctx->r32, ctx->Kd32, ctx->st));
-            c.v32[0] = ctx->cp32.var_z;
-            c.v32[1] = ctx->cp32.var_y;
-            c.v32[2] = ctx->cp32.var_x;
+            ConvPlan<float> tp = ctx->cp32; // r32, Kd32 and the spectrum hold every RHS
+            tp.nrhs            = rhs_tuned;
+            tp.active          = nullptr;
+            FANS_CUDA_CHECK(tune_convolution_reg<float>(tp, ctx->r32, ctx->Kd32, ctx->st));
+            c.v32[0] = tp.var_z;
+            c.v32[1] = tp.var_y;
+            c.v32[2] = tp.var_x;
             if (ctx->use_tc && ctx->tune == 3)
                 c.tc_slower = time_mixed_operator(ctx, false) < time_mixed_operator(ctx, true) ? 1 : 0;
         }

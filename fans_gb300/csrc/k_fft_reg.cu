@@ -568,7 +568,7 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, cudaStream_t 
         launch();
         if ((e = cudaEventRecord(e0, st)) != cudaSuccess)
             return ms;
-        for (int k = 0; k < 3; ++k)
+        for (int k = 0; k < 5; ++k)
             launch();
         if ((e = cudaEventRecord(e1, st)) == cudaSuccess && (e = cudaEventSynchronize(e1)) == cudaSuccess &&
             (e = cudaGetLastError()) == cudaSuccess)

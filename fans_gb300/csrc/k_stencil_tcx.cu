@@ -128,6 +128,24 @@ __device__ __forceinline__ void df_add(float &h, float &l, float bh, float bl)
     l = l + bl + e;
 }
 
+// the same on two lanes at once (packed FP32x2; each lane is an IEEE single operation)
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &e)
+{
+    s              = __fadd2_rn(a, b);
+    const float2 z = __fadd2_rn(s, neg2(a));
+    e              = __fadd2_rn(__fadd2_rn(a, neg2(__fadd2_rn(s, neg2(z)))), __fadd2_rn(b, neg2(z)));
+}
+
+__device__ __forceinline__ void df_add2(float2 &h, float2 &l, float2 bh, float2 bl)
+{
+    float2 s, e;
+    two_sum2(h, bh, s, e);
+    h = s;
+    l = __fadd2_rn(__fadd2_rn(l, bl), e);
+}
+
 __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v)
 {
     uint32_t r[4];
@@ -440,25 +458,38 @@ __global__ void __maxnreg__(96)
                 tmem_ld4(lane_base + (uint32_t)(3 * NW + c0), v3);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int jj = 0; jj < 4; ++jj) {
-                    const int col = c0 + jj, bb = col / NCOL, r = col % NCOL;
+                for (int jj = 0; jj < 4; jj += 2) { // two columns per packed FP32x2 instruction
+                    const int col = c0 + jj, bb = col / NCOL, r = col % NCOL; // NCOL % 4 == 0
                     if (col < Cfg::NROW) {
                         // the exact integer sums back to one double-float value, unscaled
-                        float h, l;
-                        two_sum(v0[jj], v1[jj] * 4.8828125e-4f, h, l);                 // 2^-11 (exact)
-                        l = fmaf(v2[jj], 2.384185791015625e-7f, fmaf(v3[jj], 1.1641532182693481e-10f, l)); // 2^-22, 2^-33
-                        h *= inv;
-                        l *= inv;
+                        float2 h, l;
+                        two_sum2(make_float2(v0[jj], v0[jj + 1]),
+                                 __fmul2_rn(make_float2(v1[jj], v1[jj + 1]), make_float2(4.8828125e-4f, 4.8828125e-4f)),
+                                 h, l); // 2^-11 (exact)
+                        l = __ffma2_rn(make_float2(v2[jj], v2[jj + 1]), make_float2(2.384185791015625e-7f, 2.384185791015625e-7f),
+                                       __ffma2_rn(make_float2(v3[jj], v3[jj + 1]),
+                                                  make_float2(1.1641532182693481e-10f, 1.1641532182693481e-10f), l)); // 2^-22, 2^-33
+                        const float2 inv2 = make_float2(inv, inv);
+                        h                 = __fmul2_rn(h, inv2);
+                        l                 = __fmul2_rn(l, inv2);
                         // times the phase coefficient (double-float product)
-                        const int   b2 = bb < NB ? bb : 0;
-                        const float p  = cfh[b2] * h;
-                        const float pe = fmaf(cfh[b2], h, -p);
-                        const float pl = fmaf(cfh[b2], l, fmaf(cfl[b2], h, pe));
+                        const int    b2  = bb < NB ? bb : 0;
+                        const float2 ch2 = make_float2(cfh[b2], cfh[b2]), cl2 = make_float2(cfl[b2], cfl[b2]);
+                        const float2 p   = __fmul2_rn(ch2, h);
+                        const float2 pe  = __ffma2_rn(ch2, h, make_float2(-p.x, -p.y));
+                        const float2 pl  = __ffma2_rn(ch2, l, __ffma2_rn(cl2, h, pe));
                         if (bb == 0) {
-                            oh[r] = p;
-                            ol[r] = pl;
+                            oh[r]     = p.x;
+                            oh[r + 1] = p.y;
+                            ol[r]     = pl.x;
+                            ol[r + 1] = pl.y;
                         } else {
-                            df_add(oh[r], ol[r], p, pl);
+                            float2 sh = make_float2(oh[r], oh[r + 1]), sl = make_float2(ol[r], ol[r + 1]);
+                            df_add2(sh, sl, p, pl);
+                            oh[r]     = sh.x;
+                            oh[r + 1] = sh.y;
+                            ol[r]     = sl.x;
+                            ol[r + 1] = sl.y;
                         }
                     }
                 }
@@ -467,8 +498,15 @@ __global__ void __maxnreg__(96)
             mbar_arrive(bar(BAR_DFREE));
             if (force)
 #pragma unroll
-                for (int r = 0; r < NCOL; ++r)
-                    df_add(oh[r], ol[r], fsm[ph * NCOL + r], fsm[kMaxPhX * NCOL + ph * NCOL + r]);
+                for (int r = 0; r < NCOL; r += 2) {
+                    float2 sh = make_float2(oh[r], oh[r + 1]), sl = make_float2(ol[r], ol[r + 1]);
+                    df_add2(sh, sl, make_float2(fsm[ph * NCOL + r], fsm[ph * NCOL + r + 1]),
+                            make_float2(fsm[kMaxPhX * NCOL + ph * NCOL + r], fsm[kMaxPhX * NCOL + ph * NCOL + r + 1]));
+                    oh[r]     = sh.x;
+                    oh[r + 1] = sh.y;
+                    ol[r]     = sl.x;
+                    ol[r + 1] = sl.y;
+                }
             // x: near-x rows plus the carried far-x rows
             float Ph[4 * C], Pl[4 * C];
 #pragma unroll
