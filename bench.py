@@ -30,6 +30,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -205,6 +206,21 @@ def fp64_rate():
     return v.value if rc == 0 else None
 
 
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (model name, or the Arm implementer/part ids)."""
+    try:
+        info = open("/proc/cpuinfo").read()
+    except OSError:
+        return platform.machine()
+    for key in ("model name", "Model"):
+        for line in info.splitlines():
+            if line.startswith(key) and ":" in line:
+                return line.split(":", 1)[1].strip()
+    ids = [line.split(":", 1)[1].strip() for line in info.splitlines()
+           if line.startswith(("CPU implementer", "CPU part")) and ":" in line][:2]
+    return f"{platform.machine()} (implementer/part {'/'.join(ids)})" if ids else platform.machine()
+
+
 def build_problem(n, seed=0):
     from fans_gb300.microstructure import spheres
 
@@ -342,7 +358,8 @@ def run_reference(args):
             "dtype": "f64", "data": f"synthetic: seeded spheres ({nsph}), seed 0, r=6, vf=0.30",
             "config": {"workload": f"{n}^3 two-phase elastic HEX8, 6 unit load cases, CG rel L2 {args.tol}",
                        "parallelism": "cpu-openmp", "iterations": res["iterations"]},
-            "cpu_baseline": {"value": round(value_ms, 1), "unit": "ms", "cores": res["cores"], "kind": "port",
+            "cpu_baseline": {"value": round(value_ms, 1), "unit": "ms", "cores": res["cores"], "cpu": cpu_model(),
+                             "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value_ms, 1), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "ceff_rel_diff_vs_committed_oracle_run": check}
@@ -584,7 +601,8 @@ def main():
             it_cpu, it_src = (fp64["iterations"] if fp64 else iters), "this run's GPU iteration counts"
         cb = cpu_baseline(ms, n, args.cpu_iters)
         cpu_ms = 1e3 * (6 * cb["setup_s"] + cb["per_iter_s"] * sum(it_cpu))
-        cpu = {"value": round(cpu_ms, 1), "unit": "ms", "cores": cb["cores"], "kind": "port", "estimate": True,
+        cpu = {"value": round(cpu_ms, 1), "unit": "ms", "cores": cb["cores"], "cpu": cpu_model(), "kind": "port",
+               "estimate": True,
                "sample": (f"oracle (FP64 C restatement, OpenMP) on {n}^3: solver setup + {args.cpu_iters} CG "
                           f"iterations of load case 0 ({cb['sample_s']:.1f} s, {cb['per_iter_s'] * 1e3:.0f} ms per "
                           f"iteration), times 6 setups and the iteration counts {it_cpu} of {it_src}; the measured "

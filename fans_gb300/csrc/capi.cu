@@ -1057,7 +1057,16 @@ int autotune(fansgpu_ctx *ctx)
     auto                        it = g_tune_cache.find(key);
     if (it == g_tune_cache.end()) {
         TuneChoice c{};
-        FANS_CUDA_CHECK(tune_convolution_reg<double>(ctx->cp64, ctx->r, ctx->Kd, ctx->st));
+        // scratch CG scalars for the z-inverse pass's fused reduction (the context's own are
+        // left untouched)
+        CgScalars *tscal = nullptr;
+        FANS_CUDA_CHECK(cudaMalloc((void **)&tscal, sizeof(CgScalars) * kMaxRhs));
+        FANS_CUDA_CHECK(cudaMemsetAsync(tscal, 0, sizeof(CgScalars) * kMaxRhs, ctx->st));
+        struct Free {
+            CgScalars *p;
+            ~Free() { cudaFree(p); }
+        } free_tscal{tscal};
+        FANS_CUDA_CHECK(tune_convolution_reg<double>(ctx->cp64, ctx->r, ctx->Kd, tscal, ctx->red, SITE_CONV, ctx->st));
         c.v64[0] = ctx->cp64.var_z;
         c.v64[1] = ctx->cp64.var_y;
         c.v64[2] = ctx->cp64.var_x;
@@ -1065,7 +1074,7 @@ int autotune(fansgpu_ctx *ctx)
             ConvPlan<float> tp = ctx->cp32; // r32, Kd32 and the spectrum hold every RHS
             tp.nrhs            = rhs_tuned;
             tp.active          = nullptr;
-            FANS_CUDA_CHECK(tune_convolution_reg<float>(tp, ctx->r32, ctx->Kd32, ctx->st));
+            FANS_CUDA_CHECK(tune_convolution_reg<float>(tp, ctx->r32, ctx->Kd32, tscal, ctx->red, SITE_CONV, ctx->st));
             c.v32[0] = tp.var_z;
             c.v32[1] = tp.var_y;
             c.v32[2] = tp.var_x;

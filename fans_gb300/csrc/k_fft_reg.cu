@@ -551,12 +551,13 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
 // so the choice changes the speed only (the fused dot of the z inverse pass
 // sums in another block order).
 template <typename T>
-cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, cudaStream_t st)
+cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *scal, GridRed red, int red_site,
+                                 cudaStream_t st)
 {
     if (!conv_reg_supported(p.g))
         return cudaSuccess;
     using TL = Tiles<T>;
-    ConvArgs    a{r, s, 1.0, 0, nullptr, GridRed{}, 0, nullptr};
+    ConvArgs    a{r, s, 1.0, 1, scal, red, red_site, nullptr}; // with the fused <r, s>, as in the iteration
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e  = cudaEventCreate(&e0);
     if (e == cudaSuccess)
@@ -612,7 +613,9 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, cudaStream_t 
 
 template cudaError_t launch_convolution_reg<double>(const ConvPlan<double> &, const ConvArgs &, cudaStream_t);
 template cudaError_t launch_convolution_reg<float>(const ConvPlan<float> &, const ConvArgs &, cudaStream_t);
-template cudaError_t tune_convolution_reg<double>(ConvPlan<double> &, const double *, double *, cudaStream_t);
-template cudaError_t tune_convolution_reg<float>(ConvPlan<float> &, const float *, float *, cudaStream_t);
+template cudaError_t tune_convolution_reg<double>(ConvPlan<double> &, const double *, double *, CgScalars *, GridRed,
+                                                   int, cudaStream_t);
+template cudaError_t tune_convolution_reg<float>(ConvPlan<float> &, const float *, float *, CgScalars *, GridRed, int,
+                                                  cudaStream_t);
 
 } // namespace fansgpu

@@ -244,7 +244,10 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
 // Times the register passes' tile variants on p's buffers (r in, s out) and
 // stores the faster ones in p.var_z / var_y / var_x.
 template <typename T>
-cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, cudaStream_t st);
+// times the tile variants as the CG iteration runs them: the z-inverse pass with its fused
+// <r, s> reduction (into `scal`, scratch scalars, through `red` at `red_site`)
+cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *scal, GridRed red, int red_site,
+                                 cudaStream_t st);
 
 // Green's table (solver.h:145-204) in FP64, optionally also rounded to FP32.
 struct GreenArgs {
