@@ -68,6 +68,7 @@ struct fansgpu_ctx {
     std::vector<float>  K32h;
     bool                u_zero = true; // v_u known to be zero (fresh context / reset): R(u) = F
     double *K64 = nullptr, *f64 = nullptr, *Cph = nullptr, *Bbar_d = nullptr, *g0_d = nullptr, *K0c = nullptr;
+    double *fnode = nullptr; // r = F at u = 0 for <= 2 phases: 256 x C node sums by element-phase key
     double *Bgp_d = nullptr; // Gauss-point B matrices, ngp x n_str x 8C
     double *Bb_d  = nullptr; // basic B (dN_q/dx_j) per Gauss point, ngp x 3 x 8: HEX8 / HEX8R mechanics
     float  *K32 = nullptr;
@@ -611,6 +612,23 @@ int setup(fansgpu_ctx *ctx)
         }
         ctx->f64h = f;
         FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->f64, f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice, ctx->st));
+        if (ctx->nph <= 2) {
+            // node sums of the force rows for every key of the 8 element phases, summed over the
+            // local node p = 0..7 in the order the stencil kernels add them (bitwise the same r)
+            std::vector<double> tab((size_t)256 * C);
+            for (int key = 0; key < 256; ++key)
+                for (int cr = 0; cr < C; ++cr) {
+                    double acc = 0.0;
+                    for (int p = 0; p < 8; ++p)
+                        acc += f[(size_t)(std::min((key >> p) & 1, ctx->nph - 1)) * NC + p * C + cr];
+                    tab[(size_t)key * C + cr] = acc;
+                }
+            int rc3;
+            if (!ctx->fnode && (rc3 = dalloc(ctx, &ctx->fnode, (size_t)256 * 3)))
+                return rc3;
+            FANS_CUDA_CHECK(cudaMemcpyAsync(ctx->fnode, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice,
+                                            ctx->st));
+        }
         {
             std::vector<float> fdf(2 * f.size());
             for (size_t i = 0; i < f.size(); ++i) {
@@ -651,6 +669,13 @@ int run_stencil(fansgpu_ctx *ctx, const T *x, T *y, bool with_f)
     a.fph_host = with_f ? ctx->f64h.data() : nullptr;
     a.force_only = (with_f && (const void *)x == (const void *)ctx->u && ctx->u_zero) ? 1 : 0;
     a.nph    = ctx->nph;
+    if (std::is_same<T, double>::value && a.force_only && ctx->nph <= 2 && ctx->fnode && !ctx->vscale &&
+        ctx->all_linear) { // r = F from the node table
+        int e0 = tk_mark(ctx);
+        FANS_CUDA_CHECK(launch_force_nodes(ctx->g, ctx->C, ctx->d_ms, ctx->fnode, reinterpret_cast<double *>(y), ctx->st));
+        tk_span(ctx, FANSGPU_K_RESIDUAL, e0, tk_mark(ctx));
+        return 0;
+    }
     a.scal   = ctx->scal;
     a.red    = ctx->red;
     a.red_site = SITE_STENCIL;
@@ -2028,7 +2053,7 @@ int fansgpu_destroy(fansgpu_ctx *ctx)
         cudaStreamSynchronize(ctx->st);
     void *ptrs[] = {ctx->d_ms, ctx->u0,   ctx->r0,     ctx->s,      ctx->dd[0],  ctx->dd[1],      ctx->Kd,
                     ctx->up0,  ctx->act,  ctx->ctlr,   ctx->Wtb,    ctx->coef_tb, ctx->coef_tx, ctx->r32, ctx->s32,   ctx->d32[0], ctx->d32[1], ctx->Kd32, ctx->e32, ctx->Kdf, ctx->fdf,       ctx->K64,
-                    ctx->f64,  ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
+                    ctx->f64,  ctx->fnode, ctx->Cph,  ctx->Bbar_d, ctx->g0_d,  ctx->K0c,    ctx->K32,        ctx->G64,
                     ctx->G32,  ctx->spec64, ctx->tw64, ctx->spec32, ctx->tw32,  ctx->trig,       ctx->staging,
                     ctx->scal, ctx->red.partials, ctx->red.counter, ctx->red_out, ctx->max_id, ctx->Bgp_d, ctx->Bb_d,
                     ctx->ep_t, ctx->q_t, ctx->ep, ctx->q, ctx->rows, ctx->law_d, ctx->prm_d, ctx->Wtc, ctx->pb_t, ctx->pb,

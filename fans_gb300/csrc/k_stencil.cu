@@ -787,6 +787,48 @@ cudaError_t launch_strain_stress(const StrainStressArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// r = F(g0) alone (u = 0, the initial residual of a load case, solver.h:231-270 with zero u):
+// node (x, y, z) sums row p of the g0 force of the element whose local node p it is, p = 0..7,
+// in that order.  With at most two phases the 8 element phases form an 8-bit key and `table`
+// holds the 256 sums per component, made on the host in the same order (bitwise the sums the
+// full stencil forms), so a node costs 8 phase loads and C stores.
+template <int C>
+__global__ void __launch_bounds__(256) k_force_nodes(const uint8_t *__restrict__ ms, const double *__restrict__ table,
+                                                     double *__restrict__ y, Grid3 g)
+{
+    __shared__ double T[256 * C];
+    for (int i = threadIdx.x; i < 256 * C; i += blockDim.x)
+        T[i] = table[i];
+    __syncthreads();
+    const int       nx = g.nx, ny = g.ny, nz = g.nz;
+    const long long N  = (long long)nx * ny * nz;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(i % nz), yy = (int)((i / nz) % ny), x = (int)(i / ((long long)ny * nz));
+        unsigned  key = 0;
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            const int ex = pmod(x - (p & 1), nx), ey = pmod(yy - ((p >> 1) & 1), ny), ez = pmod(z - ((p >> 2) & 1), nz);
+            key |= (unsigned)(ms[((long long)ex * ny + ey) * nz + ez] & 1) << p;
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            y[c * N + i] = T[key * C + c];
+    }
+}
+
+cudaError_t launch_force_nodes(const Grid3 &g, int C, const uint8_t *ms, const double *table, double *y, cudaStream_t st)
+{
+    const long long N  = (long long)g.nx * g.ny * g.nz;
+    const int       nb = grid_blocks_for(N);
+    if (C == 3)
+        k_force_nodes<3><<<nb, 256, 0, st>>>(ms, table, y, g);
+    else if (C == 1)
+        k_force_nodes<1><<<nb, 256, 0, st>>>(ms, table, y, g);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
 template <typename TI, typename TO>
 cudaError_t launch_aos_to_soa(const TI *aos, TO *soa, long long N, int C, cudaStream_t st)
 {

@@ -56,6 +56,11 @@ cudaError_t launch_stencil(const StencilArgs &a, cudaStream_t st);
 // fph = FP64 force table.  FP64-accurate true residual at FP32 issue rates.
 cudaError_t launch_residual_df(const StencilArgs &a, cudaStream_t st);
 
+// r = F(g0) for u = 0 with at most two phases: `table` = 256 x C node sums indexed by the 8-bit
+// key of the phases (0/1) of the 8 elements around a node (bit p: the element whose node p it is)
+cudaError_t launch_force_nodes(const Grid3 &g, int C, const uint8_t *ms, const double *table, double *y,
+                               cudaStream_t st);
+
 // Element-averaged strain/stress of linear laws (matmodel.h:203-225,
 // solver.h:708-737): eps_e = Bbar u_e + g0 with Bbar (the Gauss-point mean of
 // B) = B at the element centre, sig_e = C_ph eps_e.  Sums over the
