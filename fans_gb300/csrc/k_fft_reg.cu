@@ -461,11 +461,19 @@ cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
-    const int    grid = (int)(nblk < 2LL * nsm ? nblk : 2LL * nsm); // persistent: two CTAs per SM
-    const size_t sm   = sizeof(cplx<T>) * (size_t)(2 * R * (M + N2) + 3 * R * M);
-    cudaError_t  e    = allow_max_dyn_smem(k_z_inv_reg<T, N1, N2, R>);
+    const size_t sm = sizeof(cplx<T>) * (size_t)(2 * R * (M + N2) + 3 * R * M);
+    cudaError_t  e  = allow_max_dyn_smem(k_z_inv_reg<T, N1, N2, R>);
     if (e != cudaSuccess)
         return e;
+    // persistent: as many CTAs per SM as fit (at least two; shared memory allows two at 256^3,
+    // more on smaller rows), at most one per block of rows
+    static int occ = 0;
+    if (!occ) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_z_inv_reg<T, N1, N2, R>, R * N1, sm) != cudaSuccess)
+            occ = 2;
+        occ = occ < 2 ? 2 : occ;
+    }
+    const int grid = (int)(nblk < (long long)occ * nsm ? nblk : (long long)occ * nsm);
     k_z_inv_reg<T, N1, N2, R><<<grid, R * N1, sm, st>>>(p, a);
     return cudaSuccess;
 }
