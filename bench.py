@@ -623,7 +623,8 @@ def main():
                            "rhs": "one multi-RHS solve of the 6 load cases" if args.rhs == 6 else "6 solves in turn",
                            "l2": "inputs larger than L2 (fields 0.2-0.4 GB each)",
                            "parallelism": f"replicas{world}" if world > 1 else "single-gpu",
-                           "iterations": iters, "refinements": refinements},
+                           "iterations": iters, "refinements": refinements,
+                           "fft_tiles_zyx": list(ctx.tuning()["fp32"])},
                 "ceff_rel_err_vs_oracle": ceff_err,
                 "e2e": {"value": round(e2e_ms, 2), "unit": "ms", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "wall_ms": round(e2e_wall, 2)},

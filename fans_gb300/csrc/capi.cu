@@ -74,6 +74,7 @@ struct fansgpu_ctx {
     float  *K32 = nullptr;
     double *G64 = nullptr;
     float  *G32 = nullptr;
+    TmaMaps tmaps{}; // tensor maps of the FP32 spectrum and Green's table (TMA-fed x pass)
     cplx<double> *spec64 = nullptr, *tw64 = nullptr;
     cplx<float>  *spec32 = nullptr, *tw32 = nullptr;
     double       *trig = nullptr; // cos/sin tables for the Green's table
@@ -255,6 +256,7 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
     p.tw_r2c = tw + g.nx + g.ny + p.M;
     p.spec   = spec;
     p.G      = G;
+    p.gzs    = sizeof(T) == 4 ? p.nzp : p.nzh;
     const size_t cs = sizeof(cplx<T>), budget = 100 * 1024;
     int          kc = 16;
     while (kc > 1 && cs * (2 * (size_t)g.ny * kc + g.ny) > budget)
@@ -267,6 +269,8 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
     p.use_reg = conv_reg_supported(g) ? 1 : 0;
     p.nrhs    = 1;
     p.active  = nullptr;
+    p.tma     = nullptr;
+    p.nrhs_alloc = ctx->nrhs;
     if (!p.use_reg && cs * (2 * (size_t)p.C * g.nx * p.kc_x + g.nx) > 200 * 1024)
         return fail(ctx, FANSGPU_EUNSUPPORTED, "n_x=%d too large for the shared-memory x pass", g.nx);
     return 0;
@@ -594,8 +598,9 @@ int setup(fansgpu_ctx *ctx)
         ga.sy  = ga.cy + g.ny;
         ga.cz  = ga.sy + g.ny;
         ga.sz  = ga.cz + nzh;
-        ga.G64 = ctx->G64;
-        ga.G32 = ctx->G32;
+        ga.G64  = ctx->G64;
+        ga.G32  = ctx->G32;
+        ga.g32s = ((nzh + 15) / 16) * 16; // FP32 rows padded as the spectrum's (16-byte starts)
         int e0 = tk_mark(ctx);
         FANS_CUDA_CHECK(launch_green(ga, ctx->st));
         tk_span(ctx, FANSGPU_K_GREEN, e0, tk_mark(ctx));
@@ -1055,10 +1060,10 @@ int autotune(fansgpu_ctx *ctx)
     auto apply = [&](const TuneChoice &c) {
         ctx->cp64.var_z = c.v64[0];
         ctx->cp64.var_y = c.v64[1];
-        ctx->cp64.var_x = c.v64[2];
+        ctx->cp64.var_x = std::min(c.v64[2], 1); // the TMA-fed x pass (2) is FP32 only
         ctx->cp32.var_z = c.v32[0];
         ctx->cp32.var_y = c.v32[1];
-        ctx->cp32.var_x = c.v32[2];
+        ctx->cp32.var_x = (c.v32[2] == 2 && !ctx->cp32.tma) ? 0 : c.v32[2];
         if (c.tc_slower && ctx->use_tc) {
             ctx->tc_slower = true;
             ctx->use_tc    = false;
@@ -1903,7 +1908,7 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
             ctx->tune = 0;
         else if (std::strcmp(ev, "all") == 0)
             ctx->tune = 3;
-        else if (std::strlen(ev) == 3 && std::strspn(ev, "01") == 3) {
+        else if (std::strlen(ev) == 3 && std::strspn(ev, "01") >= 2 && std::strchr("012", ev[2])) {
             ctx->tune = 2;
             for (int k = 0; k < 3; ++k)
                 ctx->tune_force[k] = ev[k] - '0';
@@ -1980,7 +1985,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         if ((rc = dalloc(ctx, &ctx->r32, nr)) || (rc = dalloc(ctx, &ctx->s32, nr)) ||
             (rc = dalloc(ctx, &ctx->d32[0], nr)) || (rc = dalloc(ctx, &ctx->d32[1], nr)) ||
             (rc = dalloc(ctx, &ctx->Kd32, nr)) || (rc = dalloc(ctx, &ctx->e32, nr)) ||
-            (rc = dalloc(ctx, &ctx->spec32, nspec * nrhs)) || (rc = dalloc(ctx, &ctx->G32, F * NT)))
+            (rc = dalloc(ctx, &ctx->spec32, nspec * nrhs)) ||
+            (rc = dalloc(ctx, &ctx->G32, (long long)ctx->g.nx * ctx->g.ny * nzp * NT)))
             return bail(rc);
     }
     if (cudaMallocHost((void **)&ctx->scal_h, sizeof(CgScalars) * kMaxRhs) != cudaSuccess ||
@@ -2041,6 +2047,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         return bail(rc);
     if (mixed && (rc = make_plan<float>(ctx, ctx->cp32, ctx->spec32, ctx->tw32, ctx->G32)))
         return bail(rc);
+    if (mixed && ctx->cp32.use_reg && make_x_tma_maps(ctx->cp32, &ctx->tmaps))
+        ctx->cp32.tma = &ctx->tmaps;
     *out = ctx;
     return 0;
 }

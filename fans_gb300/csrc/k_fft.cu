@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(kFftThreads) k_x_green(ConvPlan<T> p)
         const int x = i / KC, l = i % KC;
         if (l >= nk)
             continue;
-        const T *g = p.G + (((long long)x * ny + ky) * p.nzh + kz0 + l) * NT;
+        const T *g = p.G + (((long long)x * ny + ky) * p.gzs + kz0 + l) * NT;
         T        gm[NT];
 #pragma unroll
         for (int t = 0; t < NT; ++t)
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(256) k_green(GreenArgs a)
         for (int t = 0; t < NT; ++t) {
             a.G64[f * NT + t] = out[t];
             if (a.G32)
-                a.G32[f * NT + t] = (float)out[t];
+                a.G32[((f / nzh) * a.g32s + iz) * NT + t] = (float)out[t]; // row (ix, iy) at stride g32s
         }
     }
 }

@@ -6,6 +6,12 @@
 // line transform.  Shared memory holds one copy of the tile (no ping-pong), so
 // more CTAs are resident.  Used for line lengths with a register plan
 // (reg_n1(n) != 0); other sizes use the shared-memory Stockham passes.
+#include <cuda.h> // CUtensorMap (the encoder is reached through the runtime)
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <type_traits>
+
 #include "fft_reg.cuh"
 #include "kernels.cuh"
 
@@ -90,7 +96,7 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
     // Green's table slice [kx][kz0 .. kz0+nk)[NT] -> Gs, asynchronously
     for (int i = t; i < n * nk * NT; i += blockDim.x) {
         const int kx = i / (nk * NT), r2 = i % (nk * NT);
-        const T  *src = p.G + (((long long)kx * ny + ky) * p.nzh + kz0) * NT + r2;
+        const T  *src = p.G + (((long long)kx * ny + ky) * p.gzs + kz0) * NT + r2;
         T        *dst = Gs + (size_t)kx * KC * NT + r2;
         if constexpr (sizeof(T) == 4)
             asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
@@ -198,6 +204,255 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
                     gb[(w + N2 * k1) * xstride] = u[k1];
         }
         __syncthreads(); // F is reused by the next right-hand side
+    }
+}
+
+// ------------------------------------------- x pass + Green's op, TMA-fed ---
+// FP32 form of the x pass with its inputs brought in by the tensor memory
+// accelerator.  Persistent: CTA b takes a contiguous share of the jobs
+// (tile, RHS), tile = (ky, KX kz columns), and keeps two job buffers in flight.
+// A job's [C][nx][KX] spectrum tile arrives by one tensor-map copy per component
+// and completes on its buffer's mbarrier; the copy of job q + 2 is issued as
+// soon as every thread has read job q's buffer, so the reads run two jobs ahead
+// of the transforms.  The tile's Green's slice [nx][KX][NT] arrives the same
+// way, issued when the previous tile's last job has applied its slice.  The
+// Green multiply is fused into the load of the inverse transform (each thread
+// forms its component's row of G . F for its own kx), and the twiddles of a
+// worker live in registers.  The arithmetic per value is that of
+// k_x_green_reg, so both give the same spectrum bit for bit.  Every wait is
+// bounded: one that runs out sets an abort flag that releases the others, no
+// further copies are issued, the CTA waits (bounded) for the copies it has in
+// flight, and the status -3 goes to every active RHS's converged field.
+constexpr int      kTmaKC        = 8;       // kz columns per tile: 64-byte rows of complex FP32
+constexpr unsigned kTmaWaitLimit = 1u << 22; // polls of one mbarrier wait
+
+__device__ __forceinline__ bool tma_bar_try(uint32_t bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 " selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void tma_bar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag)
+{
+    for (unsigned it = 0; it < kTmaWaitLimit; ++it)
+        if (tma_bar_try(bar, parity) || *abort_flag)
+            return;
+    *abort_flag = 1;
+}
+
+// box {2 KX floats, 1, n} of a 3-d float tensor map at (x, y, z) into shared memory,
+// completing `bytes` on `bar` (the caller has posted them with expect_tx)
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *tm, int x, int y, int z, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_expect(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+template <int N1, int N2, int C>
+struct XTma {
+    static constexpr int n = N1 * N2, KX = kTmaKC, NT = C * (C + 1) / 2;
+    static constexpr int JOB_BYTES = C * n * KX * 8; // one job's spectrum tile
+    static constexpr int G_BYTES   = n * KX * NT * 4;
+    static constexpr int OFF_F     = 2 * JOB_BYTES;  // exchange buffer [C][n][KX]
+    static constexpr int OFF_G     = 3 * JOB_BYTES;  // Green's slice [n][KX][NT]
+    static constexpr int OFF_BAR   = (OFF_G + G_BYTES + 15) / 16 * 16; // full[2], green, flags
+    static constexpr int SMEM      = OFF_BAR + 64;
+};
+
+template <int N1, int N2, int C>
+__global__ void __launch_bounds__(C * kTmaKC * N1, 1)
+    k_x_green_tma(ConvPlan<float> p, ConvArgs a, const __grid_constant__ CUtensorMap tm_spec,
+                  const __grid_constant__ CUtensorMap tm_green)
+{
+    using L          = XTma<N1, N2, C>;
+    constexpr int n  = L::n, KX = L::KX, NT = L::NT;
+    extern __shared__ __align__(1024) unsigned char xsm[];
+    cplx<float>  *Bf  = reinterpret_cast<cplx<float> *>(xsm);            // [2][C][n][KX]
+    cplx<float>  *F   = reinterpret_cast<cplx<float> *>(xsm + L::OFF_F); // [C][n][KX]
+    const float  *Gs  = reinterpret_cast<const float *>(xsm + L::OFF_G); // [n][KX][NT]
+    const uint32_t sb = (uint32_t)__cvta_generic_to_shared(xsm);
+    const uint32_t bar_full = sb + L::OFF_BAR, bar_green = bar_full + 16;
+    volatile int  *abort_flag = reinterpret_cast<volatile int *>(xsm + L::OFF_BAR + 24);
+    int           *s_act      = reinterpret_cast<int *>(xsm + L::OFF_BAR + 28); // nact, then kMaxRhs ids
+
+    const int t = threadIdx.x, comp = t / (KX * N1), rem = t % (KX * N1), w = rem / KX, l = rem % KX;
+    const int ny = p.g.ny, ntz = (p.nzh + KX - 1) / KX;
+    if (t == 0) {
+        int nact = 0;
+        for (int k = 0; k < p.nrhs; ++k)
+            if (!p.active || p.active[k])
+                s_act[1 + nact++] = k;
+        s_act[0]    = nact;
+        *abort_flag = (sb & 127) ? 1 : 0; // copies land on 128-byte boundaries of the window
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_full) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_full + 8) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_green) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int       nact = s_act[0];
+    const long long J    = (long long)ntz * ny * nact;
+    const long long jb   = J * blockIdx.x / gridDim.x, je = J * (blockIdx.x + 1) / gridDim.x;
+    if (nact == 0 || jb >= je || *abort_flag) {
+        if (*abort_flag && t == 0 && a.scal)
+            for (int kk = 0; kk < nact; ++kk)
+                a.scal[s_act[1 + kk]].converged = -3;
+        return; // no copy was issued
+    }
+    const int nq = (int)(je - jb);
+
+    // thread 0 only: issue the copies of job q (into buffer q & 1) or of job q's Green's slice
+    int iss[3] = {0, 0, 0}; // phases issued per barrier (full 0, full 1, green)
+    auto issue_job = [&](int q) {
+        const long long jg = jb + q;
+        const int       tile = (int)(jg / nact), k = s_act[1 + (int)(jg % nact)], b = q & 1;
+        const int       kz0 = (tile % ntz) * KX, ky = tile / ntz;
+        const uint32_t  bar = bar_full + 8 * b;
+        tma_expect(bar, L::JOB_BYTES);
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+            tma_load3(sb + b * L::JOB_BYTES + c * n * KX * 8, &tm_spec, 2 * kz0, ky, (k * C + c) * n, bar);
+        ++iss[b];
+    };
+    auto issue_green = [&](int q) {
+        const int tile = (int)((jb + q) / nact), kz0 = (tile % ntz) * KX, ky = tile / ntz;
+        tma_expect(bar_green, L::G_BYTES);
+        tma_load3(sb + L::OFF_G, &tm_green, kz0 * NT, ky, 0, bar_green);
+        ++iss[2];
+    };
+    if (t == 0) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_spec)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_green)) : "memory");
+        issue_green(0);
+        issue_job(0);
+        if (nq > 1)
+            issue_job(1);
+    }
+
+    // this worker's twiddles W_n^(w k2), k2 = 1..N2-1 (line_phase1's table values)
+    cplx<float> twr[N2];
+#pragma unroll
+    for (int k2 = 1; k2 < N2; ++k2)
+        twr[k2] = p.tw_x[w * k2];
+    const long long xstride  = (long long)ny * p.nzp;
+    const long long rhs_spec = (long long)p.C * n * ny * p.nzp;
+    cplx<float>    *Fc       = F + (size_t)comp * n * KX;
+    int             gph      = 0; // Green's slices waited for
+
+    for (int q = 0; q < nq; ++q) {
+        const long long jg = jb + q;
+        const int tile = (int)(jg / nact), kk = (int)(jg % nact), k = s_act[1 + kk], b = q & 1;
+        const int kz0 = (tile % ntz) * KX, ky = tile / ntz;
+        const bool valid = l < p.nzh - kz0;
+        const bool first_of_tile = q == 0 || kk == 0, last_of_tile = kk == nact - 1;
+
+        // forward FFT along x: phase 1 from the job's buffer
+        tma_bar_wait(bar_full + 8 * b, (uint32_t)((q >> 1) & 1), abort_flag);
+        const cplx<float> *Bc = Bf + ((size_t)b * C + comp) * n * KX;
+        cplx<float>        v[N2];
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2)
+            v[j2] = Bc[(w + N1 * j2) * KX + l];
+        __syncthreads(); // the buffer is read (and F is free)
+        if (t == 0 && q + 2 < nq && !*abort_flag) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_job(q + 2);
+        }
+        Dft<float, N2, false>::run(v);
+#pragma unroll
+        for (int k2 = 1; k2 < N2; ++k2)
+            v[k2] = cmul(v[k2], twr[k2]);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2)
+            Fc[(k2 * N1 + w) * KX + l] = v[k2];
+        __syncthreads();
+        cplx<float> u[N1];
+        if (w < N2) {
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1)
+                u[j1] = Fc[(w * N1 + j1) * KX + l];
+            Dft<float, N1, false>::run(u);
+        }
+        __syncthreads();
+        if (w < N2)
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1)
+                Fc[(w + N2 * k1) * KX + l] = u[k1];
+        if (first_of_tile)
+            tma_bar_wait(bar_green, (uint32_t)(gph++ & 1), abort_flag);
+        __syncthreads();
+
+        // Green's operator (solver.h:400-406), row `comp` of the C x C real symmetric block per
+        // frequency, fused into the inverse transform's load
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2) {
+            const int    kx = w + N1 * j2;
+            const float *g  = Gs + ((size_t)kx * KX + l) * NT;
+            cplx<float>  acc = {0, 0};
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int         ia = comp > c ? comp : c, ib = comp > c ? c : comp;
+                const float       gv = g[ia * (ia + 1) / 2 + ib];
+                const cplx<float> x  = F[((size_t)c * n + kx) * KX + l];
+                acc.x += gv * x.x;
+                acc.y += gv * x.y;
+            }
+            v[j2] = acc;
+        }
+        __syncthreads(); // F and the Green's slice are read
+        if (t == 0 && last_of_tile && q + 1 < nq && !*abort_flag) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_green(q + 1);
+        }
+        // inverse FFT along x
+        Dft<float, N2, true>::run(v);
+#pragma unroll
+        for (int k2 = 1; k2 < N2; ++k2) {
+            cplx<float> tc = twr[k2];
+            tc.y           = -tc.y;
+            v[k2]          = cmul(v[k2], tc);
+        }
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2)
+            Fc[(k2 * N1 + w) * KX + l] = v[k2];
+        __syncthreads();
+        if (w < N2) {
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1)
+                u[j1] = Fc[(w * N1 + j1) * KX + l];
+            Dft<float, N1, true>::run(u);
+            if (valid) {
+                cplx<float> *gb = p.spec + k * rhs_spec + ((long long)comp * n * ny + ky) * p.nzp + kz0 + l;
+#pragma unroll
+                for (int k1 = 0; k1 < N1; ++k1)
+                    gb[(w + N2 * k1) * xstride] = u[k1];
+            }
+        }
+    }
+    __syncthreads();
+    if (*abort_flag && t == 0) {
+        // wait (bounded) for the copies still in flight: the last issued phase of each barrier
+        for (int i = 0; i < 3; ++i)
+            if (iss[i] > 0) {
+                const uint32_t bar = i < 2 ? bar_full + 8 * i : bar_green;
+                for (unsigned it = 0; it < kTmaWaitLimit && !tma_bar_try(bar, (uint32_t)((iss[i] - 1) & 1)); ++it)
+                    ;
+            }
+        if (a.scal)
+            for (int kk = 0; kk < nact; ++kk)
+                a.scal[s_act[1 + kk]].converged = -3; // a copy of the TMA-fed x pass did not arrive
     }
 }
 
@@ -442,6 +697,39 @@ cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
     return cudaSuccess;
 }
 
+// the TMA-fed x pass (FP32 plans with tensor maps): persistent, as many CTAs per SM as fit
+template <int N1, int N2>
+cudaError_t go_x_tma(const ConvPlan<float> &p, const ConvArgs &a, cudaStream_t st)
+{
+    const TmaMaps *m   = static_cast<const TmaMaps *>(p.tma);
+    const int      ntz = (p.nzh + kTmaKC - 1) / kTmaKC;
+    auto           run = [&]<int C>() -> cudaError_t {
+        constexpr int  NTH = C * kTmaKC * N1;
+        constexpr int  SM  = XTma<N1, N2, C>::SMEM;
+        auto           fn  = k_x_green_tma<N1, N2, C>;
+        static int     grid_per_sm = 0, nsm = 0;
+        cudaError_t    e   = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SM);
+        if (e != cudaSuccess)
+            return e;
+        if (!grid_per_sm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&grid_per_sm, fn, NTH, SM) != cudaSuccess ||
+                grid_per_sm < 1)
+                grid_per_sm = 1;
+        }
+        long long jobs = (long long)ntz * p.g.ny * p.nrhs;
+        const int grid = (int)(jobs < (long long)grid_per_sm * nsm ? jobs : (long long)grid_per_sm * nsm);
+        CUtensorMap ts, tg;
+        std::memcpy(&ts, m->spec, sizeof ts);
+        std::memcpy(&tg, m->green, sizeof tg);
+        fn<<<grid, NTH, SM, st>>>(p, a, ts, tg);
+        return cudaGetLastError();
+    };
+    return p.C == 1 ? run.template operator()<1>() : run.template operator()<3>();
+}
+
 template <typename T, int N1, int N2, int R>
 void go_zf(const ConvPlan<T> &p, const T *r, cudaStream_t st)
 {
@@ -534,7 +822,12 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
     });
     mark(2);
     with_plan(p.g.nx, [&]<int N1, int N2>() {
-        e = p.var_x ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
+        if constexpr (std::is_same_v<T, float>)
+            if (p.var_x == 2 && p.tma) {
+                e = go_x_tma<N1, N2>(p, a, st);
+                return;
+            }
+        e = p.var_x == 1 ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
     });
     if (e != cudaSuccess)
         return e;
@@ -605,18 +898,65 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
             });
         });
     p.var_y = t[1] < t[0] ? 1 : 0;
-    for (int v = 0; v < 2; ++v)
-        t[v] = timed([&] {
+    float tx[3] = {1e30f, 1e30f, 1e30f};
+    const int nvx = (std::is_same_v<T, float> && p.tma) ? 3 : 2;
+    for (int v = 0; v < nvx; ++v)
+        tx[v] = timed([&] {
             with_plan(p.g.nx, [&]<int N1, int N2>() {
+                if constexpr (std::is_same_v<T, float>)
+                    if (v == 2) {
+                        e = go_x_tma<N1, N2>(p, a, st);
+                        return;
+                    }
                 e = v ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
             });
         });
-    p.var_x = t[1] < t[0] ? 1 : 0;
+    p.var_x = 0;
+    for (int v = 1; v < nvx; ++v)
+        if (tx[v] < tx[p.var_x])
+            p.var_x = v;
     if (e0)
         cudaEventDestroy(e0);
     if (e1)
         cudaEventDestroy(e1);
     return e;
+}
+
+bool make_x_tma_maps(const ConvPlan<float> &p, TmaMaps *out)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static bool                              looked = false;
+    if (!looked) {
+        looked                               = true;
+        cudaDriverEntryPointQueryResult qres = cudaDriverEntryPointSymbolNotFound;
+        void                           *fn   = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qres) ==
+                cudaSuccess &&
+            qres == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    }
+    const int nx = p.g.nx, ny = p.g.ny, NT = p.C * (p.C + 1) / 2;
+    if (!encode || !reg_n1(nx) || nx > 256 || (p.C != 1 && p.C != 3) || p.gzs != p.nzp)
+        return false;
+    const cuuint32_t one[3] = {1, 1, 1};
+    // spectrum: floats [nrhs_alloc * C * nx][ny][2 * nzh], rows 2 * nzp floats apart
+    const cuuint64_t sd[3]  = {(cuuint64_t)2 * p.nzh, (cuuint64_t)ny, (cuuint64_t)p.nrhs_alloc * p.C * nx};
+    const cuuint64_t ss[2]  = {(cuuint64_t)2 * p.nzp * 4, (cuuint64_t)ny * 2 * p.nzp * 4};
+    const cuuint32_t sbx[3] = {2 * kTmaKC, 1, (cuuint32_t)nx};
+    // Green's table: floats [nx][ny][nzh * NT], rows nzp * NT floats apart
+    const cuuint64_t gd[3]  = {(cuuint64_t)p.nzh * NT, (cuuint64_t)ny, (cuuint64_t)nx};
+    const cuuint64_t gs[2]  = {(cuuint64_t)p.nzp * NT * 4, (cuuint64_t)ny * p.nzp * NT * 4};
+    const cuuint32_t gbx[3] = {(cuuint32_t)(kTmaKC * NT), 1, (cuuint32_t)nx};
+    CUresult r1 = encode(reinterpret_cast<CUtensorMap *>(out->spec), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, p.spec, sd,
+                         ss, sbx, one, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r2 = encode(reinterpret_cast<CUtensorMap *>(out->green), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                         const_cast<float *>(p.G), gd, gs, gbx, one, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS;
 }
 
 template cudaError_t launch_convolution_reg<double>(const ConvPlan<double> &, const ConvArgs &, cudaStream_t);

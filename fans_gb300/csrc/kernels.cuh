@@ -216,7 +216,8 @@ struct ConvPlan {
     FftDim         dx, dy, dz;     // dz has length M
     const cplx<T> *tw_x, *tw_y, *tw_z, *tw_r2c; // tw_r2c: exp(-2 pi i k/nz), k <= M
     cplx<T>       *spec;           // C * nx * ny * nzp
-    const T       *G;              // nx*ny*nzh*C(C+1)/2
+    const T       *G;              // [nx][ny][gzs][C(C+1)/2], kz < nzh filled
+    int            gzs;            // kz row stride of G (nzh for FP64; nzp for FP32, so rows start on 16 bytes)
     int            kc_y, kc_x;     // kz columns per CTA in the y / x passes
     int            use_reg;        // register-resident passes (conv_reg_supported)
     int            var_z, var_y, var_x; // register passes: tile variant (0 default, 1 the alternative)
@@ -224,7 +225,22 @@ struct ConvPlan {
     // of nrhs consecutive fields; the Green's table is shared); active[k] == 0 skips RHS k
     int            nrhs;
     const int     *active;
+    // FP32 x pass fed by the tensor memory accelerator (var_x == 2): host pointer to the
+    // TmaMaps of this plan's spectrum and Green's table, or null where none were made
+    const void    *tma;
+    int            nrhs_alloc; // right-hand sides the spectrum buffer holds (the tensor map's extent)
 };
+
+// Tensor maps of the TMA-fed x pass (host side, one per FP32 plan): the spectrum as floats
+// [nrhs_alloc * C * nx][ny][2 * nzh] (row stride 2 * nzp) and the Green's table as floats
+// [nx][ny][nzh * NT] (row stride nzp * NT), both with boxes of KC = 8 kz columns by all kx.
+struct TmaMaps {
+    alignas(64) unsigned char spec[128];
+    alignas(64) unsigned char green[128];
+};
+// Encode the maps of an FP32 plan (spec, G, gzs, nrhs_alloc set); false if the driver has no
+// tensor-map encoder or the shapes do not fit a tensor map.
+bool make_x_tma_maps(const ConvPlan<float> &p, TmaMaps *out);
 
 // s = sign * IFFT(G . FFT(r)); with reduce, <r, s> -> scal (delta0, delta,
 // beta) as in solverCG.h:86-94.
@@ -261,7 +277,8 @@ struct GreenArgs {
     const double *K0c;   // 8C x 8C, component-major ("C groups of 8")
     const double *cx, *sx, *cy, *sy, *cz, *sz; // cos/sin(2 pi k / n)
     double       *G64;
-    float        *G32;   // optional
+    float        *G32;   // optional; kz row stride g32s
+    int           g32s;
 };
 cudaError_t launch_green(const GreenArgs &a, cudaStream_t st);
 

@@ -88,3 +88,62 @@ def test_graph_modes_take_the_same_decisions(monkeypatch, n_it):
             assert np.array_equal(h0, h1), mode
             assert np.array_equal(s0, s1), mode
     assert ref[0][2] == (n_it == 500)
+
+
+def _multi_solve(P, n_rhs):
+    from fans_gb300 import Context
+
+    ctx = Context((P.nx, P.ny, P.nz), tuple(P.L), P.c, "HEX8", "mixed", "cg", n_rhs=n_rhs)
+    ctx.set_microstructure(P.ms)
+    for ph in range(P.nphase):
+        ctx.set_phase_material(ph, int(P.law[ph]), P.param[ph, : (1 if P.c == 1 else 2)])
+    ctx.set_reference(P.kapparef)
+    ctx.set_tolerance("L2", "relative", 1e-8, 1000)
+    loads = np.eye(P.nstr)[:n_rhs] if n_rhs > 1 else np.eye(P.nstr)[:1] * 0.7
+    ctx.set_gradients(loads)
+    agg = ctx.solve()
+    out = {"tuning": ctx.tuning()["fp32"], "agg": (agg["iterations"], agg["converged"])}
+    for k in range(n_rhs):
+        ctx.select_rhs(k)
+        st = ctx.rhs_stats(k)
+        out[k] = (st["iterations"], st["refinements"], ctx.error_history(), ctx.homogenized_stress(),
+                  ctx.get_field(0))
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("c,shape,n_rhs", [
+    (3, (32, 32, 64), 6),   # elastic, six RHS, N1 = N2 x line, ragged last kz tile (nz/2+1 = 33)
+    (3, (48, 16, 32), 3),   # N1 != N2 (48 = 8 x 6), three RHS
+    (1, (64, 32, 48), 3),   # thermal (one component, one Green's entry per frequency)
+    (3, (128, 16, 32), 1),  # one RHS: every job starts a new tile (a Green's slice per job)
+])
+def test_tma_x_pass_equals_register_x_pass(monkeypatch, c, shape, n_rhs):
+    """The FP32 x pass fed by tensor-map copies (x variant 2: persistent CTAs, two job
+    buffers in flight, Green's multiply fused into the inverse transform's load) runs
+    the register x pass's operations per value; only FP32 roundings may differ (the
+    compiler may fuse the Green's products with the transform's first additions).  A
+    mixed multi-RHS solve forced onto it must therefore follow the register pass's
+    residual history to FP32 accuracy in its first iterations (a wrong tile, Green's
+    entry or stale buffer moves it at once by far more), take the same refreshes and
+    the same iterations within one (the mixed path's bar against the oracle), and
+    reach the same stresses and displacements within the FP64 true residual
+    tolerance."""
+    from helpers import THERMAL
+
+    ms = random_ms(shape, vf=0.3, seed=61)
+    P = oracle_problem(ms, c, ELASTIC if c == 3 else THERMAL, "HEX8")
+    monkeypatch.setenv("FANSGPU_TUNE", "000")
+    ref = _multi_solve(P, n_rhs)
+    monkeypatch.setenv("FANSGPU_TUNE", "002")
+    got = _multi_solve(P, n_rhs)
+    assert ref["tuning"] == (0, 0, 0) and got["tuning"] == (0, 0, 2)
+    assert ref["agg"][1] and got["agg"][1] and abs(got["agg"][0] - ref["agg"][0]) <= 1
+    for k in range(n_rhs):
+        i0, r0, h0, s0, u0 = ref[k]
+        i1, r1, h1, s1, u1 = got[k]
+        assert abs(i0 - i1) <= 1 and r0 == r1, (k, i0, i1, r0, r1)
+        assert h0[0] == h1[0], k
+        assert np.abs(h1[:4] / h0[:4] - 1).max() < 2e-6, (k, h0[:4], h1[:4])
+        assert rel(s1, s0) < 1e-8, k
+        assert rel(u1, u0) < 1e-6, k
