@@ -125,13 +125,17 @@ def algo_bytes(kernel, n, C=3, w=4, r=1.0):
         "fft_y_fwd": r * 2 * spec,
         "fft_x_green": r * 2 * spec + nt * n * n * nzh * w,  # + Green's table, once
         "fft_y_inv": r * 2 * spec,
-        "fft_z_inv": r * (spec + 2 * C * w * N),        # read spectrum + r, write s
+        # read spectrum (+ r where <r, s> is taken from r and s), write s; on the FP32 path
+        # <r, s> comes from the spectra in the x pass unless FANSGPU_SPECTRAL_DOT=0
+        "fft_z_inv": r * (spec + (1 if w == 4 and SPECTRAL_DOT else 2) * C * w * N),
         "cg_update": r * 7 * C * w * N,                 # read r, Kd, e, d, s; write r, e (FP32)
         "residual64": (2 * 8 * C + 1) * N,
         "norm": (8 * C + 4 * C) * N,
         "strain_stress": (8 * C + 1) * N,
     }.get(kernel)
 
+
+SPECTRAL_DOT = os.environ.get("FANSGPU_SPECTRAL_DOT", "1") != "0"
 
 ITER_KERNELS = ("stencil", "fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "cg_update")
 

@@ -75,6 +75,7 @@ struct fansgpu_ctx {
     double *G64 = nullptr;
     float  *G32 = nullptr;
     TmaMaps tmaps{}; // tensor maps of the FP32 spectrum and Green's table (TMA-fed x pass)
+    bool    spectral_dot = true; // FP32 convolutions take <r, s> from the spectra in the x pass
     cplx<double> *spec64 = nullptr, *tw64 = nullptr;
     cplx<float>  *spec32 = nullptr, *tw32 = nullptr;
     double       *trig = nullptr; // cos/sin tables for the Green's table
@@ -268,6 +269,8 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
     p.kc_x    = kc;
     p.use_reg = conv_reg_supported(g) ? 1 : 0;
     p.nrhs    = 1;
+    p.fuse_zy = 0;
+    p.spectral_dot = 0;
     p.active  = nullptr;
     p.tma     = nullptr;
     p.nrhs_alloc = ctx->nrhs;
@@ -1058,10 +1061,11 @@ int autotune(fansgpu_ctx *ctx)
     ctx->tuned       = true;
     const bool mixed = ctx->desc.precision == FANSGPU_MIXED;
     auto apply = [&](const TuneChoice &c) {
-        ctx->cp64.var_z = c.v64[0];
-        ctx->cp64.var_y = c.v64[1];
-        ctx->cp64.var_x = std::min(c.v64[2], 1); // the TMA-fed x pass (2) is FP32 only
-        ctx->cp32.var_z = c.v32[0];
+        ctx->cp64.var_z = c.v64[0] & 1; // the fused z + y forward pass (bit 1) and the TMA-fed
+        ctx->cp64.var_y = c.v64[1];     // x pass (2) are FP32 only
+        ctx->cp64.var_x = std::min(c.v64[2], 1);
+        ctx->cp32.var_z = c.v32[0] & 1;
+        ctx->cp32.fuse_zy = (c.v32[0] & 2) && zy_supported(ctx->g) ? 1 : 0;
         ctx->cp32.var_y = c.v32[1];
         ctx->cp32.var_x = (c.v32[2] == 2 && !ctx->cp32.tma) ? 0 : c.v32[2];
         if (c.tc_slower && ctx->use_tc) {
@@ -1105,7 +1109,7 @@ int autotune(fansgpu_ctx *ctx)
             tp.nrhs            = rhs_tuned;
             tp.active          = nullptr;
             FANS_CUDA_CHECK(tune_convolution_reg<float>(tp, ctx->r32, ctx->Kd32, tscal, ctx->red, SITE_CONV, ctx->st));
-            c.v32[0] = tp.var_z;
+            c.v32[0] = tp.var_z + 2 * tp.fuse_zy;
             c.v32[1] = tp.var_y;
             c.v32[2] = tp.var_x;
             if (ctx->use_tc && ctx->tune == 3)
@@ -1908,12 +1912,15 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
             ctx->tune = 0;
         else if (std::strcmp(ev, "all") == 0)
             ctx->tune = 3;
-        else if (std::strlen(ev) == 3 && std::strspn(ev, "01") >= 2 && std::strchr("012", ev[2])) {
+        else if (std::strlen(ev) == 3 && std::strchr("0123", ev[0]) && std::strchr("01", ev[1]) &&
+                 std::strchr("012", ev[2])) {
             ctx->tune = 2;
             for (int k = 0; k < 3; ++k)
                 ctx->tune_force[k] = ev[k] - '0';
         }
     }
+    if (const char *ev = std::getenv("FANSGPU_SPECTRAL_DOT")) // "0": the FP32 <r, s> from r and s in the z pass
+        ctx->spectral_dot = std::strcmp(ev, "0") != 0;
     if (const char *ev = std::getenv("FANSGPU_EXACT")) // "df": FP64-accurate products on the CUDA cores
         ctx->exact_tc = std::strcmp(ev, "df") != 0;
     if (const char *ev = std::getenv("FANSGPU_FP64_OPERATOR")) // "dfma": the FP64 CG operator on the FP64 pipe
@@ -2049,6 +2056,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
         return bail(rc);
     if (mixed && ctx->cp32.use_reg && make_x_tma_maps(ctx->cp32, &ctx->tmaps))
         ctx->cp32.tma = &ctx->tmaps;
+    if (mixed && ctx->cp32.use_reg) // the FP32 <r, s> from the spectra (FANSGPU_SPECTRAL_DOT=0: from r and s)
+        ctx->cp32.spectral_dot = ctx->spectral_dot ? 1 : 0;
     *out = ctx;
     return 0;
 }
@@ -2180,7 +2189,7 @@ int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out)
     const ConvPlan<float>  &b = ctx->cp32;
     // the FP64-accurate operator: of the FP64 CG iterations, else of the mixed path's true residual
     const bool fp64_pipe = ctx->desc.precision != FANSGPU_MIXED && !(ctx->fp64_df && ctx->all_linear && !ctx->vscale);
-    const int32_t v[8] = {a.var_z, a.var_y, a.var_x, b.var_z, b.var_y, b.var_x,
+    const int32_t v[8] = {a.var_z, a.var_y, a.var_x, b.var_z + 2 * b.fuse_zy, b.var_y, b.var_x,
                          ctx->use_tcb ? 2 : ctx->use_tc ? 1 : 0, fp64_pipe ? 0 : ctx->use_tcx ? 2 : 1};
     for (int k = 0; k < 8; ++k)
         out[k] = v[k];

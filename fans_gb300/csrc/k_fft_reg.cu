@@ -31,6 +31,43 @@ struct Tiles {
     static constexpr int z[2] = {sizeof(T) == 4 ? 256 : 128, sizeof(T) == 4 ? 128 : 64};
 };
 
+// <r, s> of a reducing convolution from the spectra, by Parseval: with r^ the forward spectrum
+// and y^ = G r^ (G holding 1/N), s = sign * c2r(y^) unnormalised gives <r, s> = sign * sum over
+// the full spectrum of Re(r^ conj y^); on the half spectrum kz = 1..M-1 count twice (the
+// conjugate half has equal terms), kz = 0 and M once.
+__device__ __forceinline__ int dot_weight(int kz, int M) { return (kz == 0 || kz == M) ? 1 : 2; }
+
+// this thread's per-RHS partial sums -> block -> grid partials; the last block sets delta0 <-
+// delta, delta <- <r, s>, beta = max(0, (delta - deltamid) / delta0) per active RHS
+// (solverCG.h:86-94), as the z-inverse pass does for the spatial dot
+template <typename T>
+__device__ void conv_dot_finish(const double (&dk)[kMaxRhs], const ConvPlan<T> &p, const ConvArgs &a,
+                                double *red_smem)
+{
+    double vv[kMaxRhs];
+    int    ops[kMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) {
+        vv[q]  = a.sign * dk[q];
+        ops[q] = RED_SUM;
+    }
+    block_reduce<kMaxRhs>(vv, ops, red_smem);
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    if (grid_partial_commit<kMaxRhs>(vv, a.red.partials, a.red.counter + a.red_site, nb)) {
+        grid_final<kMaxRhs>(vv, ops, a.red.partials, nb, red_smem);
+        if (threadIdx.x == 0)
+            for (int q = 0; q < p.nrhs; ++q) {
+                if (p.active && !p.active[q])
+                    continue;
+                CgScalars *sc = a.scal + q;
+                sc->delta0    = sc->delta;
+                sc->delta     = vv[q];
+                double beta   = (sc->delta - sc->deltamid) / sc->delta0;
+                sc->beta      = beta > 0.0 ? beta : 0.0;
+            }
+    }
+}
+
 // ------------------------------------------------------------------ y pass ---
 template <typename T, int N1, int N2, bool INV, int KC>
 __global__ void __launch_bounds__(KC * N1) k_y_reg(ConvPlan<T> p)
@@ -78,8 +115,14 @@ struct KXCtas { // resident CTAs per SM the register budget is set for
 };
 
 template <typename T, int N1, int N2, int C, int KC>
-__global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_reg(ConvPlan<T> p)
+__global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_reg(ConvPlan<T> p, ConvArgs a)
 {
+    __shared__ double red_smem[32 * kMaxRhs];
+    const bool        sdot = p.spectral_dot && a.reduce;
+    double            dk[kMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q)
+        dk[q] = 0.0;
     constexpr int n = N1 * N2, NT = C * (C + 1) / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T>  *F  = reinterpret_cast<cplx<T> *>(smem_raw);        // [C][n][KC]
@@ -152,6 +195,7 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
         __syncthreads();
 
         // Green's operator: C x C real symmetric per frequency (solver.h:400-406)
+        T dsum = (T)0;
         for (int i = t; i < n * KC; i += blockDim.x) {
             const int kx = i / KC, ll = i % KC;
             if (ll >= nk)
@@ -161,10 +205,10 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
 #pragma unroll
             for (int q = 0; q < NT; ++q)
                 gm[q] = g[q];
-            cplx<T> a[C], o[C];
+            cplx<T> fr[C], o[C];
 #pragma unroll
             for (int c = 0; c < C; ++c)
-                a[c] = F[((size_t)c * n + kx) * KC + ll];
+                fr[c] = F[((size_t)c * n + kx) * KC + ll];
 #pragma unroll
             for (int r = 0; r < C; ++r) {
                 cplx<T> acc = {0, 0};
@@ -172,15 +216,27 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
                 for (int c = 0; c < C; ++c) {
                     const int ia = r > c ? r : c, ib = r > c ? c : r;
                     const T   gv = gm[ia * (ia + 1) / 2 + ib];
-                    acc.x += gv * a[c].x;
-                    acc.y += gv * a[c].y;
+                    acc.x += gv * fr[c].x;
+                    acc.y += gv * fr[c].y;
                 }
                 o[r] = acc;
             }
 #pragma unroll
             for (int c = 0; c < C; ++c)
                 F[((size_t)c * n + kx) * KC + ll] = o[c];
+            if (sdot) {
+                T dd = (T)0;
+#pragma unroll
+                for (int c = 0; c < C; ++c)
+                    dd += fr[c].x * o[c].x + fr[c].y * o[c].y;
+                dsum += (T)dot_weight(kz0 + ll, p.M) * dd;
+            }
         }
+        if (sdot)
+#pragma unroll
+            for (int q = 0; q < kMaxRhs; ++q)
+                if (q == k)
+                    dk[q] += (double)dsum;
         __syncthreads();
 
         // inverse FFT along x
@@ -205,6 +261,8 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
         }
         __syncthreads(); // F is reused by the next right-hand side
     }
+    if (sdot)
+        conv_dot_finish<T>(dk, p, a, red_smem);
 }
 
 // ------------------------------------------- x pass + Green's op, TMA-fed ---
@@ -289,6 +347,11 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
 
     const int t = threadIdx.x, comp = t / (KX * N1), rem = t % (KX * N1), w = rem / KX, l = rem % KX;
     const int ny = p.g.ny, ntz = (p.nzh + KX - 1) / KX;
+    const bool sdot = p.spectral_dot && a.reduce;
+    double     dk[kMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q)
+        dk[q] = 0.0;
     if (t == 0) {
         int nact = 0;
         for (int k = 0; k < p.nrhs; ++k)
@@ -305,12 +368,14 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
     const int       nact = s_act[0];
     const long long J    = (long long)ntz * ny * nact;
     const long long jb   = J * blockIdx.x / gridDim.x, je = J * (blockIdx.x + 1) / gridDim.x;
-    if (nact == 0 || jb >= je || *abort_flag) {
+    if (nact == 0 || *abort_flag) { // uniform over the grid: no CTA commits reduction partials
         if (*abort_flag && t == 0 && a.scal)
             for (int kk = 0; kk < nact; ++kk)
                 a.scal[s_act[1 + kk]].converged = -3;
         return; // no copy was issued
     }
+    // a CTA may have no jobs when converged RHS left fewer jobs than CTAs: it still commits its
+    // (zero) partials of the spectral <r, s> below
     const int nq = (int)(je - jb);
 
     // thread 0 only: issue the copies of job q (into buffer q & 1) or of job q's Green's slice
@@ -332,7 +397,7 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
         tma_load3(sb + L::OFF_G, &tm_green, kz0 * NT, ky, 0, bar_green);
         ++iss[2];
     };
-    if (t == 0) {
+    if (t == 0 && nq > 0) {
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_spec)) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm_green)) : "memory");
         issue_green(0);
@@ -396,11 +461,12 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
 
         // Green's operator (solver.h:400-406), row `comp` of the C x C real symmetric block per
         // frequency, fused into the inverse transform's load
+        float dsum = 0.f;
 #pragma unroll
         for (int j2 = 0; j2 < N2; ++j2) {
             const int    kx = w + N1 * j2;
             const float *g  = Gs + ((size_t)kx * KX + l) * NT;
-            cplx<float>  acc = {0, 0};
+            cplx<float>  acc = {0, 0}, xc = {0, 0};
 #pragma unroll
             for (int c = 0; c < C; ++c) {
                 const int         ia = comp > c ? comp : c, ib = comp > c ? c : comp;
@@ -408,9 +474,17 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
                 const cplx<float> x  = F[((size_t)c * n + kx) * KX + l];
                 acc.x += gv * x.x;
                 acc.y += gv * x.y;
+                if (c == comp)
+                    xc = x;
             }
             v[j2] = acc;
+            dsum += xc.x * acc.x + xc.y * acc.y;
         }
+        if (sdot)
+#pragma unroll
+            for (int q = 0; q < kMaxRhs; ++q)
+                if (q == k)
+                    dk[q] += (double)((float)dot_weight(kz0 + l, p.M) * dsum);
         __syncthreads(); // F and the Green's slice are read
         if (t == 0 && last_of_tile && q + 1 < nq && !*abort_flag) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -454,6 +528,8 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
             for (int kk = 0; kk < nact; ++kk)
                 a.scal[s_act[1 + kk]].converged = -3; // a copy of the TMA-fed x pass did not arrive
     }
+    if (sdot) // every CTA of the grid commits
+        conv_dot_finish<float>(dk, p, a, reinterpret_cast<double *>(xsm + L::OFF_F));
 }
 
 // ------------------------------------------------------------------ z fwd ---
@@ -516,6 +592,166 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
     }
 }
 
+// ------------------------------------------- fused z + y forward, cluster ---
+// r2c along z and the complex FFT along y of one (RHS, component, x) plane in one
+// pass, so the half spectrum after z is never written to and read back from HBM.
+// A plane of ny rows does not fit one CTA's shared memory at 256^2, so a cluster
+// of CL CTAs holds it: CTA h loads rows [h RY, (h+1) RY), RY = ny / CL, with
+// 16-byte cp.async and transforms them along z in place (rows of ZS = M + 2
+// complex; the half-length FFT as in k_z_fwd_reg, then the unpack to kz = 0..M
+// by (k, M - k) pairs, each pair by one thread).  After a cluster barrier, CTA h
+// runs the y FFTs of the kz tiles h, h + CL, ... (KC columns, 256 / N1y threads
+// per line), reading the rows of every CTA of the cluster through distributed
+// shared memory, and writes the spectrum plane [ky][kz] (stride nzp) once.  A
+// last cluster barrier keeps every CTA's rows alive until its peers have read
+// them.  The arithmetic per value is that of k_z_fwd_reg and k_y_reg.
+template <int N1z, int N2z, int N1y, int N2y, int CL>
+struct ZyFwd {
+    static constexpr int NT = 256, M = N1z * N2z, NY = N1y * N2y, RY = NY / CL, ZS = M + 2;
+    static constexpr int RZ = NT / N1z, EPz = N1z + 1, KC = NT / N1y;
+    static constexpr int EX_Z = RZ * N2z * EPz, EX_Y = NY * KC;
+    static constexpr int SMEM = (RY * ZS + (EX_Z > EX_Y ? EX_Z : EX_Y)) * 8;
+};
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ cplx<float> ld_dsmem(uint32_t local_addr, uint32_t rank)
+{
+    uint32_t    ra;
+    cplx<float> v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(local_addr), "r"(rank));
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra) : "memory");
+    return v;
+}
+
+template <int N1z, int N2z, int N1y, int N2y, int CL>
+__global__ void __launch_bounds__(256, 2) k_zy_fwd(ConvPlan<float> p, const float *__restrict__ r)
+{
+    using L = ZyFwd<N1z, N2z, N1y, N2y, CL>;
+    constexpr int M = L::M, NY = L::NY, RY = L::RY, ZS = L::ZS, RZ = L::RZ, EPz = L::EPz, KC = L::KC;
+    extern __shared__ __align__(16) unsigned char zysm[];
+    cplx<float> *Zs = reinterpret_cast<cplx<float> *>(zysm); // [RY][ZS]
+    cplx<float> *Ex = Zs + RY * ZS;                          // exchange (z) / line staging (y)
+    uint32_t     rank;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    const long long plane = blockIdx.x / CL;                  // (rhs * C + c) * nx + x
+    const int       t     = threadIdx.x;
+    const long long ppr   = (long long)p.C * p.g.nx;          // planes per right-hand side
+    if (p.active && !p.active[plane / ppr])
+        return; // the whole cluster leaves: its RHS is inactive
+
+    // rows [rank * RY, rank * RY + RY) of the plane, 16-byte copies into rows of ZS complex
+    {
+        const float *src = r + plane * (long long)NY * (2 * M) + (long long)rank * RY * (2 * M);
+        for (int i = t; i < RY * (M / 2); i += L::NT) {
+            const int row = i / (M / 2), q = i % (M / 2); // q: 16-byte chunk (2 complex) of the row
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                             (uint32_t)__cvta_generic_to_shared(Zs + row * ZS + 2 * q)),
+                         "l"(src + (long long)row * (2 * M) + 4 * q)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_all;" ::: "memory");
+        __syncthreads();
+    }
+
+    // r2c along z, RZ rows at a time
+    {
+        const int Lr = t / N1z, w = t % N1z;
+        for (int r0 = 0; r0 < RY; r0 += RZ) {
+            const int    row = r0 + Lr;
+            const bool   ok  = row < RY;
+            cplx<float> *Zr  = Zs + (ok ? row : 0) * ZS;
+            cplx<float>  v[N2z];
+#pragma unroll
+            for (int j2 = 0; j2 < N2z; ++j2)
+                v[j2] = ok ? Zr[w + N1z * j2] : cplx<float>{0, 0};
+            line_phase1<float, N1z, N2z, false>(v, w, p.tw_z);
+#pragma unroll
+            for (int k2 = 0; k2 < N2z; ++k2)
+                Ex[(Lr * N2z + k2) * EPz + w] = v[k2];
+            __syncthreads();
+            if (w < N2z && ok) {
+                cplx<float> u[N1z];
+#pragma unroll
+                for (int j1 = 0; j1 < N1z; ++j1)
+                    u[j1] = Ex[(Lr * N2z + w) * EPz + j1];
+                Dft<float, N1z, false>::run(u);
+#pragma unroll
+                for (int k1 = 0; k1 < N1z; ++k1)
+                    Zr[w + N2z * k1] = u[k1]; // the row's inputs were all read before the barrier
+            }
+            __syncthreads();
+            // unpack to the half spectrum in place: the pair (k, M - k) by one thread
+            for (int i = t; i < RZ * (M / 2 + 1); i += L::NT) {
+                const int rr = r0 + i / (M / 2 + 1), k = i % (M / 2 + 1);
+                if (rr >= RY)
+                    continue;
+                cplx<float> *Z  = Zs + rr * ZS;
+                const int    km = k == 0 ? 0 : M - k;
+                const cplx<float> a = Z[k], b = Z[km];
+                auto out = [&](cplx<float> zk, cplx<float> zm, int kk) {
+                    zm.y = -zm.y;
+                    cplx<float> Ev = {0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y)};
+                    cplx<float> Od = {0.5f * (zk.x - zm.x), 0.5f * (zk.y - zm.y)};
+                    cplx<float> P  = cmul(p.tw_r2c[kk], Od);
+                    return cplx<float>{Ev.x + P.y, Ev.y - P.x};
+                };
+                if (k == 0) {
+                    Z[0] = out(a, a, 0);
+                    Z[M] = out(a, a, M);
+                } else if (k == M / 2) {
+                    Z[k] = out(a, a, k);
+                } else {
+                    Z[k]  = out(a, b, k);
+                    Z[km] = out(b, a, km);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    cluster_sync_all(); // every CTA's rows hold their half spectra
+
+    // FFT along y of this CTA's kz tiles, the rows of the whole cluster through DSMEM
+    {
+        const int       w = t / KC, l = t % KC;
+        const uint32_t  zbase = (uint32_t)__cvta_generic_to_shared(Zs);
+        cplx<float>    *out   = p.spec + plane * (long long)NY * p.nzp;
+        const int       ntz   = (M + 1 + KC - 1) / KC;
+        for (int tz = (int)rank; tz < ntz; tz += CL) {
+            const int  kz    = tz * KC + l;
+            const bool valid = kz <= M;
+            cplx<float> v[N2y];
+#pragma unroll
+            for (int j2 = 0; j2 < N2y; ++j2) {
+                const int y = w + N1y * j2;
+                v[j2]       = valid ? ld_dsmem(zbase + (uint32_t)(((y % RY) * ZS + kz) * 8), (uint32_t)(y / RY))
+                                    : cplx<float>{0, 0};
+            }
+            line_phase1<float, N1y, N2y, false>(v, w, p.tw_y);
+#pragma unroll
+            for (int k2 = 0; k2 < N2y; ++k2)
+                Ex[(k2 * N1y + w) * KC + l] = v[k2];
+            __syncthreads();
+            if (w < N2y) {
+                cplx<float> u[N1y];
+#pragma unroll
+                for (int j1 = 0; j1 < N1y; ++j1)
+                    u[j1] = Ex[(w * N1y + j1) * KC + l];
+                Dft<float, N1y, false>::run(u);
+                if (valid)
+#pragma unroll
+                    for (int k1 = 0; k1 < N1y; ++k1)
+                        out[(long long)(w + N2y * k1) * p.nzp + kz] = u[k1];
+            }
+            __syncthreads();
+        }
+    }
+    cluster_sync_all(); // peers may still read this CTA's rows until here
+}
+
 // ------------------------------------------------------------------ z inv ---
 // Hermitian pack of the half spectrum, half-length inverse, real rows scaled by
 // `sign`; fused partial <r, s> (solverCG.h:90-92) with delta/beta in the last block.
@@ -526,16 +762,29 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
 template <typename T, int N1, int N2, int R>
 __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
 {
-    constexpr int M = N1 * N2, EP = N1 + 1, XS = R * (M + N2); // spectrum rows (stride M+1), then the exchange
+    constexpr int M = N1 * N2, EP = N1 + 1;
+    // spectrum rows at their global stride nzp (>= M + N2, so the exchange fits in a block's rows)
+    const int     XS = R * p.nzp;
     extern __shared__ __align__(16) unsigned char zsm[];
     cplx<T>          *Xb = reinterpret_cast<cplx<T> *>(zsm); // [2][XS]
-    cplx<T>          *Rb = Xb + 2 * XS;                      // [2][R*M] r rows
-    cplx<T>          *Zp = Rb + 2 * R * M;                   // [R*M] packed half-length rows
+    cplx<T>          *Zp = Xb + 2 * XS;                      // [R*M] packed half-length rows
+    cplx<T>          *Rb = Zp + R * M;                       // [2][R*M] r rows (fused dot only)
     __shared__ double red_smem[32 * kMaxRhs];
+    __shared__ __align__(8) uint64_t zbar[2];                // block copies of buffer 0 / 1
+    __shared__ int    s_abort;
+    volatile int     *abort_flag = &s_abort;
     const int       t = threadIdx.x, L = t / N1, w = t % N1;
     const long long rpr   = (long long)p.C * p.g.nx * p.g.ny; // rows per right-hand side
     const long long nrows = rpr * p.nrhs;
     const long long nblk  = (nrows + R - 1) / R;
+    const uint32_t  bar0  = (uint32_t)__cvta_generic_to_shared(&zbar[0]);
+    if (t == 0) {
+        s_abort = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
     // a block's rows belong to at most two right-hand sides (as in k_z_fwd_reg); a block is
     // skipped when all its rows belong to inactive ones
     auto live = [&](long long blk) {
@@ -545,33 +794,31 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
         const long long last = min(blk * R + R, nrows) - 1;
         return p.active[k0] || (last >= (k0 + 1) * rpr && p.active[k0 + 1]);
     };
+    // the block's spectrum rows (and r rows) are contiguous in global memory: one bulk copy each
+    // by thread 0, completing on the buffer's mbarrier
+    int waited[2] = {0, 0}; // block copies per buffer waited for (every thread keeps the count)
+    int sent[2]   = {0, 0}; // block copies per buffer issued (thread 0; none after an abort)
     auto fetch = [&](long long blk, int b) {
-        if (blk < nblk && live(blk)) {
-            const long long row0 = blk * R;
-            const int       nval = (int)(nrows - row0 < R ? nrows - row0 : R);
-            cplx<T>        *X    = Xb + b * XS;
-            for (int i = t; i < R * (M + 1); i += blockDim.x) {
-                const int Lr = i / (M + 1), k = i % (M + 1);
-                if (Lr < nval)
-                    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
-                                     (uint32_t)__cvta_generic_to_shared(X + i)),
-                                 "l"(p.spec + (row0 + Lr) * p.nzp + k), "n"(sizeof(cplx<T>))
-                                 : "memory");
-                else
-                    X[i] = cplx<T>{0, 0};
-            }
-            if (a.reduce) {
-                constexpr int  Q    = 16 / (int)sizeof(cplx<T>); // complex values per 16-byte copy
-                const cplx<T> *rin0 = reinterpret_cast<const cplx<T> *>(a.r) + row0 * M;
-                cplx<T>       *Rr   = Rb + b * R * M;
-                for (int i = t * Q; i < nval * M; i += blockDim.x * Q)
-                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                                     (uint32_t)__cvta_generic_to_shared(Rr + i)),
-                                 "l"(rin0 + i)
-                                 : "memory");
-            }
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
+        if (t != 0 || blk >= nblk || !live(blk) || *abort_flag)
+            return;
+        ++sent[b];
+        const long long row0  = blk * R;
+        const int       nval  = (int)(nrows - row0 < R ? nrows - row0 : R);
+        const uint32_t  bytes = (uint32_t)(nval * p.nzp * sizeof(cplx<T>));
+        const uint32_t  rbyt  = a.reduce ? (uint32_t)(nval * M * sizeof(cplx<T>)) : 0u;
+        const uint32_t  bar   = bar0 + 8 * b;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tma_expect(bar, bytes + rbyt);
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(Xb + b * XS)),
+                     "l"(p.spec + row0 * p.nzp), "r"(bytes), "r"(bar)
+                     : "memory");
+        if (a.reduce)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    (uint32_t)__cvta_generic_to_shared(Rb + b * R * M)),
+                "l"(reinterpret_cast<const cplx<T> *>(a.r) + row0 * M), "r"(rbyt), "r"(bar)
+                : "memory");
     };
     T dotk[kMaxRhs]; // <r, s> per right-hand side, this thread's rows
 #pragma unroll
@@ -581,17 +828,16 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
     int it = 0;
     for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++it) {
         const int b = it & 1;
-        fetch(blk + gridDim.x, b ^ 1);                       // the next block, into the other buffer
-        asm volatile("cp.async.wait_group 1;" ::: "memory"); // this block's copies (this thread's) ...
-        __syncthreads();                                     // ... and everyone else's
+        fetch(blk + gridDim.x, b ^ 1); // the next block, into the other buffer (read two blocks ago)
         if (!live(blk))
             continue; // uniform across the CTA: nothing was fetched for it
+        tma_bar_wait(bar0 + 8 * b, (uint32_t)(waited[b]++ & 1), abort_flag);
         cplx<T>        *X    = Xb + b * XS;
         const long long row0 = blk * R;
         for (int i = t; i < R * M; i += blockDim.x) {
             const int Lr = i / M, k = i % M;
-            cplx<T>   xk = X[Lr * (M + 1) + k];
-            cplx<T>   xm = X[Lr * (M + 1) + (M - k)];
+            cplx<T>   xk = X[Lr * p.nzp + k];
+            cplx<T>   xm = X[Lr * p.nzp + (M - k)];
             if (k == 0) {
                 xk.y = 0;
                 xm.y = 0;
@@ -602,7 +848,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
             Zp[i]      = cplx<T>{Ev.x - Od.y, Ev.y + Od.x};
         }
         __syncthreads();
-        cplx<T> *E = X; // the spectrum rows are consumed: reuse as the exchange (R * N2 * EP = XS)
+        cplx<T> *E = X; // the spectrum rows are consumed: reuse as the exchange (R * N2 * EP <= XS)
         cplx<T>  v[N2];
 #pragma unroll
         for (int j2 = 0; j2 < N2; ++j2)
@@ -642,7 +888,19 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
         }
         __syncthreads(); // buffers b and Zp are free for the fetch two blocks on
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    if (t == 0 && *abort_flag) {
+        // wait (bounded) for the copies still in flight, then report the expired wait
+        for (int b = 0; b < 2; ++b)
+            if (sent[b] > 0)
+                for (unsigned n = 0;
+                     n < kTmaWaitLimit && !tma_bar_try(bar0 + 8 * b, (uint32_t)((sent[b] - 1) & 1)); ++n)
+                    ;
+        if (a.scal)
+            for (int q = 0; q < p.nrhs; ++q)
+                if (!p.active || p.active[q])
+                    a.scal[q].converged = -3;
+    }
     if (a.reduce) {
         double vv[kMaxRhs];
         int    ops[kMaxRhs];
@@ -677,7 +935,7 @@ void go_y(const ConvPlan<T> &p, cudaStream_t st)
 }
 
 template <typename T, int N1, int N2, int KC>
-cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
+cudaError_t go_x(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
 {
     dim3         g((p.nzh + KC - 1) / KC, p.g.ny);
     const size_t n = (size_t)N1 * N2;
@@ -686,13 +944,13 @@ cudaError_t go_x(const ConvPlan<T> &p, cudaStream_t st)
         cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 1, KC>);
         if (e != cudaSuccess)
             return e;
-        k_x_green_reg<T, N1, N2, 1, KC><<<g, KC * N1, sm, st>>>(p);
+        k_x_green_reg<T, N1, N2, 1, KC><<<g, KC * N1, sm, st>>>(p, a);
     } else {
         const size_t sm = sizeof(cplx<T>) * 3 * n * KC + sizeof(T) * n * KC * 6;
         cudaError_t  e  = allow_max_dyn_smem(k_x_green_reg<T, N1, N2, 3, KC>);
         if (e != cudaSuccess)
             return e;
-        k_x_green_reg<T, N1, N2, 3, KC><<<g, 3 * KC * N1, sm, st>>>(p);
+        k_x_green_reg<T, N1, N2, 3, KC><<<g, 3 * KC * N1, sm, st>>>(p, a);
     }
     return cudaSuccess;
 }
@@ -749,19 +1007,21 @@ cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
-    const size_t sm = sizeof(cplx<T>) * (size_t)(2 * R * (M + N2) + 3 * R * M);
+    // spectrum rows [2][R][nzp] (nzp >= M + N2: the exchange reuses them), packed rows [R][M],
+    // and r rows [2][R][M] for the fused dot
+    const size_t sm = sizeof(cplx<T>) * (size_t)(2 * R * p.nzp + R * M + (a.reduce ? 2 * R * M : 0));
     cudaError_t  e  = allow_max_dyn_smem(k_z_inv_reg<T, N1, N2, R>);
     if (e != cudaSuccess)
         return e;
-    // persistent: as many CTAs per SM as fit (at least two; shared memory allows two at 256^3,
-    // more on smaller rows), at most one per block of rows
-    static int occ = 0;
-    if (!occ) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_z_inv_reg<T, N1, N2, R>, R * N1, sm) != cudaSuccess)
-            occ = 2;
-        occ = occ < 2 ? 2 : occ;
+    // persistent: as many CTAs per SM as fit (at least two), at most one per block of rows
+    static int occ[2] = {0, 0};
+    int       &oc     = occ[a.reduce ? 1 : 0];
+    if (!oc) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, k_z_inv_reg<T, N1, N2, R>, R * N1, sm) != cudaSuccess)
+            oc = 2;
+        oc = oc < 2 ? 2 : oc;
     }
-    const int grid = (int)(nblk < (long long)occ * nsm ? nblk : (long long)occ * nsm);
+    const int grid = (int)(nblk < (long long)oc * nsm ? nblk : (long long)oc * nsm);
     k_z_inv_reg<T, N1, N2, R><<<grid, R * N1, sm, st>>>(p, a);
     return cudaSuccess;
 }
@@ -792,7 +1052,59 @@ bool with_plan_z(int n, Fn &&f)
     return n <= 128 && with_plan(n, f);
 }
 
+// the fused z + y forward pass for cubic-in-(y, z) grids (nz == ny) whose half length has a
+// register plan; CL = the smallest cluster whose CTAs fit two per SM
+template <int N1y, int N2y>
+struct ZyPick {
+    static constexpr int  NY = N1y * N2y, M = NY / 2, N1z = reg_n1(M) ? reg_n1(M) : 1, N2z = M / N1z;
+    template <int CL>
+    static constexpr bool fits = NY % CL == 0 && ZyFwd<N1z, N2z, N1y, N2y, CL>::SMEM <= 113 * 1024;
+    static constexpr int  CL = !reg_n1(M) ? 0 : fits<1> ? 1 : fits<2> ? 2 : fits<4> ? 4 : fits<8> ? 8 : 0;
+};
+
+bool zy_supported_impl(const Grid3 &g)
+{
+    bool ok = false;
+    if (g.nz == g.ny && g.nz / 2 <= 128)
+        with_plan(g.ny, [&]<int N1, int N2>() { ok = ZyPick<N1, N2>::CL != 0; });
+    return ok;
+}
+
+cudaError_t go_zy(const ConvPlan<float> &p, const float *r, cudaStream_t st)
+{
+    cudaError_t e = cudaErrorNotSupported;
+    if (p.g.nz != p.g.ny)
+        return e;
+    with_plan(p.g.ny, [&]<int N1y, int N2y>() {
+        using P = ZyPick<N1y, N2y>;
+        if constexpr (P::CL != 0) {
+            constexpr int CL = P::CL;
+            using L          = ZyFwd<P::N1z, P::N2z, N1y, N2y, CL>;
+            auto fn          = k_zy_fwd<P::N1z, P::N2z, N1y, N2y, CL>;
+            if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, L::SMEM)) != cudaSuccess)
+                return;
+            cudaLaunchConfig_t  cfg{};
+            cudaLaunchAttribute at[1];
+            at[0].id               = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = CL;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim            = dim3((unsigned)(CL * (long long)p.nrhs * p.C * p.g.nx));
+            cfg.blockDim           = dim3(L::NT);
+            cfg.dynamicSmemBytes   = L::SMEM;
+            cfg.stream             = st;
+            cfg.attrs              = at;
+            cfg.numAttrs           = 1;
+            e                      = cudaLaunchKernelEx(&cfg, fn, p, r);
+        }
+    });
+    return e;
+}
+
+
 } // namespace
+
+bool zy_supported(const Grid3 &g) { return zy_supported_impl(g); }
 
 bool conv_reg_supported(const Grid3 &g)
 {
@@ -813,13 +1125,22 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
     using TL      = Tiles<T>;
     const T *r    = reinterpret_cast<const T *>(a.r);
     mark(0);
-    with_plan_z(p.M, [&]<int N1, int N2>() {
-        p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
-    });
+    bool fused = false;
+    if constexpr (std::is_same_v<T, float>)
+        if (p.fuse_zy) {
+            if ((e = go_zy(p, r, st)) != cudaSuccess)
+                return e;
+            fused = true;
+        }
+    if (!fused)
+        with_plan_z(p.M, [&]<int N1, int N2>() {
+            p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
+        });
     mark(1);
-    with_plan(p.g.ny, [&]<int N1, int N2>() {
-        p.var_y ? go_y<T, N1, N2, false, TL::y[1]>(p, st) : go_y<T, N1, N2, false, TL::y[0]>(p, st);
-    });
+    if (!fused)
+        with_plan(p.g.ny, [&]<int N1, int N2>() {
+            p.var_y ? go_y<T, N1, N2, false, TL::y[1]>(p, st) : go_y<T, N1, N2, false, TL::y[0]>(p, st);
+        });
     mark(2);
     with_plan(p.g.nx, [&]<int N1, int N2>() {
         if constexpr (std::is_same_v<T, float>)
@@ -827,7 +1148,7 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
                 e = go_x_tma<N1, N2>(p, a, st);
                 return;
             }
-        e = p.var_x == 1 ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
+        e = p.var_x == 1 ? go_x<T, N1, N2, TL::x[1]>(p, a, st) : go_x<T, N1, N2, TL::x[0]>(p, a, st);
     });
     if (e != cudaSuccess)
         return e;
@@ -836,8 +1157,11 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
         p.var_y ? go_y<T, N1, N2, true, TL::y[1]>(p, st) : go_y<T, N1, N2, true, TL::y[0]>(p, st);
     });
     mark(4);
+    ConvArgs az = a; // with the spectral <r, s>, the z-inverse pass only transforms
+    if (p.spectral_dot)
+        az.reduce = 0;
     with_plan_z(p.M, [&]<int N1, int N2>() {
-        e = p.var_z ? go_zi<T, N1, N2, TL::z[1] / N1>(p, a, st) : go_zi<T, N1, N2, TL::z[0] / N1>(p, a, st);
+        e = p.var_z ? go_zi<T, N1, N2, TL::z[1] / N1>(p, az, st) : go_zi<T, N1, N2, TL::z[0] / N1>(p, az, st);
     });
     if (e != cudaSuccess)
         return e;
@@ -859,6 +1183,9 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
         return cudaSuccess;
     using TL = Tiles<T>;
     ConvArgs    a{r, s, 1.0, 1, scal, red, red_site, nullptr}; // with the fused <r, s>, as in the iteration
+    ConvArgs    az = a;                                        // in the x pass when spectral
+    if (p.spectral_dot)
+        az.reduce = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e  = cudaEventCreate(&e0);
     if (e == cudaSuccess)
@@ -883,10 +1210,10 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
             with_plan_z(p.M, [&]<int N1, int N2>() {
                 if (v) {
                     go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st);
-                    e = go_zi<T, N1, N2, TL::z[1] / N1>(p, a, st);
+                    e = go_zi<T, N1, N2, TL::z[1] / N1>(p, az, st);
                 } else {
                     go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
-                    e = go_zi<T, N1, N2, TL::z[0] / N1>(p, a, st);
+                    e = go_zi<T, N1, N2, TL::z[0] / N1>(p, az, st);
                 }
             });
         });
@@ -908,13 +1235,28 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
                         e = go_x_tma<N1, N2>(p, a, st);
                         return;
                     }
-                e = v ? go_x<T, N1, N2, TL::x[1]>(p, st) : go_x<T, N1, N2, TL::x[0]>(p, st);
+                e = v ? go_x<T, N1, N2, TL::x[1]>(p, a, st) : go_x<T, N1, N2, TL::x[0]>(p, a, st);
             });
         });
     p.var_x = 0;
     for (int v = 1; v < nvx; ++v)
         if (tx[v] < tx[p.var_x])
             p.var_x = v;
+    // the forward z and y passes (the chosen variants) against the fused cluster pass
+    p.fuse_zy = 0;
+    if constexpr (std::is_same_v<T, float>)
+        if (zy_supported_impl(p.g)) {
+            const float t_sep = timed([&] {
+                with_plan_z(p.M, [&]<int N1, int N2>() {
+                    p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
+                });
+                with_plan(p.g.ny, [&]<int N1, int N2>() {
+                    p.var_y ? go_y<T, N1, N2, false, TL::y[1]>(p, st) : go_y<T, N1, N2, false, TL::y[0]>(p, st);
+                });
+            });
+            const float t_fused = timed([&] { e = go_zy(p, r, st); });
+            p.fuse_zy = t_fused < t_sep ? 1 : 0;
+        }
     if (e0)
         cudaEventDestroy(e0);
     if (e1)

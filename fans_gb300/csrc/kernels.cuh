@@ -221,6 +221,10 @@ struct ConvPlan {
     int            kc_y, kc_x;     // kz columns per CTA in the y / x passes
     int            use_reg;        // register-resident passes (conv_reg_supported)
     int            var_z, var_y, var_x; // register passes: tile variant (0 default, 1 the alternative)
+    int            fuse_zy;        // FP32: the forward z and y passes as one cluster pass (k_zy_fwd)
+    // register passes: the fused <r, s> of a reducing convolution is taken in the x pass from the
+    // spectra (Parseval) instead of in the z-inverse pass from r and s, which then reads no r
+    int            spectral_dot;
     // register passes over several right-hand sides: RHS k's rows follow RHS k-1's (r, s and spec
     // of nrhs consecutive fields; the Green's table is shared); active[k] == 0 skips RHS k
     int            nrhs;
@@ -260,6 +264,8 @@ template <typename T>
 size_t conv_smem_bytes(const ConvPlan<T> &p, int pass);
 // register-resident passes (line lengths with a two-phase register plan)
 bool conv_reg_supported(const Grid3 &g);
+// the fused z + y forward cluster pass exists for this grid (FP32, nz == ny)
+bool zy_supported(const Grid3 &g);
 template <typename T>
 cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st);
 // Times the register passes' tile variants on p's buffers (r in, s out) and

@@ -112,18 +112,26 @@ def _multi_solve(P, n_rhs):
     return out
 
 
-@pytest.mark.parametrize("c,shape,n_rhs", [
-    (3, (32, 32, 64), 6),   # elastic, six RHS, N1 = N2 x line, ragged last kz tile (nz/2+1 = 33)
-    (3, (48, 16, 32), 3),   # N1 != N2 (48 = 8 x 6), three RHS
-    (1, (64, 32, 48), 3),   # thermal (one component, one Green's entry per frequency)
-    (3, (128, 16, 32), 1),  # one RHS: every job starts a new tile (a Green's slice per job)
+@pytest.mark.parametrize("tiles,c,shape,n_rhs", [
+    ("002", 3, (32, 32, 64), 6),   # elastic, six RHS, N1 = N2 x line, ragged last kz tile (nz/2+1 = 33)
+    ("002", 3, (48, 16, 32), 3),   # N1 != N2 (48 = 8 x 6), three RHS
+    ("002", 1, (64, 32, 48), 3),   # thermal (one component, one Green's entry per frequency)
+    ("002", 3, (128, 16, 32), 1),  # one RHS: every job starts a new tile (a Green's slice per job)
+    # the fused z + y forward cluster pass (z entry + 2)
+    ("200", 3, (32, 32, 32), 6),   # one CTA per plane
+    ("200", 3, (48, 64, 64), 3),
+    ("200", 1, (40, 48, 48), 3),   # thermal, 48 = 8 x 6 lines in y, 24 = 8 x 3 in z
+    ("200", 3, (16, 256, 256), 1), # four CTAs per plane (rows shared through distributed shared memory)
+    ("302", 1, (16, 256, 256), 2), # with the other z-inverse tile and the TMA-fed x pass
 ])
-def test_tma_x_pass_equals_register_x_pass(monkeypatch, c, shape, n_rhs):
+def test_fft_pass_variants_equal_register_passes(monkeypatch, tiles, c, shape, n_rhs):
     """The FP32 x pass fed by tensor-map copies (x variant 2: persistent CTAs, two job
-    buffers in flight, Green's multiply fused into the inverse transform's load) runs
-    the register x pass's operations per value; only FP32 roundings may differ (the
-    compiler may fuse the Green's products with the transform's first additions).  A
-    mixed multi-RHS solve forced onto it must therefore follow the register pass's
+    buffers in flight, Green's multiply fused into the inverse transform's load) and
+    the fused z + y forward cluster pass (z entry + 2: a plane's rows transformed
+    along z in shared memory, then along y through distributed shared memory) run
+    the register passes' operations per value; only FP32 roundings may differ (the
+    compiler may fuse products and sums differently).  A mixed multi-RHS solve
+    forced onto them must therefore follow the register passes
     residual history to FP32 accuracy in its first iterations (a wrong tile, Green's
     entry or stale buffer moves it at once by far more), take the same refreshes and
     the same iterations within one (the mixed path's bar against the oracle), and
@@ -135,9 +143,9 @@ def test_tma_x_pass_equals_register_x_pass(monkeypatch, c, shape, n_rhs):
     P = oracle_problem(ms, c, ELASTIC if c == 3 else THERMAL, "HEX8")
     monkeypatch.setenv("FANSGPU_TUNE", "000")
     ref = _multi_solve(P, n_rhs)
-    monkeypatch.setenv("FANSGPU_TUNE", "002")
+    monkeypatch.setenv("FANSGPU_TUNE", tiles)
     got = _multi_solve(P, n_rhs)
-    assert ref["tuning"] == (0, 0, 0) and got["tuning"] == (0, 0, 2)
+    assert ref["tuning"] == (0, 0, 0) and got["tuning"] == tuple(int(v) for v in tiles)
     assert ref["agg"][1] and got["agg"][1] and abs(got["agg"][0] - ref["agg"][0]) <= 1
     for k in range(n_rhs):
         i0, r0, h0, s0, u0 = ref[k]
