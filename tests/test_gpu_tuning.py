@@ -1,7 +1,9 @@
 """Autotuned tile shapes (FANSGPU_TUNE; the tuner runs on a context's first
-setup).  Every forced combination of the register FFT passes' variants (z, y, x)
-gives the bitwise-same FP64 convolution and the same mixed-precision solve; the
-default (tuned) context agrees with the oracle."""
+setup).  Every forced combination of the register FFT passes' variants (z, y, x;
+z + 4: the persistent bulk-copy forward z pass) gives the bitwise-same FP64
+convolution and the same mixed-precision solve; the FP32-only variants (z + 2:
+fused z + y forward cluster pass, x = 2: TMA-fed x pass) follow the register
+passes to FP32 rounding; the default (tuned) context agrees with the oracle."""
 import numpy as np
 import pytest
 
@@ -18,7 +20,7 @@ def _problem():
     return oracle_problem(ms, 3, ELASTIC, "HEX8")
 
 
-@pytest.mark.parametrize("tiles", ["000", "100", "010", "001", "111"])
+@pytest.mark.parametrize("tiles", ["000", "100", "010", "001", "111", "400", "501", "003", "113"])
 def test_forced_tile_variants_agree(tiles, monkeypatch):
     monkeypatch.setenv("FANSGPU_TUNE", tiles)
     P = _problem()
@@ -123,6 +125,10 @@ def _multi_solve(P, n_rhs):
     ("200", 1, (40, 48, 48), 3),   # thermal, 48 = 8 x 6 lines in y, 24 = 8 x 3 in z
     ("200", 3, (16, 256, 256), 1), # four CTAs per plane (rows shared through distributed shared memory)
     ("302", 1, (16, 256, 256), 2), # with the other z-inverse tile and the TMA-fed x pass
+    # the persistent forward z pass fed by bulk copies (z entry + 4)
+    ("400", 3, (32, 32, 64), 6),
+    ("502", 1, (64, 32, 48), 3),
+    ("402", 3, (48, 16, 32), 3),
 ])
 def test_fft_pass_variants_equal_register_passes(monkeypatch, tiles, c, shape, n_rhs):
     """The FP32 x pass fed by tensor-map copies (x variant 2: persistent CTAs, two job
