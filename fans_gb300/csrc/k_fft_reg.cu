@@ -418,6 +418,8 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
     const long long rhs_spec = (long long)p.C * n * ny * p.nzp;
     cplx<float>    *Fc       = F + (size_t)comp * n * KX;
     int             gph      = 0; // Green's slices waited for
+    // barrier of this component's KX * N1 threads (named barriers 1..C; 0 is __syncthreads)
+    auto comp_bar = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + comp), "n"(KX * N1) : "memory"); };
 
     for (int q = 0; q < nq; ++q) {
         const long long jg = jb + q;
@@ -445,7 +447,7 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2)
             Fc[(k2 * N1 + w) * KX + l] = v[k2];
-        __syncthreads();
+        comp_bar(); // the transforms of one component meet only its own warps
         cplx<float> u[N1];
         if (w < N2) {
 #pragma unroll
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
                 u[j1] = Fc[(w * N1 + j1) * KX + l];
             Dft<float, N1, false>::run(u);
         }
-        __syncthreads();
+        comp_bar();
         if (w < N2)
 #pragma unroll
             for (int k1 = 0; k1 < N1; ++k1)
@@ -504,7 +506,7 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2)
             Fc[(k2 * N1 + w) * KX + l] = v[k2];
-        __syncthreads();
+        comp_bar();
         if (w < N2) {
 #pragma unroll
             for (int j1 = 0; j1 < N1; ++j1)
