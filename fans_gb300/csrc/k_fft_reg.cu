@@ -544,6 +544,7 @@ template <typename T, int N1, int N2, int R>
 __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__restrict__ r)
 {
     constexpr int M = N1 * N2, EP = N1 + 1; // exchange row padded against bank conflicts
+    static_assert(32 % N1 == 0, "a row's workers share one warp");
     __shared__ cplx<T> E[R * N2 * EP];
     __shared__ cplx<T> Z[R * M];
     const int       t = threadIdx.x, L = t / N1, w = t % N1;
@@ -566,10 +567,11 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
     for (int j2 = 0; j2 < N2; ++j2)
         v[j2] = valid ? rin[w + N1 * j2] : cplx<T>{0, 0};
     line_phase1<T, N1, N2, false>(v, w, p.tw_z);
+    // a row's N1 <= 16 workers are lanes of one warp: its exchanges need only that warp
 #pragma unroll
     for (int k2 = 0; k2 < N2; ++k2)
         E[(L * N2 + k2) * EP + w] = v[k2];
-    __syncthreads();
+    __syncwarp();
     if (w < N2) {
         cplx<T> u[N1];
 #pragma unroll
@@ -580,21 +582,18 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
         for (int k1 = 0; k1 < N1; ++k1)
             Z[L * M + w + N2 * k1] = u[k1];
     }
-    __syncthreads();
-    // unpack to the half spectrum, k = 0..M, coalesced over k
-    const long long row0 = (long long)blockIdx.x * R;
-    for (int i = t; i < R * (M + 1); i += blockDim.x) {
-        const int Lr = i / (M + 1), k = i % (M + 1);
-        if (row0 + Lr >= nrows || !on(row0 + Lr))
-            continue;
-        cplx<T> zk = Z[Lr * M + (k == M ? 0 : k)];
-        cplx<T> zm = Z[Lr * M + (k == 0 ? 0 : M - k)];
-        zm.y       = -zm.y;
-        cplx<T> Ev = {(T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y + zm.y)};
-        cplx<T> Od = {(T)0.5 * (zk.x - zm.x), (T)0.5 * (zk.y - zm.y)};
-        cplx<T> P  = cmul(p.tw_r2c[k], Od);
-        p.spec[(row0 + Lr) * p.nzp + k] = cplx<T>{Ev.x + P.y, Ev.y - P.x};
-    }
+    __syncwarp();
+    // unpack the row to the half spectrum, k = 0..M, by its own workers (coalesced over k)
+    if (valid)
+        for (int k = w; k <= M; k += N1) {
+            cplx<T> zk = Z[L * M + (k == M ? 0 : k)];
+            cplx<T> zm = Z[L * M + (k == 0 ? 0 : M - k)];
+            zm.y       = -zm.y;
+            cplx<T> Ev = {(T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y + zm.y)};
+            cplx<T> Od = {(T)0.5 * (zk.x - zm.x), (T)0.5 * (zk.y - zm.y)};
+            cplx<T> P  = cmul(p.tw_r2c[k], Od);
+            p.spec[row * p.nzp + k] = cplx<T>{Ev.x + P.y, Ev.y - P.x};
+        }
 }
 
 // ------------------------------------------------- z fwd, bulk-copy fed ---
@@ -881,12 +880,12 @@ template <typename T, int N1, int N2, int R>
 __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
 {
     constexpr int M = N1 * N2, EP = N1 + 1;
-    // spectrum rows at their global stride nzp (>= M + N2, so the exchange fits in a block's rows)
-    const int     XS = R * p.nzp;
+    const int     XS = R * p.nzp; // spectrum rows at their global stride nzp
     extern __shared__ __align__(16) unsigned char zsm[];
+    static_assert(32 % N1 == 0, "a row's workers share one warp");
     cplx<T>          *Xb = reinterpret_cast<cplx<T> *>(zsm); // [2][XS]
-    cplx<T>          *Zp = Xb + 2 * XS;                      // [R*M] packed half-length rows
-    cplx<T>          *Rb = Zp + R * M;                       // [2][R*M] r rows (fused dot only)
+    cplx<T>          *E  = Xb + 2 * XS;                      // [R*N2*EP] exchange, per row
+    cplx<T>          *Rb = E + R * N2 * EP;                  // [2][R*M] r rows (fused dot only)
     __shared__ double red_smem[32 * kMaxRhs];
     __shared__ __align__(8) uint64_t zbar[2];                // block copies of buffer 0 / 1
     __shared__ int    s_abort;
@@ -950,32 +949,30 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
         if (!live(blk))
             continue; // uniform across the CTA: nothing was fetched for it
         tma_bar_wait(bar0 + 8 * b, (uint32_t)(waited[b]++ & 1), abort_flag);
-        cplx<T>        *X    = Xb + b * XS;
         const long long row0 = blk * R;
-        for (int i = t; i < R * M; i += blockDim.x) {
-            const int Lr = i / M, k = i % M;
-            cplx<T>   xk = X[Lr * p.nzp + k];
-            cplx<T>   xm = X[Lr * p.nzp + (M - k)];
+        // Hermitian pack of row L by its own N1 workers (lanes of one warp), straight into the
+        // registers of phase 1: only that warp meets at the exchange
+        const cplx<T> *Xr = Xb + b * XS + L * p.nzp;
+        cplx<T>        v[N2];
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2) {
+            const int k  = w + N1 * j2;
+            cplx<T>   xk = Xr[k];
+            cplx<T>   xm = Xr[M - k];
             if (k == 0) {
                 xk.y = 0;
                 xm.y = 0;
             }
-            xm.y      = -xm.y;
+            xm.y       = -xm.y;
             cplx<T> Ev = cadd(xk, xm);
             cplx<T> Od = cmulc(csub(xk, xm), p.tw_r2c[k]);
-            Zp[i]      = cplx<T>{Ev.x - Od.y, Ev.y + Od.x};
+            v[j2]      = cplx<T>{Ev.x - Od.y, Ev.y + Od.x};
         }
-        __syncthreads();
-        cplx<T> *E = X; // the spectrum rows are consumed: reuse as the exchange (R * N2 * EP <= XS)
-        cplx<T>  v[N2];
-#pragma unroll
-        for (int j2 = 0; j2 < N2; ++j2)
-            v[j2] = Zp[L * M + w + N1 * j2];
         line_phase1<T, N1, N2, true>(v, w, p.tw_z);
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2)
             E[(L * N2 + k2) * EP + w] = v[k2];
-        __syncthreads();
+        __syncwarp();
         const long long row = row0 + L;
         const int       rk0 = p.active || p.nrhs > 1 ? (int)(row0 / rpr) : 0;
         const int       rk  = rk0 + (row >= (rk0 + 1) * rpr ? 1 : 0);
@@ -1004,7 +1001,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
                 if (q == rk)
                     dotk[q] += dot;
         }
-        __syncthreads(); // buffers b and Zp are free for the fetch two blocks on
+        __syncthreads(); // buffer b is free for the fetch two blocks on
     }
     __syncthreads();
     if (t == 0 && *abort_flag) {
@@ -1144,9 +1141,9 @@ cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
-    // spectrum rows [2][R][nzp] (nzp >= M + N2: the exchange reuses them), packed rows [R][M],
-    // and r rows [2][R][M] for the fused dot
-    const size_t sm = sizeof(cplx<T>) * (size_t)(2 * R * p.nzp + R * M + (a.reduce ? 2 * R * M : 0));
+    // spectrum rows [2][R][nzp], the rows' exchange [R][N2][N1 + 1], and r rows [2][R][M] for
+    // the fused dot
+    const size_t sm = sizeof(cplx<T>) * (size_t)(2 * R * p.nzp + R * N2 * (N1 + 1) + (a.reduce ? 2 * R * M : 0));
     cudaError_t  e  = allow_max_dyn_smem(k_z_inv_reg<T, N1, N2, R>);
     if (e != cudaSuccess)
         return e;

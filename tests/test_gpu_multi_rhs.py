@@ -49,7 +49,11 @@ def _separate(P, precision, loads, tol):
     (1, THERMAL, (24, 32, 32), "mixed"),
     (3, ELASTIC, (16, 24, 32), "fp64"),
 ])
-def test_multi_rhs_equals_separate_solves(c, groups, shape, precision):
+def test_multi_rhs_equals_separate_solves(monkeypatch, c, groups, shape, precision):
+    # the autotuner's choice is cached per RHS count, and its FP32-only FFT forms agree with the
+    # register passes to FP32 rounding only: pin the register tiles so that both solves run the
+    # same kernels
+    monkeypatch.setenv("FANSGPU_TUNE", "000")
     ms = random_ms(shape, vf=0.3, seed=51)
     P = oracle_problem(ms, c, groups, "HEX8")
     loads = list(np.eye(P.nstr))
