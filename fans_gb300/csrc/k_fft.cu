@@ -325,13 +325,57 @@ __device__ bool spd_inv3(int n, const double *A, double *P)
     return true;
 }
 
+// Node offset class of d = x_p - x_q in {-1, 0, 1}^3 (x_p: the bits of node p, x first): 0 for
+// d = 0, else 1..13 for the representative of {d, -d} whose first non-zero coordinate (x, y, z
+// order) is positive, in the order of cos(theta . d) in k_green.
+__device__ __forceinline__ int offset_class(int dx, int dy, int dz)
+{
+    if (dx < 0 || (dx == 0 && (dy < 0 || (dy == 0 && dz < 0)))) {
+        dx = -dx;
+        dy = -dy;
+        dz = -dz;
+    }
+    if (dx == 0 && dy == 0)
+        return dz == 0 ? 0 : 3;
+    if (dx == 0)
+        return dz == 0 ? 2 : (dz > 0 ? 8 : 9);
+    if (dy == 0)
+        return dz == 0 ? 1 : (dz > 0 ? 6 : 7);
+    if (dy > 0)
+        return dz == 0 ? 4 : (dz > 0 ? 10 : 11);
+    return dz == 0 ? 5 : (dz > 0 ? 12 : 13);
+}
+
+// The weighted contraction of solver.h:177-186, block_ij = sum_pq K0_ij[p][q] Re(A_p conj A_q),
+// depends on the node pair only through d = x_p - x_q, since Re(A_p conj A_q) = cos(theta . d):
+// block_ij = sum_d S_ij(d) cos(theta . d) with S_ij(d) the sum of K0_ij over the pairs of
+// offset d.  cos is even, so d and -d share one term: 14 coefficients per block entry (summed
+// by every CTA from K0 in shared memory) replace the 64 products per entry and frequency.
 template <int C>
 __global__ void __launch_bounds__(256) k_green(GreenArgs a)
 {
     constexpr int NC = 8 * C, NT = C * (C + 1) / 2;
     __shared__ double K0[NC * NC];
+    __shared__ double Tc[NT * 14]; // [entry (i <= j, row-major)][offset class]
     for (int i = threadIdx.x; i < NC * NC; i += blockDim.x)
         K0[i] = a.K0c[i];
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < NT * 14; idx += blockDim.x) {
+        const int e = idx / 14, m = idx % 14;
+        int       i = 0, j = 0;
+        for (int r = 0, n = 0; r < C; ++r)
+            for (int c = r; c < C; ++c, ++n)
+                if (n == e) {
+                    i = r;
+                    j = c;
+                }
+        double acc = 0.0;
+        for (int pp = 0; pp < 8; ++pp)
+            for (int q = 0; q < 8; ++q)
+                if (offset_class((pp & 1) - (q & 1), ((pp >> 1) & 1) - ((q >> 1) & 1), (pp >> 2) - (q >> 2)) == m)
+                    acc += K0[(8 * i + pp) * NC + 8 * j + q];
+        Tc[idx] = acc;
+    }
     __syncthreads();
     const int       nx = a.g.nx, ny = a.g.ny, nz = a.g.nz, nzh = nz / 2 + 1;
     const long long F  = (long long)nx * ny * nzh;
@@ -344,27 +388,33 @@ __global__ void __launch_bounds__(256) k_green(GreenArgs a)
             for (int t = 0; t < NT; ++t)
                 out[t] = 0.0;
         } else {
-            const double exr = a.cx[ix], exi = a.sx[ix], eyr = a.cy[iy], eyi = a.sy[iy], ezr = a.cz[iz], ezi = a.sz[iz];
-            double Ar[8], Ai[8];
-            Ar[0] = 1.0; Ai[0] = 0.0;
-            Ar[1] = exr; Ai[1] = exi;
-            Ar[2] = eyr; Ai[2] = eyi;
-            Ar[3] = exr * eyr - exi * eyi; Ai[3] = exr * eyi + exi * eyr;
-            Ar[4] = ezr; Ai[4] = ezi;
-            Ar[5] = exr * ezr - exi * ezi; Ai[5] = exr * ezi + exi * ezr;
-            Ar[6] = ezr * eyr - ezi * eyi; Ai[6] = ezr * eyi + ezi * eyr;
-            Ar[7] = Ar[3] * ezr - Ai[3] * ezi; Ai[7] = Ar[3] * ezi + Ai[3] * ezr;
+            const double cx = a.cx[ix], sx = a.sx[ix], cy = a.cy[iy], sy = a.sy[iy], cz = a.cz[iz], sz = a.sz[iz];
+            const double pr = cx * cy - sx * sy, pi = sx * cy + cx * sy; // e^{i(tx + ty)}
+            const double mr = cx * cy + sx * sy, mi = sx * cy - cx * sy; // e^{i(tx - ty)}
+            const double cv[14] = {1.0,
+                                   cx,
+                                   cy,
+                                   cz,
+                                   pr,
+                                   mr,
+                                   cx * cz - sx * sz,
+                                   cx * cz + sx * sz,
+                                   cy * cz - sy * sz,
+                                   cy * cz + sy * sz,
+                                   pr * cz - pi * sz,
+                                   pr * cz + pi * sz,
+                                   mr * cz - mi * sz,
+                                   mr * cz + mi * sz};
             double blk[9], pinv[9];
+            int    e = 0;
 #pragma unroll
             for (int i = 0; i < C; ++i)
 #pragma unroll
-                for (int j = i; j < C; ++j) {
+                for (int j = i; j < C; ++j, ++e) {
                     double acc = 0.0;
 #pragma unroll
-                    for (int pp = 0; pp < 8; ++pp)
-#pragma unroll
-                        for (int q = 0; q < 8; ++q)
-                            acc += K0[(8 * i + pp) * NC + 8 * j + q] * (Ar[pp] * Ar[q] + Ai[pp] * Ai[q]);
+                    for (int m = 0; m < 14; ++m)
+                        acc += Tc[e * 14 + m] * cv[m];
                     blk[i * C + j] = acc;
                     blk[j * C + i] = acc;
                 }
