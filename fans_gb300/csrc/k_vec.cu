@@ -148,9 +148,8 @@ __global__ void __launch_bounds__(kVecThreads) k_norm_fast(const T *__restrict__
     const long long nv = n / 2;
     const double2 *r2 = reinterpret_cast<const double2 *>(r);
     float2        *o2 = reinterpret_cast<float2 *>(r_out);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
-        const double2 v = r2[i];
-        const float2  f = make_float2((float)v.x, (float)v.y);
+    auto           one = [&](const double2 v, long long i) {
+        const float2 f = make_float2((float)v.x, (float)v.y);
         if (o2)
             o2[i] = f;
         float cn;
@@ -161,7 +160,19 @@ __global__ void __launch_bounds__(kVecThreads) k_norm_fast(const T *__restrict__
         else
             cn = fabsf(f.x) + fabsf(f.y);
         nrm = mx ? nan_max(nrm, (double)cn) : nrm + (double)cn;
+    };
+    // four independent 16-byte loads in flight per thread and step, then the remainder
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long       i      = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < nv; i += 4 * stride) {
+        const double2 v0 = r2[i], v1 = r2[i + stride], v2 = r2[i + 2 * stride], v3 = r2[i + 3 * stride];
+        one(v0, i);
+        one(v1, i + stride);
+        one(v2, i + 2 * stride);
+        one(v3, i + 3 * stride);
     }
+    for (; i < nv; i += stride)
+        one(r2[i], i);
     double v[1]   = {nrm};
     int    ops[1] = {mx ? RED_MAX : RED_SUM};
     block_reduce<1>(v, ops, red_smem);
@@ -227,7 +238,28 @@ __global__ void k_extrapolate(double *__restrict__ u, double *__restrict__ up, l
 
 __global__ void k_fold(double *__restrict__ u, float *__restrict__ e, long long n)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    // four values per step with 16-byte accesses where u and e are 16-byte aligned (every
+    // field of the context is), else one at a time; the same additions either way
+    const long long stride = (long long)gridDim.x * blockDim.x, t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long       done   = 0;
+    if (((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(e)) & 15) == 0) {
+        const long long nq = n / 4;
+        double2        *u2 = reinterpret_cast<double2 *>(u);
+        float4         *e4 = reinterpret_cast<float4 *>(e);
+        for (long long i = t0; i < nq; i += stride) {
+            const float4 ev = e4[i];
+            double2      a  = u2[2 * i], b = u2[2 * i + 1];
+            a.x += (double)ev.x;
+            a.y += (double)ev.y;
+            b.x += (double)ev.z;
+            b.y += (double)ev.w;
+            u2[2 * i]     = a;
+            u2[2 * i + 1] = b;
+            e4[i]         = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        done = 4 * nq;
+    }
+    for (long long i = done + t0; i < n; i += stride) {
         u[i] += (double)e[i];
         e[i] = 0.0f;
     }
