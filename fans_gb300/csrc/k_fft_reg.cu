@@ -876,8 +876,10 @@ __global__ void __launch_bounds__(256, 2) k_zy_fwd(ConvPlan<float> p, const floa
 // transformed cp.async brings the next block's spectrum rows (and, for the
 // fused dot, its r rows) into the other buffer, so the DRAM reads overlap the
 // transforms instead of alternating with them.
-template <typename T, int N1, int N2, int R>
-__global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
+// RED: the pass takes the fused <r, s> (FP64 path, FANSGPU_SPECTRAL_DOT=0); without it the
+// reduction and the r rows are compiled out, and more CTAs fit an SM
+template <typename T, int N1, int N2, int R, bool RED>
+__global__ void __launch_bounds__(R * N1, RED ? 2 : 4) k_z_inv_reg(ConvPlan<T> p, ConvArgs a)
 {
     constexpr int M = N1 * N2, EP = N1 + 1;
     const int     XS = R * p.nzp; // spectrum rows at their global stride nzp
@@ -922,7 +924,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
         const long long row0  = blk * R;
         const int       nval  = (int)(nrows - row0 < R ? nrows - row0 : R);
         const uint32_t  bytes = (uint32_t)(nval * p.nzp * sizeof(cplx<T>));
-        const uint32_t  rbyt  = a.reduce ? (uint32_t)(nval * M * sizeof(cplx<T>)) : 0u;
+        const uint32_t  rbyt  = RED ? (uint32_t)(nval * M * sizeof(cplx<T>)) : 0u;
         const uint32_t  bar   = bar0 + 8 * b;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tma_expect(bar, bytes + rbyt);
@@ -930,7 +932,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
                          (uint32_t)__cvta_generic_to_shared(Xb + b * XS)),
                      "l"(p.spec + row0 * p.nzp), "r"(bytes), "r"(bar)
                      : "memory");
-        if (a.reduce)
+        if (RED)
             asm volatile(
                 "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                     (uint32_t)__cvta_generic_to_shared(Rb + b * R * M)),
@@ -991,7 +993,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
                 const int m = w + N2 * k1;
                 cplx<T>   z = {sg * u[k1].x, sg * u[k1].y};
                 sout[m]     = z;
-                if (a.reduce) {
+                if (RED) {
                     const cplx<T> rv = rr[m];
                     dot += rv.x * z.x + rv.y * z.y;
                 }
@@ -1016,7 +1018,7 @@ __global__ void __launch_bounds__(R * N1, 2) k_z_inv_reg(ConvPlan<T> p, ConvArgs
                 if (!p.active || p.active[q])
                     a.scal[q].converged = -3;
     }
-    if (a.reduce) {
+    if (RED) {
         double vv[kMaxRhs];
         int    ops[kMaxRhs];
 #pragma unroll
@@ -1144,19 +1146,20 @@ cudaError_t go_zi(const ConvPlan<T> &p, const ConvArgs &a, cudaStream_t st)
     // spectrum rows [2][R][nzp], the rows' exchange [R][N2][N1 + 1], and r rows [2][R][M] for
     // the fused dot
     const size_t sm = sizeof(cplx<T>) * (size_t)(2 * R * p.nzp + R * N2 * (N1 + 1) + (a.reduce ? 2 * R * M : 0));
-    cudaError_t  e  = allow_max_dyn_smem(k_z_inv_reg<T, N1, N2, R>);
+    auto        fn = a.reduce ? k_z_inv_reg<T, N1, N2, R, true> : k_z_inv_reg<T, N1, N2, R, false>;
+    cudaError_t e  = allow_max_dyn_smem(fn);
     if (e != cudaSuccess)
         return e;
     // persistent: as many CTAs per SM as fit (at least two), at most one per block of rows
     static int occ[2] = {0, 0};
     int       &oc     = occ[a.reduce ? 1 : 0];
     if (!oc) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, k_z_inv_reg<T, N1, N2, R>, R * N1, sm) != cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, fn, R * N1, sm) != cudaSuccess)
             oc = 2;
         oc = oc < 2 ? 2 : oc;
     }
     const int grid = (int)(nblk < (long long)oc * nsm ? nblk : (long long)oc * nsm);
-    k_z_inv_reg<T, N1, N2, R><<<grid, R * N1, sm, st>>>(p, a);
+    fn<<<grid, R * N1, sm, st>>>(p, a);
     return cudaSuccess;
 }
 
