@@ -70,8 +70,9 @@ __device__ void conv_dot_finish(const double (&dk)[kMaxRhs], const ConvPlan<T> &
 }
 
 // ------------------------------------------------------------------ y pass ---
+// FP32 tiles of 256 threads: registers for five CTAs per SM (the inverse pass would take four)
 template <typename T, int N1, int N2, bool INV, int KC>
-__global__ void __launch_bounds__(KC * N1) k_y_reg(ConvPlan<T> p)
+__global__ void __launch_bounds__(KC * N1, (sizeof(T) == 4 && KC * N1 == 256) ? 5 : 1) k_y_reg(ConvPlan<T> p)
 {
     constexpr int n = N1 * N2;
     __shared__ cplx<T> S[n * KC];

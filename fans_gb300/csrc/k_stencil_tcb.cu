@@ -483,17 +483,25 @@ __global__ void __launch_bounds__(TPB, 3)
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             float out[NCOL]; // K_ph u_e = sum_b cf_b D_b, two rows per packed FP32x2 instruction
+            // the first two 16-column loads share one wait, the rest wait one at a time
+            constexpr int NLD0 = Cfg::NW >= 32 ? 2 : 1;
+            float         vv[16 * NLD0];
+#pragma unroll
+            for (int h = 0; h < NLD0; ++h)
+                tmem_ld16(lane_base + (uint32_t)(COL_D + 16 * h), vv + 16 * h);
 #pragma unroll
             for (int c0 = 0; c0 < Cfg::NW; c0 += 16) {
-                float vv[16];
-                tmem_ld16(lane_base + (uint32_t)(COL_D + c0), vv);
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                float *vc = c0 < 16 * NLD0 ? vv + c0 : vv;
+                if (c0 >= 16 * NLD0)
+                    tmem_ld16(lane_base + (uint32_t)(COL_D + c0), vc);
+                if (c0 == 0 || c0 >= 16 * NLD0)
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
                 for (int jj = 0; jj < 16; jj += 2) { // NCOL is even: a pair never straddles two blocks
                     const int col = c0 + jj, bb = col / NCOL, r = col % NCOL;
                     if (col < Cfg::NROW) {
                         const float  c1 = cf[bb < NB ? bb : 0];
-                        const float2 v2 = make_float2(vv[jj], vv[jj + 1]);
+                        const float2 v2 = make_float2(vc[jj], vc[jj + 1]);
                         const float2 o2 = bb == 0 ? __fmul2_rn(make_float2(c1, c1), v2)
                                                   : __ffma2_rn(make_float2(c1, c1), v2, make_float2(out[r], out[r + 1]));
                         out[r]     = o2.x;
