@@ -272,11 +272,11 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
 // ------------------------------------------- x pass + Green's op, TMA-fed ---
 // FP32 form of the x pass with its inputs brought in by the tensor memory
 // accelerator.  Persistent: CTA b takes a contiguous share of the jobs
-// (tile, RHS), tile = (ky, KX kz columns), and keeps two job buffers in flight.
-// A job's [C][nx][KX] spectrum tile arrives by one tensor-map copy per component
-// and completes on its buffer's mbarrier; the copy of job q + 2 is issued as
-// soon as every thread has read job q's buffer, so the reads run two jobs ahead
-// of the transforms.  The tile's Green's slice [nx][KX][NT] arrives the same
+// (tile, RHS), tile = (ky, KX kz columns), and keeps two job buffers.  A job's
+// [C][nx][KX] spectrum tile arrives by one tensor-map copy per component and
+// completes on its buffer's mbarrier; the buffer then serves as the job's inverse
+// exchange, and the copy of job q + 1 into the other buffer is issued at job q's
+// first barrier, so the reads run one job ahead of the transforms.  The tile's Green's slice [nx][KX][NT] arrives the same
 // way, issued when the previous tile's last job has applied its slice.  The
 // Green multiply is fused into the load of the inverse transform (each thread
 // forms its component's row of G . F for its own kx), and the twiddles of a
@@ -436,10 +436,10 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
 #pragma unroll
         for (int j2 = 0; j2 < N2; ++j2)
             v[j2] = Bc[(w + N1 * j2) * KX + l];
-        __syncthreads(); // the buffer is read (and F is free)
-        if (t == 0 && q + 2 < nq && !*abort_flag) {
+        __syncthreads(); // the buffer is read, F is free, and job q - 1 is done with its buffer
+        if (t == 0 && q >= 1 && q + 1 < nq && !*abort_flag) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_job(q + 2);
+            issue_job(q + 1); // into the buffer job q - 1 used for its inverse exchange
         }
         Dft<float, N2, false>::run(v);
 #pragma unroll
@@ -491,11 +491,17 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
             for (int q = 0; q < kMaxRhs; ++q)
                 if (q == k)
                     dk[q] += (double)((float)dot_weight(kz0 + l, p.M) * dsum);
-        __syncthreads(); // F and the Green's slice are read
-        if (t == 0 && last_of_tile && q + 1 < nq && !*abort_flag) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_green(q + 1);
+        // the inverse exchange goes to this job's input buffer (read by every component before
+        // the first barrier), so the Green's reads of F need no barrier after them; only the
+        // refill of the Green's slice waits for them, on a tile's last job
+        if (last_of_tile) {
+            __syncthreads();
+            if (t == 0 && q + 1 < nq && !*abort_flag) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_green(q + 1);
+            }
         }
+        cplx<float> *Xc = Bf + ((size_t)b * C + comp) * n * KX;
         // inverse FFT along x
         Dft<float, N2, true>::run(v);
 #pragma unroll
@@ -506,12 +512,12 @@ __global__ void __launch_bounds__(C * kTmaKC * N1, 1)
         }
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2)
-            Fc[(k2 * N1 + w) * KX + l] = v[k2];
+            Xc[(k2 * N1 + w) * KX + l] = v[k2];
         comp_bar();
         if (w < N2) {
 #pragma unroll
             for (int j1 = 0; j1 < N1; ++j1)
-                u[j1] = Fc[(w * N1 + j1) * KX + l];
+                u[j1] = Xc[(w * N1 + j1) * KX + l];
             Dft<float, N1, true>::run(u);
             if (valid) {
                 cplx<float> *gb = p.spec + k * rhs_spec + ((long long)comp * n * ny + ky) * p.nzp + kz0 + l;
