@@ -270,7 +270,6 @@ int make_plan(fansgpu_ctx *ctx, ConvPlan<T> &p, cplx<T> *spec, cplx<T> *tw, T *G
     p.use_reg = conv_reg_supported(g) ? 1 : 0;
     p.nrhs    = 1;
     p.fuse_zy = 0;
-    p.zf_bulk = 0;
     p.spectral_dot = 0;
     p.active  = nullptr;
     p.tma     = nullptr;
@@ -1062,13 +1061,11 @@ int autotune(fansgpu_ctx *ctx)
     ctx->tuned       = true;
     const bool mixed = ctx->desc.precision == FANSGPU_MIXED;
     auto apply = [&](const TuneChoice &c) {
-        ctx->cp64.var_z = c.v64[0] & 1; // the fused z + y forward pass (bit 1) and the TMA-fed
-        ctx->cp64.var_y = c.v64[1];     // x pass (2) are FP32 only
-        ctx->cp64.var_x = c.v64[2] == 2 ? 0 : c.v64[2];
+        ctx->cp64.var_z = c.v64[0] & 1; // the fused z + y forward pass (bit 1) is FP32 only
+        ctx->cp64.var_y = c.v64[1];
+        ctx->cp64.var_x = std::min(c.v64[2], 1); // the TMA-fed x pass (2) is FP32 only
         ctx->cp32.var_z = c.v32[0] & 1;
         ctx->cp32.fuse_zy = (c.v32[0] & 2) && zy_supported(ctx->g) ? 1 : 0;
-        ctx->cp64.zf_bulk = (c.v64[0] >> 2) & 1; // the persistent bulk-copy forward z pass (bit 2)
-        ctx->cp32.zf_bulk = (c.v32[0] >> 2) & 1;
         ctx->cp32.var_y = c.v32[1];
         ctx->cp32.var_x = (c.v32[2] == 2 && !ctx->cp32.tma) ? 0 : c.v32[2];
         if (c.tc_slower && ctx->use_tc) {
@@ -1107,7 +1104,6 @@ int autotune(fansgpu_ctx *ctx)
         c.v64[0] = ctx->cp64.var_z;
         c.v64[1] = ctx->cp64.var_y;
         c.v64[2] = ctx->cp64.var_x;
-        c.v64[0] += 4 * ctx->cp64.zf_bulk;
         if (mixed) {
             ConvPlan<float> tp = ctx->cp32; // r32, Kd32 and the spectrum hold every RHS
             tp.nrhs            = rhs_tuned;
@@ -1116,7 +1112,6 @@ int autotune(fansgpu_ctx *ctx)
             c.v32[0] = tp.var_z + 2 * tp.fuse_zy;
             c.v32[1] = tp.var_y;
             c.v32[2] = tp.var_x;
-            c.v32[0] += 4 * tp.zf_bulk;
             if (ctx->use_tc && ctx->tune == 3)
                 c.tc_slower = time_mixed_operator(ctx, false) < time_mixed_operator(ctx, true) ? 1 : 0;
         }
@@ -1917,8 +1912,8 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
             ctx->tune = 0;
         else if (std::strcmp(ev, "all") == 0)
             ctx->tune = 3;
-        else if (std::strlen(ev) == 3 && std::strchr("01234567", ev[0]) && std::strchr("01", ev[1]) &&
-                 std::strchr("0123", ev[2])) {
+        else if (std::strlen(ev) == 3 && std::strchr("0123", ev[0]) && std::strchr("01", ev[1]) &&
+                 std::strchr("012", ev[2])) {
             ctx->tune = 2;
             for (int k = 0; k < 3; ++k)
                 ctx->tune_force[k] = ev[k] - '0';
@@ -2194,8 +2189,7 @@ int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out)
     const ConvPlan<float>  &b = ctx->cp32;
     // the FP64-accurate operator: of the FP64 CG iterations, else of the mixed path's true residual
     const bool fp64_pipe = ctx->desc.precision != FANSGPU_MIXED && !(ctx->fp64_df && ctx->all_linear && !ctx->vscale);
-    const int32_t v[8] = {a.var_z + 4 * a.zf_bulk, a.var_y, a.var_x, b.var_z + 2 * b.fuse_zy + 4 * b.zf_bulk,
-                          b.var_y, b.var_x,
+    const int32_t v[8] = {a.var_z, a.var_y, a.var_x, b.var_z + 2 * b.fuse_zy, b.var_y, b.var_x,
                          ctx->use_tcb ? 2 : ctx->use_tc ? 1 : 0, fp64_pipe ? 0 : ctx->use_tcx ? 2 : 1};
     for (int k = 0; k < 8; ++k)
         out[k] = v[k];

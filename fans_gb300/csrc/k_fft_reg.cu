@@ -28,7 +28,6 @@ struct Tiles {
     static constexpr int cs   = (int)sizeof(cplx<T>);
     static constexpr int y[2] = {128 / cs, 64 / cs};
     static constexpr int x[2] = {64 / cs, 32 / cs > 1 ? 32 / cs : 2};
-    static constexpr int xw   = 128 / cs; // x variant 3: 128-byte rows, one CTA per SM at 256^3
     static constexpr int z[2] = {sizeof(T) == 4 ? 256 : 128, sizeof(T) == 4 ? 128 : 64};
 };
 
@@ -113,9 +112,7 @@ __global__ void __launch_bounds__(KC * N1, (sizeof(T) == 4 && KC * N1 == 256) ? 
 // store phases.
 template <typename T, int KC>
 struct KXCtas { // resident CTAs per SM the register budget is set for
-    static constexpr int value = KC * (int)sizeof(cplx<T>) >= 128                      ? 1
-                                 : (sizeof(T) == 4 && KC * (int)sizeof(cplx<T>) <= 32) ? 4
-                                                                                        : 2;
+    static constexpr int value = (sizeof(T) == 4 && KC * (int)sizeof(cplx<T>) <= 32) ? 4 : 2;
 };
 
 template <typename T, int N1, int N2, int C, int KC>
@@ -603,119 +600,6 @@ __global__ void __launch_bounds__(R * N1) k_z_fwd_reg(ConvPlan<T> p, const T *__
         }
 }
 
-// ------------------------------------------------- z fwd, bulk-copy fed ---
-// Persistent form of k_z_fwd_reg: each CTA loops over blocks of R rows, and a
-// block's rows of r (contiguous, R * nz values) arrive by one bulk async copy
-// into one of two buffers, completing on that buffer's mbarrier; the copy of the
-// next block is issued before the current one is transformed.  Transforms and
-// unpack are those of k_z_fwd_reg.  Waits are bounded as in the z-inverse pass.
-template <typename T, int N1, int N2, int R>
-__global__ void __launch_bounds__(R * N1, 2) k_z_fwd_bulk(ConvPlan<T> p, const T *__restrict__ r, CgScalars *scal)
-{
-    constexpr int M = N1 * N2, EP = N1 + 1;
-    extern __shared__ __align__(16) unsigned char zsm[];
-    cplx<T>                         *In = reinterpret_cast<cplx<T> *>(zsm); // [2][R*M]
-    cplx<T>                         *E  = In + 2 * R * M;                   // [R*N2*EP]
-    cplx<T>                         *Z  = E + R * N2 * EP;                  // [R*M]
-    __shared__ __align__(8) uint64_t zbar[2];
-    __shared__ int                   s_abort;
-    volatile int                    *abort_flag = &s_abort;
-    const int       t = threadIdx.x, L = t / N1, w = t % N1;
-    const long long rpr   = (long long)p.C * p.g.nx * p.g.ny; // rows per right-hand side
-    const long long nrows = rpr * p.nrhs;
-    const long long nblk  = (nrows + R - 1) / R;
-    const uint32_t  bar0  = (uint32_t)__cvta_generic_to_shared(&zbar[0]);
-    if (t == 0) {
-        s_abort = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    // a block's rows belong to at most two right-hand sides (R <= 64 rows, every RHS >= 256 rows)
-    auto rhs_on = [&](long long row) { return !p.active || p.active[(int)(row / rpr)]; };
-    auto live   = [&](long long blk) {
-        const long long last = min(blk * R + R, nrows) - 1;
-        return rhs_on(blk * R) || rhs_on(last);
-    };
-    int  waited[2] = {0, 0}, sent[2] = {0, 0};
-    auto fetch     = [&](long long blk, int b) {
-        if (t != 0 || blk >= nblk || !live(blk) || *abort_flag)
-            return;
-        ++sent[b];
-        const long long row0  = blk * R;
-        const int       nval  = (int)(nrows - row0 < R ? nrows - row0 : R);
-        const uint32_t  bytes = (uint32_t)(nval * M * sizeof(cplx<T>));
-        const uint32_t  bar   = bar0 + 8 * b;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        tma_expect(bar, bytes);
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         (uint32_t)__cvta_generic_to_shared(In + b * R * M)),
-                     "l"(reinterpret_cast<const cplx<T> *>(r) + row0 * M), "r"(bytes), "r"(bar)
-                     : "memory");
-    };
-    fetch(blockIdx.x, 0);
-    int it = 0;
-    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++it) {
-        const int b = it & 1;
-        fetch(blk + gridDim.x, b ^ 1);
-        if (!live(blk))
-            continue;
-        tma_bar_wait(bar0 + 8 * b, (uint32_t)(waited[b]++ & 1), abort_flag);
-        const long long row0 = blk * R;
-        // the block's rows: RHS k0 below row bnd, k0 + 1 from there (no per-value divisions)
-        const int       k0   = p.active ? (int)(row0 / rpr) : 0;
-        const long long bnd  = p.active ? (k0 + 1) * rpr : nrows;
-        cplx<T>         v[N2];
-#pragma unroll
-        for (int j2 = 0; j2 < N2; ++j2)
-            v[j2] = In[b * R * M + L * M + w + N1 * j2];
-        line_phase1<T, N1, N2, false>(v, w, p.tw_z);
-#pragma unroll
-        for (int k2 = 0; k2 < N2; ++k2)
-            E[(L * N2 + k2) * EP + w] = v[k2];
-        __syncthreads();
-        if (w < N2) {
-            cplx<T> u[N1];
-#pragma unroll
-            for (int j1 = 0; j1 < N1; ++j1)
-                u[j1] = E[(L * N2 + w) * EP + j1];
-            Dft<T, N1, false>::run(u);
-#pragma unroll
-            for (int k1 = 0; k1 < N1; ++k1)
-                Z[L * M + w + N2 * k1] = u[k1];
-        }
-        __syncthreads();
-        // unpack to the half spectrum, k = 0..M, coalesced over k
-        for (int i = t; i < R * (M + 1); i += blockDim.x) {
-            const int Lr = i / (M + 1), k = i % (M + 1);
-            const long long rw = row0 + Lr;
-            if (rw >= nrows || (p.active && !p.active[k0 + (rw >= bnd ? 1 : 0)]))
-                continue;
-            cplx<T> zk = Z[Lr * M + (k == M ? 0 : k)];
-            cplx<T> zm = Z[Lr * M + (k == 0 ? 0 : M - k)];
-            zm.y       = -zm.y;
-            cplx<T> Ev = {(T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y + zm.y)};
-            cplx<T> Od = {(T)0.5 * (zk.x - zm.x), (T)0.5 * (zk.y - zm.y)};
-            cplx<T> P  = cmul(p.tw_r2c[k], Od);
-            p.spec[(row0 + Lr) * p.nzp + k] = cplx<T>{Ev.x + P.y, Ev.y - P.x};
-        }
-        __syncthreads(); // In[b], E and Z are free
-    }
-    __syncthreads();
-    if (t == 0 && *abort_flag) {
-        for (int b = 0; b < 2; ++b)
-            if (sent[b] > 0)
-                for (unsigned n = 0;
-                     n < kTmaWaitLimit && !tma_bar_try(bar0 + 8 * b, (uint32_t)((sent[b] - 1) & 1)); ++n)
-                    ;
-        if (scal)
-            for (int q = 0; q < p.nrhs; ++q)
-                if (!p.active || p.active[q])
-                    scal[q].converged = -3;
-    }
-}
-
 // ------------------------------------------- fused z + y forward, cluster ---
 // r2c along z and the complex FFT along y of one (RHS, component, x) plane in one
 // pass, so the half spectrum after z is never written to and read back from HBM.
@@ -1113,29 +997,10 @@ cudaError_t go_x_tma(const ConvPlan<float> &p, const ConvArgs &a, cudaStream_t s
 }
 
 template <typename T, int N1, int N2, int R>
-void go_zf(const ConvPlan<T> &p, const T *r, CgScalars *scal, cudaStream_t st)
+void go_zf(const ConvPlan<T> &p, const T *r, cudaStream_t st)
 {
     const long long nrows = (long long)p.C * p.g.nx * p.g.ny * p.nrhs;
-    const long long nblk  = (nrows + R - 1) / R;
-    if (!p.zf_bulk) {
-        k_z_fwd_reg<T, N1, N2, R><<<(int)nblk, R * N1, 0, st>>>(p, r);
-        return;
-    }
-    constexpr int M  = N1 * N2;
-    const size_t  sm = sizeof(cplx<T>) * (size_t)(3 * R * M + R * N2 * (N1 + 1));
-    auto          fn = k_z_fwd_bulk<T, N1, N2, R>;
-    if (allow_max_dyn_smem(fn) != cudaSuccess)
-        return; // the launch below then reports the error
-    static int nsm = 0, occ = 0;
-    if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, R * N1, sm) != cudaSuccess || occ < 1)
-            occ = 1;
-    }
-    const int grid = (int)(nblk < (long long)occ * nsm ? nblk : (long long)occ * nsm);
-    fn<<<grid, R * N1, sm, st>>>(p, r, scal);
+    k_z_fwd_reg<T, N1, N2, R><<<(int)((nrows + R - 1) / R), R * N1, 0, st>>>(p, r);
 }
 
 template <typename T, int N1, int N2, int R>
@@ -1278,7 +1143,7 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
         }
     if (!fused)
         with_plan_z(p.M, [&]<int N1, int N2>() {
-            p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, a.scal, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, a.scal, st);
+            p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
         });
     mark(1);
     if (!fused)
@@ -1292,9 +1157,7 @@ cudaError_t launch_convolution_reg(const ConvPlan<T> &p, const ConvArgs &a, cuda
                 e = go_x_tma<N1, N2>(p, a, st);
                 return;
             }
-        e = p.var_x == 1   ? go_x<T, N1, N2, TL::x[1]>(p, a, st)
-            : p.var_x == 3 ? go_x<T, N1, N2, TL::xw>(p, a, st)
-                           : go_x<T, N1, N2, TL::x[0]>(p, a, st);
+        e = p.var_x == 1 ? go_x<T, N1, N2, TL::x[1]>(p, a, st) : go_x<T, N1, N2, TL::x[0]>(p, a, st);
     });
     if (e != cudaSuccess)
         return e;
@@ -1355,27 +1218,15 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
         t[v] = timed([&] {
             with_plan_z(p.M, [&]<int N1, int N2>() {
                 if (v) {
-                    go_zf<T, N1, N2, TL::z[1] / N1>(p, r, a.scal, st);
+                    go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st);
                     e = go_zi<T, N1, N2, TL::z[1] / N1>(p, az, st);
                 } else {
-                    go_zf<T, N1, N2, TL::z[0] / N1>(p, r, a.scal, st);
+                    go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
                     e = go_zi<T, N1, N2, TL::z[0] / N1>(p, az, st);
                 }
             });
         });
     p.var_z = t[1] < t[0] ? 1 : 0;
-    // the forward z pass of the chosen tile, per-block loads against the persistent bulk-copy form
-    float tz[2];
-    for (int v = 0; v < 2; ++v) {
-        p.zf_bulk = v;
-        tz[v]     = timed([&] {
-            with_plan_z(p.M, [&]<int N1, int N2>() {
-                p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, a.scal, st)
-                        : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, a.scal, st);
-            });
-        });
-    }
-    p.zf_bulk = tz[1] < tz[0] ? 1 : 0;
     for (int v = 0; v < 2; ++v)
         t[v] = timed([&] {
             with_plan(p.g.ny, [&]<int N1, int N2>() {
@@ -1383,9 +1234,9 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
             });
         });
     p.var_y = t[1] < t[0] ? 1 : 0;
-    // x: 64- and 32-byte rows, the TMA-fed pass (FP32 with tensor maps), 128-byte rows
-    float tx[4] = {1e30f, 1e30f, 1e30f, 1e30f};
-    for (int v = 0; v < 4; ++v) {
+    // x: 64- and 32-byte rows, the TMA-fed pass (FP32 with tensor maps)
+    float tx[3] = {1e30f, 1e30f, 1e30f};
+    for (int v = 0; v < 3; ++v) {
         if (v == 2 && !(std::is_same_v<T, float> && p.tma))
             continue;
         tx[v] = timed([&] {
@@ -1395,14 +1246,12 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
                         e = go_x_tma<N1, N2>(p, a, st);
                         return;
                     }
-                e = v == 1 ? go_x<T, N1, N2, TL::x[1]>(p, a, st)
-                  : v == 3 ? go_x<T, N1, N2, TL::xw>(p, a, st)
-                           : go_x<T, N1, N2, TL::x[0]>(p, a, st);
+                e = v ? go_x<T, N1, N2, TL::x[1]>(p, a, st) : go_x<T, N1, N2, TL::x[0]>(p, a, st);
             });
         });
     }
     p.var_x = 0;
-    for (int v = 1; v < 4; ++v)
+    for (int v = 1; v < 3; ++v)
         if (tx[v] < tx[p.var_x])
             p.var_x = v;
     // the forward z and y passes (the chosen variants) against the fused cluster pass
@@ -1411,7 +1260,7 @@ cudaError_t tune_convolution_reg(ConvPlan<T> &p, const T *r, T *s, CgScalars *sc
         if (zy_supported_impl(p.g)) {
             const float t_sep = timed([&] {
                 with_plan_z(p.M, [&]<int N1, int N2>() {
-                    p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, a.scal, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, a.scal, st);
+                    p.var_z ? go_zf<T, N1, N2, TL::z[1] / N1>(p, r, st) : go_zf<T, N1, N2, TL::z[0] / N1>(p, r, st);
                 });
                 with_plan(p.g.ny, [&]<int N1, int N2>() {
                     p.var_y ? go_y<T, N1, N2, false, TL::y[1]>(p, st) : go_y<T, N1, N2, false, TL::y[0]>(p, st);

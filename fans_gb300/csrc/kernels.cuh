@@ -222,7 +222,6 @@ struct ConvPlan {
     int            use_reg;        // register-resident passes (conv_reg_supported)
     int            var_z, var_y, var_x; // register passes: tile variant (0 default, 1 the alternative)
     int            fuse_zy;        // FP32: the forward z and y passes as one cluster pass (k_zy_fwd)
-    int            zf_bulk;        // the forward z pass persistent, rows by bulk async copies (k_z_fwd_bulk)
     // register passes: the fused <r, s> of a reducing convolution is taken in the x pass from the
     // spectra (Parseval) instead of in the z-inverse pass from r and s, which then reads no r
     int            spectral_dot;

@@ -206,10 +206,8 @@ int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *value
 /* The tile shapes and operators the context's first setup chose (autotuned
  * unless FANSGPU_TUNE=0 or forced), out[8]: out[0..2] = FP64 z, y, x pass
  * variants, out[3..5] the FP32 ones (0 = default tile, 1 = the smaller one;
- * x pass: 3 = 128-byte rows; FP32 x pass only: 2 = the persistent pass fed by
- * tensor-map (TMA) copies;
- * FP32 z entry: + 2 when the forward z and y passes run as one cluster pass;
- * z entries: + 4 when the forward z pass is the persistent bulk-copy one),
+ * FP32 x pass only: 2 = the persistent pass fed by tensor-map (TMA) copies;
+ * FP32 z entry: + 2 when the forward z and y passes run as one cluster pass),
  * out[6] = the mixed path's CG operator (0 CUDA cores, 1 per-phase tensor-core,
  * 2 exact-basis tensor-core), out[7] = the FP64-accurate operator (the FP64 CG
  * operator, and the mixed path's true residual: 0 FP64 pipe, 1 double-float on
