@@ -514,6 +514,12 @@ def main():
     else:
         launches = sum(c for _, c in ktimes.values()) + sum(
             (s["refinements"] + 1) + max(s["iterations"] - 1, 0) for s in stats)
+    # the operator either covers every RHS still iterating in one launch (k_stencil_tcb) or runs
+    # once per RHS (k_stencil_tc, "tc_per_rhs": a converged RHS's launch returns at once); its
+    # timing span covers the iteration's operator launches either way
+    op_per_rhs = ctx.tuning()["operator"] == "tc_per_rhs" and args.rhs > 1
+    if op_per_rhs:
+        launches += (args.rhs - 1) * ktimes.get("stencil", (0, 0))[1]
     # right-hand sides per iteration-kernel launch (the multi-RHS solve's launches
     # cover every RHS still iterating)
     rhs_iters_step = sum(iters)
@@ -547,15 +553,22 @@ def main():
         return algo_bytes(k, n, r=r_avg if k in ITER_KERNELS else 1.0)
 
     dom = max((k for k in ktimes if ktimes[k][1] > 0 and abytes(k) is not None), key=lambda k: ktimes[k][0])
-    avg_ms = ktimes[dom][0] / ktimes[dom][1]
-    achieved = abytes(dom) / (avg_ms * 1e-3) / 1e9
-    traffic = traffic_table().get((dom, n, args.rhs))  # ncu bytes of a launch with every RHS active
-    if traffic is not None and dom in ITER_KERNELS:
-        traffic = round(traffic * r_avg / args.rhs)     # the average launch of the step
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 3), "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": int(abytes(dom)), "avg_launch_ms": round(avg_ms, 4),
-                "rhs_per_launch": round(r_avg, 3) if dom in ITER_KERNELS else 1.0}
+    if dom == "stencil" and op_per_rhs:
+        # one launch per RHS: the launch's bytes are one RHS's, its time the span per active RHS
+        dom_bytes, avg_ms, r_dom = algo_bytes(dom, n, r=1.0), ktimes[dom][0] / (rhs_iters_step * args.steps), 1
+        traffic = traffic_table().get((dom, n, 1))
+        kname = "k_stencil_tc (one launch per RHS)"
+    else:
+        dom_bytes, avg_ms, r_dom = abytes(dom), ktimes[dom][0] / ktimes[dom][1], args.rhs
+        traffic = traffic_table().get((dom, n, args.rhs))  # ncu bytes of a launch with every RHS active
+        if traffic is not None and dom in ITER_KERNELS:
+            traffic = round(traffic * r_avg / args.rhs)     # the average launch of the step
+        kname = {"stencil": "k_stencil_tcb"}.get(dom, dom)
+    achieved = dom_bytes / (avg_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "kernel_name": kname, "achieved": round(achieved, 1), "peak": hbm,
+                "unit": "GB/s", "frac": round(achieved / hbm, 3), "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": int(dom_bytes), "avg_launch_ms": round(avg_ms, 4),
+                "rhs_per_launch": (round(r_avg, 3) if r_dom != 1 else 1.0) if dom in ITER_KERNELS else 1.0}
     per_kernel = {k: {"ms": round(v[0] / args.steps, 3), "launches": v[1] // args.steps,
                       "GBps": (round(abytes(k) * v[1] / (v[0] * 1e-3) / 1e9, 1) if v[1] and abytes(k) else None)}
                   for k, v in ktimes.items() if v[1]}

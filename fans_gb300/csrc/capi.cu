@@ -163,6 +163,9 @@ struct fansgpu_ctx {
     float *Wtb = nullptr, *coef_tb = nullptr;
     int    tb_nb = 0;
     bool   use_tcb = false;
+    // the multi-RHS iteration's operator as one per-phase k_stencil_tc launch per RHS (at most
+    // two phases; measured faster per RHS than k_stencil_tcb); FANSGPU_STENCIL=basis keeps tcb
+    bool   tcb_via_tc = false, tcb_basis_forced = false;
     // FP64-accurate basis operator on the tensor cores (k_stencil_tcx): double-float coefficients
     float *coef_tx  = nullptr;
     bool   use_tcx  = false;
@@ -503,8 +506,9 @@ int setup(fansgpu_ctx *ctx)
         }
         // the basis operators: every phase an isotropic law of this problem, each basis block exact.
         // k_stencil_tcb (FP32, mixed path) and k_stencil_tcx (FP64-accurate: true residual, FP64 CG)
-        ctx->use_tcb = false;
-        ctx->use_tcx = false;
+        ctx->use_tcb    = false;
+        ctx->use_tcx    = false;
+        ctx->tcb_via_tc = false;
         if (ctx->nstr == (C == 1 ? 3 : 6)) {
             const int iso = C == 1 ? FANSGPU_LAW_THERMAL_ISO : FANSGPU_LAW_ELASTIC_ISO, nb = C == 1 ? 1 : 2;
             bool      ok  = ctx->nph >= 1 && ctx->nph <= 256;
@@ -558,6 +562,7 @@ int setup(fansgpu_ctx *ctx)
                 ctx->use_tcb = ctx->tc_allowed && !ctx->tc_legacy && !ctx->tc_slower &&
                                ctx->desc.precision == FANSGPU_MIXED && stencil_tcb_supported(ctx->g, C, nb, ctx->nph);
                 ctx->use_tcx = ctx->exact_tc && stencil_tcx_supported(ctx->g, C, nb, ctx->nph);
+                ctx->tcb_via_tc = ctx->use_tcb && ctx->use_tc && ctx->Wtc && !ctx->tcb_basis_forced;
             }
         }
         {
@@ -1004,7 +1009,23 @@ cudaError_t enqueue_mixed_iteration_rhs(fansgpu_ctx *ctx, int cd)
     sa.rhs_stride  = n;
     sa.active      = ctx->act;
     int e0         = tk_mark(ctx);
-    e              = launch_stencil_tcb(sa, ctx->Wtb, ctx->coef_tb, ctx->tb_nb, ctx->st);
+    if (ctx->tcb_via_tc) {
+        // the single-RHS per-phase operator once per RHS (its fields at offset k * n, its scalars
+        // at scal[k]); a converged RHS's launch returns at once
+        for (int k = 0; k < ctx->nrhs && e == cudaSuccess; ++k) {
+            StencilArgs sk = sa;
+            sk.x           = ctx->s32 + k * n;
+            sk.d_old       = ctx->d32[cd] + k * n;
+            sk.d_new       = ctx->d32[cd ^ 1] + k * n;
+            sk.y           = ctx->Kd32 + k * n;
+            sk.scal        = ctx->scal + k;
+            sk.active      = ctx->act + k;
+            sk.nrhs        = 1;
+            sk.rhs_stride  = 0;
+            e              = launch_stencil_tc(sk, ctx->Wtc, ctx->nph, ctx->st);
+        }
+    } else
+        e = launch_stencil_tcb(sa, ctx->Wtb, ctx->coef_tb, ctx->tb_nb, ctx->st);
     if (e != cudaSuccess)
         return e;
     tk_span(ctx, FANSGPU_K_STENCIL, e0, tk_mark(ctx));
@@ -1903,9 +1924,10 @@ int fansgpu_create(const fansgpu_desc *desc, fansgpu_ctx **out)
 
     fansgpu_ctx *ctx = new fansgpu_ctx();
     ctx->desc        = *desc;
-    if (const char *ev = std::getenv("FANSGPU_STENCIL")) { // "simt": CUDA-core operator; "tc": per-phase 3xTF32
-        ctx->tc_allowed = std::strcmp(ev, "simt") != 0;
-        ctx->tc_legacy  = std::strcmp(ev, "tc") == 0;
+    if (const char *ev = std::getenv("FANSGPU_STENCIL")) { // "simt": CUDA-core operator; "tc": per-phase 3xTF32;
+        ctx->tc_allowed       = std::strcmp(ev, "simt") != 0; // "basis": the multi-RHS basis operator
+        ctx->tc_legacy        = std::strcmp(ev, "tc") == 0;
+        ctx->tcb_basis_forced = std::strcmp(ev, "basis") == 0;
     }
     if (const char *ev = std::getenv("FANSGPU_TUNE")) { // "0": default tiles; "all": + operator; "zyx": forced
         if (std::strcmp(ev, "0") == 0)
@@ -2190,7 +2212,7 @@ int fansgpu_tuning(fansgpu_ctx *ctx, int32_t *out)
     // the FP64-accurate operator: of the FP64 CG iterations, else of the mixed path's true residual
     const bool fp64_pipe = ctx->desc.precision != FANSGPU_MIXED && !(ctx->fp64_df && ctx->all_linear && !ctx->vscale);
     const int32_t v[8] = {a.var_z, a.var_y, a.var_x, b.var_z + 2 * b.fuse_zy, b.var_y, b.var_x,
-                         ctx->use_tcb ? 2 : ctx->use_tc ? 1 : 0, fp64_pipe ? 0 : ctx->use_tcx ? 2 : 1};
+                         ctx->use_tcb ? (ctx->tcb_via_tc ? 3 : 2) : ctx->use_tc ? 1 : 0, fp64_pipe ? 0 : ctx->use_tcx ? 2 : 1};
     for (int k = 0; k < 8; ++k)
         out[k] = v[k];
     return 0;

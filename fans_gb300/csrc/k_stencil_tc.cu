@@ -199,6 +199,10 @@ __device__ __forceinline__ void named_bar(int id, int nthreads)
 template <int C, int NPH>
 __global__ void __launch_bounds__(TPB, 3) k_stencil_tc(StencilArgs a, const float *__restrict__ Wg)
 {
+    // one RHS of a multi-RHS solve: a.active points at its flag, and a converged RHS is skipped
+    // by every CTA (before any barrier, tensor memory or reduction partial)
+    if (a.active && !*a.active)
+        return;
     using Cfg = TcCfg<C, NPH>;
     constexpr int NCOL = Cfg::NCOL, NPF = Cfg::NPF;
     extern __shared__ __align__(16) unsigned char smem[];

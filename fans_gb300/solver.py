@@ -199,11 +199,11 @@ class Context:
 
     def tuning(self):
         """fansgpu_tuning: {"fp64": (z, y, x), "fp32": (z, y, x), "tensor_core": bool,
-        "operator": "cuda" | "tc" | "tc_basis", "exact_operator": "fp64" | "df" | "tc_slices"}."""
+        "operator": "cuda" | "tc" | "tc_basis" | "tc_per_rhs", "exact_operator": "fp64" | "df" | "tc_slices"}."""
         out = np.zeros(8, dtype=np.int32)
         self._chk(self.lib.fansgpu_tuning(self.ctx, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
         return {"fp64": tuple(int(v) for v in out[:3]), "fp32": tuple(int(v) for v in out[3:6]),
-                "tensor_core": bool(out[6]), "operator": ("cuda", "tc", "tc_basis")[int(out[6])],
+                "tensor_core": bool(out[6]), "operator": ("cuda", "tc", "tc_basis", "tc_per_rhs")[int(out[6])],
                 "exact_operator": ("fp64", "df", "tc_slices")[int(out[7])]}
 
     def set_timing(self, on=True):

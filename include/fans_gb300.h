@@ -209,7 +209,8 @@ int fansgpu_set_voxel_field(fansgpu_ctx *ctx, int32_t field, const double *value
  * FP32 x pass only: 2 = the persistent pass fed by tensor-map (TMA) copies;
  * FP32 z entry: + 2 when the forward z and y passes run as one cluster pass),
  * out[6] = the mixed path's CG operator (0 CUDA cores, 1 per-phase tensor-core,
- * 2 exact-basis tensor-core), out[7] = the FP64-accurate operator (the FP64 CG
+ * 2 exact-basis tensor-core over all right-hand sides, 3 the per-phase tensor-core
+ * operator once per right-hand side of the multi-RHS iteration), out[7] = the FP64-accurate operator (the FP64 CG
  * operator, and the mixed path's true residual: 0 FP64 pipe, 1 double-float on
  * the CUDA cores, 2 exact fixed-point slices on the tensor cores).  New on the
  * GPU path (FANS's FFTW plans are chosen by FFTW_MEASURE, solver.h:221-222). */

@@ -22,11 +22,12 @@ pytestmark = pytest.mark.gpu
 
 
 def _solve(P, g0, simt, mode=None):
-    """mode: "tcb" (default operator: exact-basis tensor cores where it applies),
-    "tc" (per-phase 3xTF32 tensor-core operator) or "simt" (CUDA cores)."""
+    """mode: "tcb" (the exact-basis tensor-core operator where it applies), "default" (the
+    default choice: for at most two phases the per-phase operator once per RHS), "tc" (per-phase
+    3xTF32 tensor-core operator) or "simt" (CUDA cores)."""
     mode = mode or ("simt" if simt else "tc")
     old = os.environ.get("FANSGPU_STENCIL")
-    os.environ["FANSGPU_STENCIL"] = "" if mode == "tcb" else mode
+    os.environ["FANSGPU_STENCIL"] = {"tcb": "basis", "default": ""}.get(mode, mode)
     try:
         ctx = gpu_context(P, precision="mixed")
     finally:
@@ -76,12 +77,13 @@ def test_basis_operator_matches_cuda_core_and_per_phase_operators(c, groups, sha
     a = _solve(P, g0, False, "tcb")
     b = _solve(P, g0, True)
     t = _solve(P, g0, False, "tc")
-    for o in (a, b, t):
+    d = _solve(P, g0, False, "default")
+    for o in (a, b, t, d):
         assert o["st"]["converged"]
-    assert abs(a["st"]["iterations"] - b["st"]["iterations"]) <= 1
-    assert abs(a["st"]["iterations"] - t["st"]["iterations"]) <= 1
-    assert rel(a["stress"], b["stress"]) < 1e-9 and rel(a["stress"], t["stress"]) < 1e-9
-    assert rel(a["u"], b["u"]) < 1e-6
+    for o in (b, t, d):
+        assert abs(a["st"]["iterations"] - o["st"]["iterations"]) <= 1
+        assert rel(a["stress"], o["stress"]) < 1e-9
+    assert rel(a["u"], b["u"]) < 1e-6 and rel(a["u"], d["u"]) < 1e-6
     P.set_gradient(g0)
     P.solve(measure="L2", type="relative", tol=1e-8, n_it=500)
     assert rel(a["stress"], P.homogenized_stress()) < 1e-7
