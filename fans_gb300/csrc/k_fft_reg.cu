@@ -271,17 +271,20 @@ __global__ void __launch_bounds__(C * KC * N1, KXCtas<T, KC>::value) k_x_green_r
 // accelerator.  Persistent: CTA b takes a contiguous share of the jobs
 // (tile, RHS), tile = (ky, KX kz columns), and keeps two job buffers.  A job's
 // [C][nx][KX] spectrum tile arrives by one tensor-map copy per component and
-// completes on its buffer's mbarrier; the buffer then serves as the job's inverse
-// exchange, and the copy of job q + 1 into the other buffer is issued at job q's
-// first barrier, so the reads run one job ahead of the transforms.  The tile's Green's slice [nx][KX][NT] arrives the same
-// way, issued when the previous tile's last job has applied its slice.  The
-// Green multiply is fused into the load of the inverse transform (each thread
-// forms its component's row of G . F for its own kx), and the twiddles of a
-// worker live in registers.  The arithmetic per value is that of
-// k_x_green_reg, so both give the same spectrum bit for bit.  Every wait is
-// bounded: one that runs out sets an abort flag that releases the others, no
-// further copies are issued, the CTA waits (bounded) for the copies it has in
-// flight, and the status -3 goes to every active RHS's converged field.
+// completes on its buffer's mbarrier; the buffer then serves as the job's
+// inverse exchange, and the copy of job q + 1 into the other buffer is issued at
+// job q's first barrier, so the reads run one job ahead of the transforms.  The
+// tile's Green's slice [nx][KX][NT] arrives the same way, issued when the
+// previous tile's last job has applied its slice.  The Green multiply is fused
+// into the load of the inverse transform (each thread forms its component's row
+// of G . F for its own kx, and with the spectral dot also its share of <r, s>),
+// the twiddles of a worker live in registers, and the exchanges of one component
+// meet only its own warps (named barriers).  The operations per value are those
+// of k_x_green_reg; the compiler may contract them differently, so the two agree
+// to FP32 rounding.  Every wait is bounded: one that runs out sets an abort flag
+// that releases the others, no further copies are issued, the CTA waits
+// (bounded) for the copies it has in flight, and the status -3 goes to every
+// active RHS's converged field.
 constexpr int      kTmaKC        = 8;       // kz columns per tile: 64-byte rows of complex FP32
 constexpr unsigned kTmaWaitLimit = 1u << 22; // polls of one mbarrier wait
 
